@@ -1,0 +1,358 @@
+"""Benchmark of the kinematic scattering sum on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config nacl_screw_8m]
+
+One step = one full kinematic exposure of the workload: stage transform and
+incident amplitudes, species/Morton tiling, per-pixel prologue, the FP32
+split-phase sum and the FP64 reduction. `value` is measured with the atom
+positions already resident in HBM; `e2e` goes through the public entry point
+``beam.atomic_scattering_kinematic`` with host arrays (host->device copies and
+the device->host read of the field inside the timed region).
+
+The workload's data (positions + tiles, ~300 MB for 8.19M atoms) exceeds the
+129 MB L2, so no flush is needed between steps.
+
+N > 1 (torchrun): every rank runs its own replica of the workload (the path
+shards into independent exposures; there is no data-path collective) and
+`value` is the sum over ranks of terms / max-over-ranks time ("weak" scaling).
+
+--impl reference times the reference algorithm's CPU implementation on the
+host cores (the C restatement in oracle/, all threads) on a bounded sample
+of the same workload, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
+MUFU_PER_CLK_SM = 16        # sin/cos results per clock per SM (MUFU)
+FP32_PER_CLK_SM = 128
+MUFU_PER_TERM, FP32_PER_TERM = 2, 12   # canonical split-phase term
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(PEAKS_FILE) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def _central_subset(det_shape, m):
+    ny, nz = det_shape
+    iy0, iz0 = (ny - m) // 2, (nz - m) // 2
+    iy, iz = np.meshgrid(np.arange(iy0, iy0 + m), np.arange(iz0, iz0 + m))
+    return (iz * ny + iy).ravel()
+
+
+def cpu_baseline(w, chunks=4, m=32, threads=None, reps=1):
+    """The oracle (C, FP64, reference algorithm) on host cores: `chunks` sample
+    chunks x a central m x m pixel subset."""
+    import oracle
+    B = w.beam
+    threads = threads or os.cpu_count() or 1
+    sel = _central_subset(w.detector.shape, m)
+    coords = np.asarray(w.detector.pixel_coordinates)[:, sel]
+    ch = []
+    for cid in range(1, min(chunks, w.sample.chunk_total) + 1):
+        ch.append((w.sample.load_chunk_positions(cid), w.sample.load_chunk_species(cid)))
+    n_atoms = sum(c[0].shape[0] for c in ch)
+    labels = sorted({str(x) for c in ch for x in np.unique(c[1])})
+    f0z = {e: B.tables.f0_zero(e) for e in labels}
+    args = (ch, coords, (m, m), w.stage.rotation, w.stage.translation, B._energy, B.tables.f0,
+            f0z, B.tables.f1f2, B._beam_E0_map, B._beam_grid(), B._polarization_state())
+    kw = dict(apply_polarization=w.sc_kwargs.get("apply_polarization", False),
+              spherical_decay=w.sc_kwargs.get("spherical_decay", False),
+              remove_forward=w.sc_kwargs.get("remove_forward", False), n_threads=threads)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.interact_cpu(*args, **kw)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    terms = float(n_atoms) * m * m
+    return {"value": terms / best / 1e9, "unit": "Gatom*pixel/s", "cores": int(threads),
+            "kind": "port",
+            "sample": f"{n_atoms} atoms ({len(ch)} of {w.sample.chunk_total} chunks) x central "
+                      f"{m}x{m} pixels, FP64 C restatement of the reference CPU kernel, "
+                      f"{threads} threads, {best:.2f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    from mosaic_gb300 import workloads
+    w = workloads.build(args.config)
+    threads = os.cpu_count() or 1
+    steps = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(w, chunks=1, m=16, threads=threads)
+        if i >= args.warmup:
+            steps.append(r)
+    val = float(np.median([s["value"] for s in steps]))
+    line = {"impl": "reference", "metric": "Gatom*pixel/s (kinematic sum)", "value": val,
+            "unit": "Gatom*pixel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.config, "host_cores": threads},
+            "cpu_baseline": {"value": val, "unit": "Gatom*pixel/s", "cores": threads,
+                             "kind": "port", "sample": steps[-1]["sample"]},
+            "e2e": {"value": val, "unit": "Gatom*pixel/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from mosaic_gb300 import autotune, engine, workloads
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    w = workloads.build(args.config)
+    B = w.beam
+    kw = w.sc_kwargs
+    phys = B.physics(kw["apply_polarization"], kw["spherical_decay"], kw["remove_forward"])
+    pos_h, idx_h, labels = B.collect_atoms(w.sample)
+    table = engine.SpeciesTable.build(labels, B.tables, B._energy, B._debye_waller)
+    pos_d = torch.as_tensor(pos_h).to(dev)             # resident inputs
+    idx_d = torch.as_tensor(idx_h.astype(np.int32)).to(dev)
+    counts = np.bincount(idx_h, minlength=len(labels)).astype(np.int64)
+    coords_m = np.asarray(w.detector.pixel_coordinates, dtype=np.float64) / 1e10
+    coords_d = torch.as_tensor(coords_m).to(dev)
+    ny, nz = w.detector.shape
+    n_atoms, n_pix = pos_h.shape[0], ny * nz
+    terms = float(n_atoms) * n_pix
+
+    # Launch shape: autotune once on a probe, cached on disk.
+    atoms = engine.atoms_lab(pos_d, idx_h, w.stage.rotation, w.stage.translation, table,
+                             e0=B._beam_E0_map, grid=B._beam_grid(), device=dev)
+    tiles = engine.Tiles(atoms, B.k, B._kernel_tile_atoms, device=dev)
+    pix = engine.Pixels(coords_m, ny, nz, phys, device=dev)
+    third, fresnel, tol, diag = B.split_budget(tiles, pix.r0_min())
+    launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel))
+    B._kernel_launch = launch
+    amp_real = tiles.amp_is_real()
+    split_times = []
+
+    def step(record=False):
+        a = engine.atoms_lab(pos_d, idx_d, w.stage.rotation, w.stage.translation, table,
+                             e0=B._beam_E0_map, grid=B._beam_grid(), device=dev, counts=counts)
+        t = engine.Tiles(a, B.k, B._kernel_tile_atoms, device=dev)
+        p = engine.Pixels(coords_d, ny, nz, phys, device=dev)
+        if record:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+        out = engine.run_split(t, p, phys, table, launch=launch, fresnel=int(fresnel),
+                               amp_real=amp_real)
+        if record:
+            e1.record()
+            split_times.append((e0, e1))
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    sampler = ClockSampler(local)
+    with sampler:
+        barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(args.steps):
+            out = step(record=True)
+        ev1.record()
+        barrier()
+    engine.sync()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    split_ms = float(np.mean([a.elapsed_time(b) for a, b in split_times]))
+    value = terms * world / (ms * 1e-3) / 1e9
+    clocks = sampler.summary()
+
+    # End to end through the public entry point with host buffers.
+    e2e_times = []
+    for i in range(max(2, min(3, args.steps))):
+        barrier()
+        t0 = time.perf_counter()
+        field = B.atomic_scattering_kinematic(w.sample, w.detector, w.stage, return_double=True,
+                                              **kw)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e_times))
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = pos_h.nbytes + idx_h.astype(np.int32).nbytes + B._beam_E0_map.nbytes + coords_m.nbytes
+    d2h = n_pix * 16
+
+    # FP64 plain (same GPU) on the central pixel subset: speed bar and error.
+    m = args.fp64_subset
+    sel = _central_subset(w.detector.shape, m)
+    pix_s = engine.Pixels(coords_m[:, sel], m, m, phys, device=dev)
+    a = engine.atoms_lab(pos_d, idx_h, w.stage.rotation, w.stage.translation, table,
+                         e0=B._beam_E0_map, grid=B._beam_grid(), device=dev)
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    ref = engine.run_plain(a, pix_s, phys)
+    f1.record()
+    engine.sync()
+    fp64_s = f0.elapsed_time(f1) * 1e-3
+    fp64_rate = float(n_atoms) * m * m / fp64_s / 1e9
+    I_ref = (ref ** 2).sum(1).cpu().numpy()
+    I_out = (np.abs(field.reshape(-1)[sel]) ** 2)
+    rel_err = float(np.abs(I_out - I_ref).max() / I_ref.max())
+    l2_err = float(np.linalg.norm(I_out - I_ref) / np.linalg.norm(I_ref))
+
+    peaks, peak_src = _peaks()
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    clk = float(peaks.get("sm_max_mhz", 2070.0))
+    peak_terms = min(MUFU_PER_CLK_SM / MUFU_PER_TERM, FP32_PER_CLK_SM / FP32_PER_TERM) * n_sm * clk * 1e6
+    achieved = terms / (split_ms * 1e-3)
+    gpu_launches = args.steps * 8
+
+    if rank == 0:
+        cpu = cpu_baseline(w) if not args.no_cpu else None
+        line = {
+            "metric": "Gatom*pixel/s (kinematic sum, FP32 split-phase) vs FP64 plain on 1 GB300",
+            "value": value, "unit": "Gatom*pixel/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 origins and reduction)",
+            "data": "synthetic",
+            "config": {"workload": args.config, "atoms": n_atoms, "pixels": n_pix,
+                       "terms_per_step": terms, "tile_atoms": B._kernel_tile_atoms,
+                       "launch": launch, "fresnel_term": bool(fresnel),
+                       "l2": "inputs larger than L2 (positions + tiles ~300 MB); no flush",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": terms * world / e2e_s / 1e9, "unit": "Gatom*pixel/s",
+                    "seconds": e2e_s, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": gpu_launches,
+            "roofline": {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak_terms / 1e9,
+                         "unit": "Gterm/s", "frac": achieved / peak_terms, "traffic": None,
+                         "peak_source": f"{MUFU_PER_CLK_SM} sin/cos per clk per SM / 2 per term x "
+                                        f"{n_sm} SMs x {clk:.0f} MHz ({peak_src} max clock)",
+                         "split_kernel_ms": split_ms},
+            "fp64_plain": {"value": fp64_rate, "unit": "Gatom*pixel/s",
+                           "subset": f"central {m}x{m} pixels, all atoms",
+                           "speedup_fp32_vs_fp64": (achieved / 1e9) / fp64_rate},
+            "accuracy": {"rel_err_max_over_peak": rel_err, "rel_err_l2": l2_err,
+                         "reference": f"FP64 plain GPU kernel, central {m}x{m} pixels",
+                         "budget": 1e-4},
+            "split_budget": {k: float(v) for k, v in diag.items()},
+            "autotune": [[float(t), c] for t, c in tune_tbl] if tune_tbl else [],
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="nacl_screw_8m")
+    ap.add_argument("--fp64-subset", type=int, default=32)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

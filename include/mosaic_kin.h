@@ -1,0 +1,176 @@
+/*
+ * mosaic_kin.h -- C ABI of the GB300 (sm_103a) kinematic scattering library
+ * libmosaic_kin.so.
+ *
+ * The library computes, for every detector pixel P, the near-field kinematic
+ * sum of the MOSAIC reference (Beam.py:663-816, the per-term arithmetic of
+ * `compute_scattering_cffi`):
+ *
+ *   A(P) = r_e sum_a E_in(a) [f0_s(Q) + f'_s + i f''_s] [exp(-B_s s^2)]
+ *          [sqrt(Pol)] [R0/r] exp(i k (b.a + |P - a|))
+ *
+ * with b the incident direction (+x in the lab frame). Two kernels:
+ *   - mk_kin_plain_f64: the FP64 direct sum, term for term as the reference
+ *     CPU kernel (drop-in and on-device oracle);
+ *   - mk_kin_split_f32: the FP32 split-phase sum over Morton-ordered atom
+ *     tiles with FP64 tile origins, Kahan-compensated across tiles and an
+ *     FP64 cross-slice reduction.
+ *
+ * Conventions
+ *   - Every pointer documented as "device" is a CUDA device pointer owned by
+ *     the caller; "host" pointers are read during the call only.
+ *   - Pixel index p = iz * ny + iy (Detector.py:204-214).
+ *   - Calls are stream-ordered on `stream` (a cudaStream_t, NULL = default)
+ *     and return before the GPU work finishes; mk_sync_status() waits and
+ *     reports device-side errors.
+ *   - Return value: MK_OK or a negative MK_E* code; mk_last_error() gives a
+ *     message (thread-local). Nothing aborts, exits or traps.
+ *   - Scratch: entry points that need scratch take a `workspace` of at least
+ *     the bytes the matching *_workspace_size() query returns.
+ */
+#ifndef MOSAIC_KIN_H
+#define MOSAIC_KIN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MK_OK 0
+#define MK_EINVAL (-1)   /* bad argument (the reference raises ValueError) */
+#define MK_ENOMEM (-2)   /* workspace too small (the reference raises MemoryError) */
+#define MK_ETIMEOUT (-3) /* a bounded device-side wait ran out */
+#define MK_EDECLINE (-4) /* the FP32 path cannot meet its error budget here */
+#define MK_ECUDA (-5)    /* CUDA runtime error */
+
+#define MK_MAX_SPECIES 16
+
+/* Per-species scattering data (host arrays, n_species <= MK_MAX_SPECIES).
+ * Replaces the per-atom tables the reference builds in
+ * cpu_scatter_chunk_cffi (Beam.py:5671-5691) and _species_rows
+ * (Beam.py:1345-1357). */
+typedef struct {
+    int n_species;
+    const float *wk;       /* (S, 11) Waasmaier-Kirfel a1..a5 c b1..b5 */
+    const float *f0_zero;  /* (S) f0 at Q = 0 */
+    const float *anom_re;  /* (S) f'  at the beam energy */
+    const float *anom_im;  /* (S) f'' at the beam energy */
+    const float *dw_b;     /* (S) Debye-Waller B [A^2]; NULL = no factor */
+} mk_species;
+
+/* Physics switches, the flags of compute_scattering_cffi (Beam.py:631-651). */
+typedef struct {
+    double k;             /* 2 pi / lambda [1/m] */
+    double beam_dir[3];   /* unit incident direction in the frame of atoms and pixels */
+    int apply_pol;        /* multiply by sqrt(P_pol) */
+    double pol_deg;       /* degree of linear polarization p */
+    double pol_e[3];      /* its unit vector (same frame) */
+    int spherical_decay;  /* multiply by R0 / r */
+    int remove_forward;   /* subtract f(0) where Q < Q_cut(pixel) */
+} mk_physics;
+
+/* Per-pixel derived data, device arrays of length n_pix, filled by
+ * mk_pixels_prepare (replaces the per-pixel prologue of Beam.py:716-746 and
+ * pixel_phasor, Beam.py:9241-9255). */
+typedef struct {
+    int ny, nz;           /* detector shape; n_pix = ny * nz */
+    const double *xyz;    /* device (3, n_pix) pixel coordinates [m] */
+    double *r0;           /* device (n_pix) |P| */
+    double *qcut;         /* device (n_pix) forward-removal cut-off Q_cut [1/m] */
+    double *qc;           /* device (3, n_pix) (k / 2 pi)(b - u_hat) [cycles/m] */
+    float *uf;            /* device (4, n_pix) u_hat (x, y, z) and 1/|P| as float */
+    double *phasor;       /* device (2, n_pix) exp(i k |P|) */
+} mk_pixels;
+
+/* Atom tiles for the split-phase kernel, filled by mk_tiles_build. Tiles
+ * hold `tile_atoms` atoms of one species (the last tile of a species is
+ * padded with zero-amplitude atoms). */
+typedef struct {
+    int n_tiles;
+    int tile_atoms;       /* power of two, 128..4096 */
+    double *origin;       /* device (4, n_tiles): origin x, y, z [m], radius [m] */
+    int *species;         /* device (n_tiles) species index */
+    float *pos;           /* device (n_tiles*tile_atoms, 4): k/2pi (a - o) [cycles], |.|^2 */
+    float *amp;           /* device (n_tiles*tile_atoms, 2): incident amplitude */
+} mk_tiles;
+
+/* Launch shape of the split-phase kernel (autotuned by the host). */
+typedef struct {
+    int pix_per_thread;   /* 1, 2, 4 or 8 */
+    int threads;          /* 64, 128 or 256 */
+    int slices;           /* tile ranges summed separately, reduced in FP64; <= 0: auto */
+    int fresnel;          /* 1: keep the |d|^2 term of the in-tile distance; 0: drop it
+                             (the caller checks k r_tile^2 / 2 R0_min against its budget);
+                             -1: keep it */
+    int amp_real;         /* 1: every incident amplitude is real (skips two FMAs a term) */
+} mk_launch;
+
+/* --- library ---------------------------------------------------------- */
+int mk_version(void);
+const char *mk_last_error(void);
+/* Wait for `stream`, then report (and clear) any device-side error flag. */
+int mk_sync_status(void *stream);
+
+/* --- staging ---------------------------------------------------------- */
+/* Per-pixel prologue. Replaces the per-pixel set-up inside
+ * compute_scattering_cffi (Beam.py:716-746) and pixel_phasor (Beam.py:9241-9255). */
+int mk_pixels_prepare(const mk_pixels *px, const mk_physics *phys, void *stream);
+
+/* Stage transform and incident amplitude per atom. Replaces the float32
+ * `pos @ R.T + T` of interact_beam_gpu/cpu (Beam.py:6277-6280, 5896-5902)
+ * and ein_bilinear_kernel / _ein_bilinear_cpu with tau = phi = 0
+ * (Beam.py:2439-2578, 956-1045): E_in is E0 sampled bilinearly on the beam
+ * grid, 0 outside it.
+ *   pos_in:  device (n, 3) float32 [A] sample frame
+ *   rot, trans: host (9) row-major float32 rotation and (3) translation [A]
+ *   e0: device (grid_ny, grid_nz) complex64 beam map (NULL: amplitude 1)
+ *   grid: host du, dv, uc, vc (Beam.py:228-231)
+ *   pos_lab: device (n, 3) float64 [m] (float32 lab position / 1e10)
+ *   amp: device (n, 2) float32 */
+int mk_atoms_lab(int64_t n, const float *pos_in, const float *rot, const float *trans,
+                 const float *e0, int grid_ny, int grid_nz, const double *grid,
+                 double *pos_lab, float *amp, void *stream);
+
+/* Bytes of workspace mk_tiles_build needs for n atoms. */
+size_t mk_tiles_workspace_size(int64_t n);
+/* Species-partitioned Morton order and tile build. Replaces _partition,
+ * _morton_order_gpu, _chunk_origins_gpu and _stage (Beam.py:9297-9319,
+ * 1204-1300, 9265-9294) with tiles of `tiles->tile_atoms` atoms whose origin
+ * is the FP64 bounding-box centre.
+ *   pos: device (n, 3) float64 [m]; species: device (n) int32 in [0, S);
+ *   amp: device (n, 2) float32; counts: host (S) atoms per species.
+ *   tiles->n_tiles must equal sum_s ceil(counts[s] / tile_atoms). */
+int mk_tiles_build(int64_t n, const double *pos, const int *species, const float *amp,
+                   int n_species, const int64_t *counts, double k, mk_tiles *tiles,
+                   void *workspace, size_t ws_bytes, void *stream);
+
+/* --- sums ------------------------------------------------------------- */
+/* Bytes of workspace the sums need (partial fields of `slices` slices). */
+size_t mk_sum_workspace_size(int n_pix, int slices);
+
+/* FP64 plain direct sum, term for term as compute_scattering_cffi
+ * (Beam.py:748-808), added into (accumulate = 1) or written to `out`.
+ *   pos: device (n, 3) float64 [m]; species: device (n) int32; amp: device (n, 2)
+ *   out: device (2, n_pix) interleaved complex128 field (including r_e) */
+int mk_kin_plain_f64(int64_t n, const double *pos, const int *species, const float *amp,
+                     const mk_species *sp, const mk_physics *phys, const mk_pixels *px,
+                     int slices, double *out, int accumulate, void *workspace,
+                     size_t ws_bytes, void *stream);
+
+/* Slice count mk_kin_split_f32 will use for this launch (resolves
+ * launch->slices <= 0), so the caller can size the workspace. */
+int mk_split_plan(const mk_tiles *tiles, const mk_pixels *px, const mk_launch *launch,
+                  int *slices_out);
+
+/* FP32 split-phase sum over tiles (replaces the `mosaic_fast` kernel and its
+ * dispatch, Beam.py:8114-8632, 9362-9496). Same output convention. */
+int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *sp, const mk_physics *phys,
+                     const mk_pixels *px, const mk_launch *launch, double *out,
+                     int accumulate, void *workspace, size_t ws_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOSAIC_KIN_H */

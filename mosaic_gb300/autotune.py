@@ -1,0 +1,107 @@
+"""Autotuner for the split-phase kernel's launch shape.
+
+Candidates are (pixels per thread, threads per block); the slice count is
+then chosen inside the library to fill whole waves of the GPU. Each candidate
+is timed with CUDA events on a probe -- the first ``PROBE_TILES`` tiles
+against every pixel, the same per-term work as the full problem -- and the
+winner is cached per (device, detector-size bucket, tile size, kernel source
+hash) in a JSON file, like the
+reference's tune store (Beam.py:8871-8940, hardware.py:1048-1081).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import threading
+
+import torch
+
+from . import engine
+
+CANDIDATES = [(4, 128), (4, 256), (2, 256), (8, 128), (2, 128), (8, 64), (4, 64), (1, 256)]
+DEFAULT = dict(pix_per_thread=4, threads=128, slices=0)
+PROBE_TILES = 96
+_mem = {}
+_lock = threading.Lock()
+
+
+def _cache_path():
+    base = os.environ.get("MOSAIC_GB300_CACHE") or os.path.join(
+        os.path.expanduser("~"), ".cache", "mosaic_gb300")
+    return os.path.join(base, "tune.json")
+
+
+def _src_hash():
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "mk_sum_f32.cu")
+    with open(d, "rb") as fh:
+        return hashlib.sha1(fh.read()).hexdigest()[:12]
+
+
+def _key(n_pix, tiles):
+    dev = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
+    bucket = 1 << max(0, (int(n_pix) - 1).bit_length())
+    return f"{dev}|{bucket}|{tiles.tile_atoms}|{_src_hash()}"
+
+
+def _load():
+    try:
+        with open(_cache_path()) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(key, val):
+    with _lock:
+        d = _load()
+        d[key] = val
+        p = _cache_path()
+        try:
+            os.makedirs(os.path.dirname(p), exist_ok=True)
+            tmp = p + f".tmp{os.getpid()}"
+            with open(tmp, "w") as fh:
+                json.dump(d, fh, indent=1)
+            os.replace(tmp, p)
+        except OSError:
+            pass
+
+
+def lookup(n_pix, tiles):
+    key = _key(n_pix, tiles)
+    if key in _mem:
+        return dict(_mem[key])
+    d = _load().get(key)
+    if d:
+        _mem[key] = d
+        return dict(d)
+    return dict(DEFAULT)
+
+
+def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, reps=3):
+    """Time every candidate on a probe of the tiles; cache and return the winner."""
+    amp_real = tiles.amp_is_real() if amp_real is None else bool(amp_real)
+    probe = engine.TilesView(tiles, min(tiles.n_tiles, PROBE_TILES))
+    results = []
+    for pix_pt, nt in (candidates or CANDIDATES):
+        cfg = dict(pix_per_thread=pix_pt, threads=nt, slices=0)
+        try:
+            engine.run_split(probe, pix, phys, table, launch=cfg, fresnel=fresnel, amp_real=amp_real)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                engine.run_split(probe, pix, phys, table, launch=cfg, fresnel=fresnel,
+                                 amp_real=amp_real)
+            e1.record()
+            e1.synchronize()
+            results.append((e0.elapsed_time(e1) / reps, cfg))
+        except Exception:   # a shape that does not fit the SM is skipped
+            continue
+    if not results:
+        return dict(DEFAULT), []
+    best = min(results, key=lambda r: r[0])[1]
+    key = _key(pix.n, tiles)
+    _mem[key] = best
+    _store(key, best)
+    return dict(best), results

@@ -1,0 +1,351 @@
+"""``beam``: the drop-in for the reference's kinematic scattering entry point.
+
+Mirrors the public surface of MOSAIC's ``beam`` class that the kinematic path
+uses (Beam.py:59-310, 1047-1156, 6028-6496, 7771-7824): ``create_beam``,
+``set_wavefield``, ``set_phase_tolerance``, ``atomic_scattering_kinematic``,
+``interact_beam_gpu``, ``atomic_direct_interaction`` -- same arguments, same
+(Nz, Ny) complex64 result, same sample/detector/stage duck types and the same
+error behaviour (ValueError for a non-+x beam or size mismatches,
+MemoryError when scratch cannot be allocated).
+
+Arithmetic runs on the GPU in libmosaic_kin.so:
+  * ``_use_fast_kernel`` True (default): FP32 split-phase sum
+    (``mk_kin_split_f32``); it declines to the FP64 sum when the geometry
+    leaves its error budget (extreme near field), as the reference's fast
+    kernel declines to its general kernel (Beam.py:1376-1441).
+  * ``_use_fast_kernel`` False: FP64 plain sum (``mk_kin_plain_f64``), the
+    reference CPU kernel's arithmetic term for term.
+There is no CPU path: ``use_gpu=False`` and a missing GPU raise.
+"""
+from __future__ import annotations
+
+import hashlib
+import warnings
+
+import numpy as np
+import torch
+
+from . import engine
+from .geometry import polarization_from_rate, polarization_state
+from .tables import ScatteringTables, anomalous_at, f0_at_zero
+
+
+class beam:
+    """X-ray beam along +x and the kinematic scattering it produces."""
+
+    def __init__(self, directory=None, tables: ScatteringTables | None = None):
+        self.directory = directory
+        self._direction = None
+        self._energy = None
+        self._wavelength = None
+        self._pol_perp_rate = 0.5
+        self._pol_direction = None
+        self._pol_degree = None
+        self._h = 6.62607015e-34
+        self._c = 299792458
+        self._q = 1.602176634e-19
+        self._hq = self._h / self._q
+        self._phase_tol_rad = 1e-3
+        # FP32 path: phase budget for every dropped term of the split phase
+        # (the reference's _kernel_phase_tol_rad, Beam.py:1404-1406).
+        self._use_fast_kernel = True
+        self._kernel_phase_tol_rad = 1e-6
+        self._kernel_tile_atoms = 1024
+        self._kernel_launch = None          # None: autotuned
+        self._debye_waller = None           # element -> B [A^2]; None = no factor
+        self.tables = tables or ScatteringTables()
+        self.last_run = {}
+
+    # ------------------------------------------------------------ beam setup
+    def create_beam(self, energy, eV=True, beam_shape="rectangular", beam_size=(1000.0, 1000.0),
+                    beam_samples=(256, 256), beam_profile="uniform", gaussian_waist=None,
+                    pol_perp_rate=0.5, pol_direction=None, pol_degree=None):
+        """+x beam of the given energy and its transverse grid (Beam.py:151-218)."""
+        self._direction = np.array([1.0, 0.0, 0.0], dtype=np.float32)
+        if not eV:
+            energy = energy / self._q
+        self._energy = float(energy)
+        self._wavelength = self._hq * self._c / self._energy
+        k = 2.0 * np.pi / self._wavelength
+        self._kx_scalar = np.float32(k)
+        self._ky_scalar = np.float32(0.0)
+        self._kz_scalar = np.float32(0.0)
+        self._beam_shape = str(beam_shape).lower()
+        self._beam_size = (float(beam_size[0]), float(beam_size[1]))
+        self._beam_samples = (int(beam_samples[0]), int(beam_samples[1]))
+        self._beam_profile = str(beam_profile).lower()
+        self._gauss_waist = gaussian_waist
+        self._set_polarization(pol_perp_rate, pol_direction, pol_degree)
+        self._beam_e1 = np.array([0.0, 1.0, 0.0], dtype=np.float32)
+        self._beam_e2 = np.array([0.0, 0.0, 1.0], dtype=np.float32)
+        self._init_beam_grid()
+
+    def _init_beam_grid(self):
+        """Centred (u, v) grid and the zero-phase field map (Beam.py:220-264)."""
+        Ny, Nz = self._beam_samples
+        Sy, Sz = self._beam_size
+        Ny, Nz = int(max(1, Ny)), int(max(1, Nz))
+        self._beam_Ny, self._beam_Nz = Ny, Nz
+        self._beam_du = float(Sy) / Ny
+        self._beam_dv = float(Sz) / Nz
+        self._beam_uc = (Ny - 1) * 0.5
+        self._beam_vc = (Nz - 1) * 0.5
+        u = (np.arange(Ny, dtype=np.float32) - self._beam_uc) * self._beam_du
+        v = (np.arange(Nz, dtype=np.float32) - self._beam_vc) * self._beam_dv
+        U, V = np.meshgrid(u, v, indexing="ij")
+        if self._beam_shape == "circular":
+            mask = ((U / max(0.5 * Sy, 1e-9)) ** 2 + (V / max(0.5 * Sz, 1e-9)) ** 2) <= 1.0
+        else:
+            mask = np.ones_like(U, dtype=bool)
+        if self._beam_profile == "gaussian":
+            wy, wz = self._gauss_waist if self._gauss_waist is not None else (0.5 * Sy, 0.5 * Sz)
+            wy, wz = max(float(wy), 1e-6), max(float(wz), 1e-6)
+            A0 = np.exp(-((U / wy) ** 2 + (V / wz) ** 2)).astype(np.float32)
+            A0 *= mask.astype(np.float32)
+        else:
+            A0 = mask.astype(np.float32)
+        self._beam_u_centers = u
+        self._beam_v_centers = v
+        self._beam_E0_map = (A0.astype(np.float32) + 0.0j).astype(np.complex64)
+
+    def set_wavefield(self, wavefield):
+        """User-supplied E0(u, v) on the beam grid (Beam.py:266-310)."""
+        arr = np.asarray(wavefield)
+        expected = (int(self._beam_Ny), int(self._beam_Nz))
+        if arr.ndim != 2:
+            raise ValueError(f"set_wavefield: expected a 2-D array of shape {expected}, got ndim={arr.ndim}")
+        if tuple(arr.shape) != expected:
+            raise ValueError(f"set_wavefield: expected shape {expected} (beam_samples), got {tuple(arr.shape)}")
+        arr = np.ascontiguousarray(arr, dtype=np.complex64)
+        if not (np.all(np.isfinite(arr.real)) and np.all(np.isfinite(arr.imag))):
+            raise ValueError("set_wavefield: wavefield contains non-finite values (NaN/Inf)")
+        self._beam_E0_map = arr
+        self._beam_profile = "custom-" + hashlib.sha1(arr.tobytes()).hexdigest()[:12]
+
+    def _set_polarization(self, pol_perp_rate, pol_direction=None, pol_degree=None):
+        self._pol_perp_rate = float(np.clip(pol_perp_rate, 0.0, 1.0))
+        self._pol_direction = (None if pol_direction is None
+                               else np.asarray(pol_direction, dtype=np.float64).reshape(3))
+        self._pol_degree = None if pol_degree is None else float(np.clip(pol_degree, 0.0, 1.0))
+
+    def _polarization_state(self):
+        """(p, ex, ey, ez) of the incident polarization (Beam.py:117-149)."""
+        return polarization_state(self._pol_perp_rate, self._pol_direction, self._pol_degree,
+                                  getattr(self, "_direction", None)
+                                  if getattr(self, "_direction", None) is not None else (1, 0, 0))
+
+    def set_phase_tolerance(self, phi_tol_rad: float):
+        """Maximum phase error per contribution; invalid values mean 1e-3 rad."""
+        try:
+            val = float(phi_tol_rad)
+            if not (val > 0.0):
+                val = 1e-3
+        except Exception:
+            val = 1e-3
+        self._phase_tol_rad = val
+
+    def set_debye_waller(self, b_factors=None):
+        """Per-element Debye-Waller B [A^2]: each scattering factor is multiplied
+        by exp(-B s^2), s = sin(theta)/lambda. None (default) applies no factor,
+        which is the reference's behaviour (thermal motion enters there only as
+        explicit displacements)."""
+        self._debye_waller = None if not b_factors else {str(k): float(v) for k, v in b_factors.items()}
+
+    def _require_forward_beam(self, k_vec=None):
+        """Refuse a beam that is not along +x (Beam.py:1132-1156)."""
+        kx, ky, kz = ((self._kx_scalar, self._ky_scalar, self._kz_scalar) if k_vec is None else k_vec)
+        kx, ky, kz = float(kx), float(ky), float(kz)
+        if kx <= 0.0 or abs(ky) > 1e-6 * kx or abs(kz) > 1e-6 * kx:
+            raise ValueError(
+                "The scattering kernels assume a beam along +x (they take |k| from kx and the "
+                f"incident phase as k*x); got k = ({kx:.4e}, {ky:.4e}, {kz:.4e}) 1/m.  Rotate the "
+                "sample and detector with the stage instead of tilting the beam.")
+
+    # ------------------------------------------------------- tables (parity)
+    def parse_f0_db_all(self, database_name="f0_WaasKirf.dat"):
+        return self.tables.f0
+
+    def parse_f1f2_db_all(self, database_name="f1f2_CromerLiberman.dat"):
+        return self.tables.f1f2
+
+    @staticmethod
+    def get_f1f2_from_params(energy, f1f2_table):
+        return anomalous_at(energy, f1f2_table)
+
+    @staticmethod
+    def _build_f0_zero_dict(db_dict_f0_all):
+        return {el: f0_at_zero(p) for el, p in db_dict_f0_all.items()}
+
+    # --------------------------------------------------------------- staging
+    @property
+    def k(self):
+        return 2.0 * np.pi / self._wavelength
+
+    def _beam_grid(self):
+        return (self._beam_du, self._beam_dv, self._beam_uc, self._beam_vc)
+
+    def collect_atoms(self, sample):
+        """Host arrays of every chunk: positions (N,3) float32 A and global
+        species indices, labels without an f0 table dropped (they scatter
+        nothing in the reference either, Beam.py:5679-5681)."""
+        n_chunks = int(sample.chunk_total or 0)
+        pos_list, idx_list, labels = [], [], []
+        lab_index = {}
+        for cid in range(1, n_chunks + 1):
+            try:
+                codes, lab = sample.load_chunk_species(cid, use_gpu=False, codes=True)
+                codes = np.asarray(codes)
+                lab = np.asarray(lab).astype(str)
+            except TypeError:
+                spc = np.asarray(sample.load_chunk_species(cid, use_gpu=False)).astype(str)
+                lab, codes = np.unique(spc, return_inverse=True)
+                codes = codes.reshape(-1)
+            if codes.size == 0:
+                continue
+            pos = np.asarray(sample.load_chunk_positions(cid, use_gpu=False), dtype=np.float32)
+            if pos.shape[0] != codes.shape[0]:
+                raise ValueError(f"positions/species size mismatch for chunk {cid}")
+            remap = np.full(len(lab), -1, dtype=np.int32)
+            for i, el in enumerate(lab):
+                if not self.tables.has(el):
+                    continue
+                if el not in lab_index:
+                    lab_index[el] = len(labels)
+                    labels.append(el)
+                remap[i] = lab_index[el]
+            g = remap[codes]
+            keep = g >= 0
+            if not keep.all():
+                pos, g = pos[keep], g[keep]
+            pos_list.append(pos)
+            idx_list.append(g)
+        if not pos_list:
+            return np.zeros((0, 3), np.float32), np.zeros(0, np.int32), labels
+        return np.concatenate(pos_list), np.concatenate(idx_list), labels
+
+    def stage_atoms(self, sample, stage, device="cuda"):
+        """All atoms on the device, lab frame, with their incident amplitudes."""
+        pos, idx, labels = self.collect_atoms(sample)
+        table = engine.SpeciesTable.build(labels or ["H"], self.tables, self._energy,
+                                          self._debye_waller)
+        return engine.atoms_lab(pos, idx, stage.rotation, stage.translation, table,
+                                e0=self._beam_E0_map, grid=self._beam_grid(), device=device)
+
+    def physics(self, apply_polarization=False, spherical_decay=False, remove_forward=False,
+                beam_dir=(1.0, 0.0, 0.0), pol=None):
+        return engine.physics(self.k, beam_dir, apply_polarization,
+                              self._polarization_state() if pol is None else pol,
+                              spherical_decay, remove_forward)
+
+    # ---------------------------------------------------------- the sum
+    def split_budget(self, tiles, r0_min):
+        """Largest phase error [rad] of the terms the FP32 split form drops,
+        and whether the |d|^2 (Fresnel) term must be kept.
+
+        Dropped always: the third-order remainders k r^3 / R0^2 of the tile
+        and origin expansions and the factor change across a tile. Dropped
+        when ``fresnel`` is False: k r^2 / 2 R0.
+        """
+        k = self.k
+        r = tiles.max_radius()
+        o = tiles.max_origin_norm()
+        third = k * (r ** 3 + o ** 3 + 3 * o * o * r) / max(r0_min, 1e-30) ** 2
+        fresnel_term = k * r * r / (2.0 * max(r0_min, 1e-30))
+        tol = min(float(self._kernel_phase_tol_rad), float(self._phase_tol_rad))
+        return third, fresnel_term > tol, tol, dict(tile_radius_m=r, origin_max_m=o,
+                                                    third_order_rad=third,
+                                                    fresnel_rad=fresnel_term)
+
+    def scatter_device(self, atoms, pix, phys, out=None, accumulate=False, launch=None):
+        """Run the configured sum on staged atoms/pixels; float64 (P, 2) on the device."""
+        if self._use_fast_kernel and atoms.n > 0:
+            tiles = engine.Tiles(atoms, self.k, self._kernel_tile_atoms, device=atoms.pos.device)
+            third, fresnel, tol, diag = self.split_budget(tiles, pix.r0_min())
+            excursion = 2.0 * diag["tile_radius_m"] / max(pix.r0_min(), 1e-30)
+            if third <= tol and excursion < 1e-6:
+                cfg = launch or self._kernel_launch or tuned_launch(pix.n, tiles)
+                res = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg,
+                                       fresnel=int(fresnel), out=out, accumulate=accumulate)
+                self.last_run = dict(path="split_f32", n_tiles=tiles.n_tiles, fresnel=fresnel,
+                                     launch=dict(cfg), **diag)
+                return res
+            self.last_run = dict(path="plain_f64", declined="split-phase error budget", **diag)
+        else:
+            self.last_run = dict(path="plain_f64")
+        return engine.run_plain(atoms, pix, phys, out=out, accumulate=accumulate)
+
+    def interact_beam_gpu(self, sample, measurement_positions, measurement_shape, stage,
+                          remove_forward: bool = False, use_depth_ein: bool = False,
+                          ein_cache_dir=None, recompute_cache: bool = False,
+                          apply_polarization: bool = False, spherical_decay: bool = True,
+                          analyser_mode="off", analyser_acceptance_angle_rad: float = 0.0,
+                          analyser_darwin_halfwidth_rad: float = 0.0, return_double=False):
+        """Kinematic scattering on the GPU (Beam.py:6028-6407); complex (Nz, Ny)."""
+        off = (analyser_mode is None
+               or (isinstance(analyser_mode, str) and analyser_mode.strip().lower() in ("off", "none", "disabled"))
+               or (not isinstance(analyser_mode, str) and analyser_mode == 0))
+        if not off:
+            raise NotImplementedError("analyser acceptance (top-hat/Darwin) is not provided")
+        if use_depth_ein:
+            raise NotImplementedError("depth-dependent E_in (absorption maps) is not provided")
+        if not torch.cuda.is_available():
+            raise RuntimeError("interact_beam_gpu: no CUDA GPU (this library has no CPU path)")
+        self._require_forward_beam()
+        Ny, Nz = int(measurement_shape[0]), int(measurement_shape[1])
+        if int(sample.chunk_total or 0) == 0:
+            return np.zeros((Nz, Ny), dtype=np.complex128 if return_double else np.complex64)
+        coords = np.asarray(measurement_positions)
+        if coords.shape != (3, Ny * Nz):
+            raise ValueError(f"pixel coordinates {coords.shape} do not match shape ({Ny}, {Nz})")
+        phys = self.physics(apply_polarization, spherical_decay, remove_forward)
+        atoms = self.stage_atoms(sample, stage)
+        pix = engine.Pixels(coords.astype(np.float64) / 1e10, Ny, Nz, phys)
+        out = self.scatter_device(atoms, pix, phys)
+        engine.sync()
+        field = torch.view_as_complex(out).cpu().numpy().reshape(Nz, Ny)
+        return field if return_double else field.astype(np.complex64)
+
+    def atomic_scattering_kinematic(self, sample, detector, stage, offset=None, use_gpu=True,
+                                    remove_forward: bool = False, use_depth_ein: bool = False,
+                                    ein_cache_dir=None, recompute_cache: bool = False,
+                                    apply_polarization: bool = False,
+                                    spherical_decay: bool = False, analyser_mode="off",
+                                    analyser_acceptance_angle_rad: float = 0.0,
+                                    analyser_darwin_halfwidth_rad: float = 0.0,
+                                    return_double: bool = False):
+        """Single-bounce kinematic field on the detector (Beam.py:6409-6496):
+        complex64 (Nz, Ny) (complex128 with ``return_double``), minus
+        ``offset`` when given."""
+        if not use_gpu:
+            raise RuntimeError("atomic_scattering_kinematic: use_gpu=False is not supported; "
+                               "this library runs the sum on the GPU only")
+        Ny, Nz = detector.shape
+        field = self.interact_beam_gpu(
+            sample, detector.pixel_coordinates, (Ny, Nz), stage, remove_forward=remove_forward,
+            use_depth_ein=use_depth_ein, ein_cache_dir=ein_cache_dir,
+            recompute_cache=recompute_cache, apply_polarization=apply_polarization,
+            spherical_decay=spherical_decay, analyser_mode=analyser_mode,
+            analyser_acceptance_angle_rad=analyser_acceptance_angle_rad,
+            analyser_darwin_halfwidth_rad=analyser_darwin_halfwidth_rad,
+            return_double=return_double)
+        return (field - offset) if offset is not None else field
+
+    def atomic_direct_interaction(self, sample, detector, stage, scattering=True, sc_kwargs=None,
+                                  transmission=False, tr_kwargs=None, use_gpu=True):
+        """Scattering term written to the detector (Beam.py:7771-7824)."""
+        if transmission:
+            raise NotImplementedError("the transmission term is not provided")
+        Ny, Nz = detector.shape
+        final = np.zeros((Nz, Ny), dtype=np.complex64)
+        if scattering:
+            final += np.asarray(self.atomic_scattering_kinematic(sample=sample, detector=detector,
+                                                                 stage=stage, **(sc_kwargs or {})),
+                                dtype=np.complex64)
+        detector.input_pixel_values(final)
+
+
+def tuned_launch(n_pix, tiles):
+    """Launch shape for the split kernel: the autotuner's cached winner, or
+    the default when none is cached."""
+    from . import autotune
+    return autotune.lookup(n_pix, tiles)

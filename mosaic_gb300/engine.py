@@ -1,0 +1,272 @@
+"""Device-side staging and launches for the kinematic sum.
+
+PyTorch supplies device memory and the stream; every computation on the
+path runs in libmosaic_kin.so (``include/mosaic_kin.h``) through ctypes.
+
+Data layout in HBM (one GPU):
+  atoms    pos_lab float64 (N, 3) [m], species int32 (N), amp float32 (N, 2)
+  tiles    origin float64 (n_tiles, 4) [m], species int32 (n_tiles),
+           pos float32 (n_tiles*T, 4) = k/2pi (a - o) [cycles] and its |.|^2,
+           amp float32 (n_tiles*T, 2); each species run padded to whole tiles
+  pixels   xyz float64 (3, P) [m] and the derived r0, qcut, qc, uf, phasor
+  output   complex128 (P,) = float64 (P, 2)
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import MkLaunch, MkPhysics, MkPixels, MkSpecies, MkTiles, check
+
+R_E = 2.81794092e-15
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("mosaic_gb300 needs a CUDA GPU: there is no CPU path")
+    return _lib.load()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream_handle(stream=None):
+    s = stream or torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+@dataclass
+class SpeciesTable:
+    """Per-species arrays in kernel order (host float32)."""
+    labels: list
+    wk: np.ndarray
+    f0z: np.ndarray
+    anom: np.ndarray
+    dw_b: np.ndarray | None = None
+
+    @classmethod
+    def build(cls, labels, tables, energy_eV, dw_b=None):
+        labels = [str(x) for x in labels]
+        if len(labels) > _lib.MAX_SPECIES:
+            raise ValueError(f"at most {_lib.MAX_SPECIES} species per call, got {len(labels)}")
+        wk = np.stack([tables.row(e) for e in labels]).astype(np.float32)
+        f0z = np.array([tables.f0_zero(e) for e in labels], dtype=np.float32)
+        an = np.array([tables.anomalous(e, energy_eV) for e in labels], dtype=np.complex128)
+        b = None
+        if dw_b is not None:
+            b = np.array([float(dw_b.get(e, 0.0)) for e in labels], dtype=np.float32)
+            if not np.any(b):
+                b = None
+        return cls(labels, wk, f0z, an, b)
+
+    def abi(self):
+        self._keep = [np.ascontiguousarray(self.wk, np.float32),
+                      np.ascontiguousarray(self.f0z, np.float32),
+                      np.ascontiguousarray(self.anom.real, np.float32),
+                      np.ascontiguousarray(self.anom.imag, np.float32),
+                      None if self.dw_b is None else np.ascontiguousarray(self.dw_b, np.float32)]
+        w, z, ar, ai, b = self._keep
+        return MkSpecies(len(self.labels), w.ctypes.data, z.ctypes.data, ar.ctypes.data,
+                         ai.ctypes.data, None if b is None else b.ctypes.data)
+
+
+def physics(k, beam_dir=(1.0, 0.0, 0.0), apply_pol=False, pol=(0.0, 0.0, 1.0, 0.0),
+            spherical_decay=False, remove_forward=False):
+    ph = MkPhysics()
+    ph.k = float(k)
+    ph.beam_dir[:] = [float(v) for v in beam_dir]
+    ph.apply_pol = int(bool(apply_pol))
+    ph.pol_deg = float(pol[0])
+    ph.pol_e[:] = [float(v) for v in pol[1:4]]
+    ph.spherical_decay = int(bool(spherical_decay))
+    ph.remove_forward = int(bool(remove_forward))
+    return ph
+
+
+class Pixels:
+    """Detector pixels on the device plus their per-pixel prologue."""
+
+    def __init__(self, xyz_m, ny, nz, phys, device="cuda", stream=None):
+        L = _require_cuda()
+        P = int(ny) * int(nz)
+        if isinstance(xyz_m, torch.Tensor):
+            self.xyz = xyz_m.to(device=device, dtype=torch.float64).reshape(3, P).contiguous()
+        else:
+            xyz = torch.as_tensor(np.ascontiguousarray(xyz_m, dtype=np.float64).reshape(3, P))
+            self.xyz = xyz.to(device, non_blocking=False)
+        dd = dict(dtype=torch.float64, device=device)
+        self.r0 = torch.empty(P, **dd)
+        self.qcut = torch.empty(P, **dd)
+        self.qc = torch.empty((3, P), **dd)
+        self.uf = torch.empty((4, P), dtype=torch.float32, device=device)
+        self.phasor = torch.empty((P, 2), **dd)
+        self.ny, self.nz, self.n = int(ny), int(nz), P
+        self.abi = MkPixels(self.ny, self.nz, self.xyz.data_ptr(), self.r0.data_ptr(),
+                            self.qcut.data_ptr(), self.qc.data_ptr(), self.uf.data_ptr(),
+                            self.phasor.data_ptr())
+        check(L.mk_pixels_prepare(ctypes.byref(self.abi), ctypes.byref(phys), _stream_handle(stream)))
+
+    def r0_min(self):
+        return float(self.r0.min())
+
+
+@dataclass
+class Atoms:
+    """Atoms on the device in the frame of the pixels."""
+    pos: torch.Tensor       # float64 (N, 3) [m]
+    species: torch.Tensor   # int32 (N,)
+    amp: torch.Tensor       # float32 (N, 2)
+    counts: np.ndarray      # int64 (S,) atoms per species
+    table: SpeciesTable
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def n(self):
+        return int(self.pos.shape[0])
+
+
+def atoms_lab(pos_A, species_idx, rot, trans, table, e0=None, grid=None, device="cuda",
+              stream=None, counts=None):
+    """Stage transform and incident amplitude on the device (mk_atoms_lab).
+
+    ``pos_A`` (N,3) float32 Angstrom and ``species_idx`` (N,) may be host
+    arrays or device tensors; with device species pass ``counts`` (atoms per
+    species) so nothing is read back."""
+    L = _require_cuda()
+    pos_A = torch.as_tensor(pos_A)
+    n = int(pos_A.shape[0])
+    pin = pos_A.to(device=device, dtype=torch.float32).contiguous()
+    pos = torch.empty((n, 3), dtype=torch.float64, device=device)
+    amp = torch.empty((n, 2), dtype=torch.float32, device=device)
+    rot = np.ascontiguousarray(rot, dtype=np.float32).reshape(9)
+    trans = np.ascontiguousarray(trans, dtype=np.float32).reshape(3)
+    e0_t, gny, gnz, g = None, 0, 0, None
+    if e0 is not None:
+        e0_t = torch.view_as_real(torch.as_tensor(np.ascontiguousarray(e0, dtype=np.complex64))).to(device)
+        gny, gnz = int(e0.shape[0]), int(e0.shape[1])
+        g = np.ascontiguousarray(grid, dtype=np.float64)
+    check(L.mk_atoms_lab(n, _ptr(pin), rot.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                         trans.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), _ptr(e0_t), gny, gnz,
+                         None if g is None else g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                         _ptr(pos), _ptr(amp), _stream_handle(stream)))
+    if isinstance(species_idx, torch.Tensor):
+        sp = species_idx.to(device=device, dtype=torch.int32).contiguous()
+        if counts is None:
+            counts = torch.bincount(sp.long(), minlength=len(table.labels)).cpu().numpy()
+    else:
+        sp = torch.as_tensor(np.ascontiguousarray(species_idx, dtype=np.int32)).to(device)
+        if counts is None:
+            counts = np.bincount(np.asarray(species_idx), minlength=len(table.labels))
+    return Atoms(pos, sp, amp, np.asarray(counts, dtype=np.int64), table)
+
+
+class Tiles:
+    """Species-partitioned, Morton-ordered atom tiles (mk_tiles_build)."""
+
+    def __init__(self, atoms: Atoms, k, tile_atoms=1024, device="cuda", stream=None):
+        L = _require_cuda()
+        T = int(tile_atoms)
+        counts = np.ascontiguousarray(atoms.counts, dtype=np.int64)
+        n_tiles = int(sum((int(c) + T - 1) // T for c in counts))
+        self.n_tiles, self.tile_atoms = n_tiles, T
+        self.origin = torch.empty((max(n_tiles, 1), 4), dtype=torch.float64, device=device)
+        self.species = torch.empty(max(n_tiles, 1), dtype=torch.int32, device=device)
+        self.pos = torch.empty((max(n_tiles, 1) * T, 4), dtype=torch.float32, device=device)
+        self.amp = torch.empty((max(n_tiles, 1) * T, 2), dtype=torch.float32, device=device)
+        self.abi = MkTiles(n_tiles, T, self.origin.data_ptr(), self.species.data_ptr(),
+                           self.pos.data_ptr(), self.amp.data_ptr())
+        self.table = atoms.table
+        if atoms.n == 0:
+            return
+        ws_n = L.mk_tiles_workspace_size(atoms.n)
+        ws = torch.empty(ws_n, dtype=torch.uint8, device=device)
+        check(L.mk_tiles_build(atoms.n, _ptr(atoms.pos), _ptr(atoms.species), _ptr(atoms.amp),
+                               len(counts), counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                               float(k), ctypes.byref(self.abi), _ptr(ws), ws_n,
+                               _stream_handle(stream)))
+        self._ws = ws   # keep until the stream has consumed it
+
+    def max_radius(self):
+        return float(self.origin[: self.n_tiles, 3].max()) if self.n_tiles else 0.0
+
+    def max_origin_norm(self):
+        if not self.n_tiles:
+            return 0.0
+        return float(torch.linalg.vector_norm(self.origin[: self.n_tiles, :3], dim=1).max())
+
+    def amp_is_real(self):
+        return bool((self.amp[:, 1] == 0).all()) if self.n_tiles else True
+
+
+DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0)
+
+
+def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None, fresnel=-1,
+              amp_real=None, out=None, accumulate=False, stream=None):
+    """FP32 split-phase sum; returns float64 (P, 2) (a view of `out` if given)."""
+    L = _require_cuda()
+    cfg = dict(DEFAULT_LAUNCH, **(launch or {}))
+    ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
+                  int(tiles.amp_is_real() if amp_real is None else bool(amp_real)))
+    ns = ctypes.c_int(0)
+    check(L.mk_split_plan(ctypes.byref(tiles.abi), ctypes.byref(pix.abi), ctypes.byref(ln),
+                          ctypes.byref(ns)))
+    ws_n = L.mk_sum_workspace_size(pix.n, max(ns.value, 1))
+    ws = torch.empty(ws_n, dtype=torch.uint8, device=pix.xyz.device)
+    if out is None:
+        out = torch.zeros((pix.n, 2), dtype=torch.float64, device=pix.xyz.device)
+    sp = table.abi()
+    check(L.mk_kin_split_f32(ctypes.byref(tiles.abi), ctypes.byref(sp), ctypes.byref(phys),
+                             ctypes.byref(pix.abi), ctypes.byref(ln), _ptr(out), int(bool(accumulate)),
+                             _ptr(ws), ws_n, _stream_handle(stream)))
+    out._mk_keep = ws
+    return out
+
+
+def run_plain(atoms: Atoms, pix: Pixels, phys, slices=0, out=None, accumulate=False, stream=None):
+    """FP64 plain sum; returns float64 (P, 2)."""
+    L = _require_cuda()
+    n = atoms.n
+    if slices > 0:
+        ns = int(slices)
+    else:
+        sms = torch.cuda.get_device_properties(pix.xyz.device).multi_processor_count
+        bx = (pix.n + 127) // 128
+        ns = max(1, min((8 * sms + bx - 1) // bx, (n + 511) // 512, 4096))
+    ws_n = L.mk_sum_workspace_size(pix.n, ns)
+    ws = torch.empty(ws_n, dtype=torch.uint8, device=pix.xyz.device)
+    if out is None:
+        out = torch.zeros((pix.n, 2), dtype=torch.float64, device=pix.xyz.device)
+    sp = atoms.table.abi()
+    check(L.mk_kin_plain_f64(n, _ptr(atoms.pos), _ptr(atoms.species), _ptr(atoms.amp),
+                             ctypes.byref(sp), ctypes.byref(phys), ctypes.byref(pix.abi), ns,
+                             _ptr(out), int(bool(accumulate)), _ptr(ws), ws_n,
+                             _stream_handle(stream)))
+    out._mk_keep = ws
+    return out
+
+
+def sync(stream=None):
+    """Wait for the stream and raise on a device-side error flag."""
+    L = _require_cuda()
+    check(L.mk_sync_status(_stream_handle(stream)))
+
+
+class TilesView:
+    """The first ``m`` tiles of a Tiles object (same device buffers)."""
+
+    def __init__(self, tiles, m):
+        self.n_tiles, self.tile_atoms = int(m), tiles.tile_atoms
+        self.origin, self.species, self.pos, self.amp = tiles.origin, tiles.species, tiles.pos, tiles.amp
+        self.table = tiles.table
+        self.abi = MkTiles(self.n_tiles, self.tile_atoms, self.origin.data_ptr(),
+                           self.species.data_ptr(), self.pos.data_ptr(), self.amp.data_ptr())
+
+    def amp_is_real(self):
+        return bool((self.amp[: self.n_tiles * self.tile_atoms, 1] == 0).all())

@@ -1,0 +1,89 @@
+"""In-memory chunked sample with the reference's chunk API.
+
+The scattering entry point reads a sample only through this duck type
+(MOSAIC Sample.py:715-872): ``chunk_total``, ``chunk_atom_count(cid)``,
+``load_chunk_positions(cid, use_gpu, raw)`` -> (N, 3) float32 Angstrom with
+the thermal displacement applied on load, and ``load_chunk_species(cid,
+use_gpu, codes)`` -> labels, or (codes, labels) with ``codes=True``.
+Chunks are 1-based.
+
+The Gaussian thermal displacement follows Sample.apply_temperature
+(Sample.py:2084-2156, 2321-2334): one NumPy generator per chunk seeded with
+SeedSequence([seed, chunk]), standard normals in the positions' dtype times
+sigma, clipped to +-max_displacement when that is positive.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def thermal_displacement(positions, sigma, max_displacement=1.0, seed=40, chunk_number=None):
+    """Displaced copy of ``positions`` (the reference's Gaussian rule)."""
+    pos = np.asarray(positions)
+    root = np.random.SeedSequence().entropy if seed is None else int(seed)
+    key = [root] if chunk_number is None else [root, int(chunk_number)]
+    rng = np.random.default_rng(np.random.SeedSequence(key))
+    d = rng.standard_normal(size=pos.shape, dtype=pos.dtype)
+    d *= float(sigma)
+    if max_displacement is not None and max_displacement > 0.0:
+        np.clip(d, -max_displacement, max_displacement, out=d)
+    return pos + d
+
+
+class ChunkedSample:
+    """Chunks of (positions (N,3) Angstrom, species) held in host memory.
+
+    Args:
+        chunks: list of (positions, species) where species is an (N,) label
+            array, or a (codes (N,) uint8/int, labels (S,)) pair.
+        thermal: None or dict(sigma=, max_displacement=, seed=) for the
+            Gaussian displacement applied on every load.
+        dimensions: (Lx, Ly, Lz) in Angstrom (the sample box, informational).
+    """
+
+    def __init__(self, chunks, thermal=None, dimensions=None, directory=""):
+        self._chunks = []
+        for pos, spc in chunks:
+            pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+            if isinstance(spc, tuple):
+                codes, labels = np.asarray(spc[0]), np.asarray(spc[1]).astype(str)
+            else:
+                labels, codes = np.unique(np.asarray(spc).astype(str), return_inverse=True)
+                codes = codes.reshape(-1).astype(np.uint8 if labels.size <= 256 else np.uint16)
+            if codes.shape[0] != pos.shape[0]:
+                raise ValueError("positions/species size mismatch")
+            self._chunks.append((pos, codes, labels))
+        self.thermal = thermal
+        self.directory = directory
+        if dimensions is None and self._chunks:
+            allp = [c[0] for c in self._chunks if c[0].size]
+            if allp:
+                lo = np.min([p.min(0) for p in allp], axis=0)
+                hi = np.max([p.max(0) for p in allp], axis=0)
+                dimensions = tuple((hi - lo).tolist())
+        self.dimensions = dimensions
+
+    @property
+    def chunk_total(self):
+        return len(self._chunks)
+
+    def chunk_atom_count(self, chunk_number):
+        return int(self._chunks[chunk_number - 1][0].shape[0])
+
+    def load_chunk_positions(self, chunk_number, use_gpu=False, raw=False):
+        pos = self._chunks[chunk_number - 1][0]
+        if self.thermal and not raw:
+            t = self.thermal
+            return thermal_displacement(pos, t.get("sigma", 0.25), t.get("max_displacement", 1.0),
+                                        t.get("seed", 40), chunk_number)
+        return pos.copy()
+
+    def load_chunk_species(self, chunk_number, use_gpu=False, codes=False):
+        _, c, labels = self._chunks[chunk_number - 1]
+        if codes:
+            return c, labels
+        return labels[c]
+
+    @property
+    def n_atoms(self):
+        return sum(c[0].shape[0] for c in self._chunks)

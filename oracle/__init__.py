@@ -1,0 +1,251 @@
+"""CPU oracle for the kinematic scattering path -- TEST INFRASTRUCTURE ONLY.
+
+Nothing in the product (``mosaic_gb300``) imports this package. Only
+``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
+it, and only as the checker (or as the timed CPU baseline).
+
+Contents
+--------
+* ``kin_oracle.c`` -- FP64 C restatement of the reference CPU kernel
+  ``compute_scattering_cffi`` (MOSAIC ``Beam.py:663-816``), threaded over atom
+  slices summed in slice order (``Beam.py:5941-5955``), plus the free-space
+  propagator multiply (``Beam.py:4747-4834``).
+* ``ref_tables`` / ``ein_bilinear`` / ``polarization_state`` /
+  ``interact_cpu`` below -- NumPy restatements of the reference host logic
+  around that kernel (``Beam.py:31-47``, ``117-149``, ``503-615``, ``956-1045``,
+  ``5621-5956``).
+
+Pinning: every function here is checked against fixtures produced by running
+the reference itself (``tests/golden/make_golden.py``), see
+``tests/test_oracle_golden.py``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "kin_oracle.c")
+_SO = os.path.join(_HERE, "_ref", "libkin_oracle.so")
+_lib = None
+
+R_E = 2.81794092e-15          # classical electron radius [m] (Beam.py:704)
+H_PLANCK = 6.62607015e-34     # SI constants of beam.__init__ (Beam.py:98-101)
+C_LIGHT = 299792458
+Q_E = 1.602176634e-19
+
+
+def build(force: bool = False) -> str:
+    """Compile kin_oracle.c into oracle/_ref/libkin_oracle.so.
+
+    gcc -O3 with -ffp-contract=off: without contraction the x86 and Arm builds
+    round every operation identically. The absolute phase k (x + r) is ~1e10 rad,
+    where one double ulp is ~2e-6 rad, so an FMA-contracted build (as the
+    reference's -march=native cffi build is) differs from an uncontracted one
+    by ~1e-6 relative in the summed field.
+    """
+    os.makedirs(os.path.dirname(_SO), exist_ok=True)
+    if (not force and os.path.exists(_SO)
+            and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
+        return _SO
+    tmp = _SO + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", "-O3", "-ffp-contract=off", "-std=c11", "-shared", "-fPIC", "-pthread",
+                           _SRC, "-o", tmp, "-lm"])
+    os.replace(tmp, _SO)
+    return _SO
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_SO)
+        dp = ctypes.POINTER(ctypes.c_double)
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.mko_scatter_f64.restype = ctypes.c_int
+        L.mko_scatter_f64.argtypes = [
+            ctypes.c_int64, dp, fp, fp, ctypes.c_int, fp, fp, fp, fp, fp,
+            ctypes.c_int, ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int,
+            ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+            ctypes.c_int, dp, dp, ctypes.c_int]
+        L.mko_prop_mul_f64.restype = None
+        L.mko_prop_mul_f64.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, dp]
+        _lib = L
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def scatter_f64(pos_m, wk, f0z, anom_re, anom_im, amp_re, amp_im, cx, cy, cz, k,
+                ny, nz, remove_forward=False, apply_pol=False,
+                pol=(0.0, 0.0, 1.0, 0.0), decay=False, dw_b=None, n_threads=None):
+    """FP64 kinematic sum (compute_scattering_cffi semantics, double output).
+
+    Args mirror ``Beam.py:631-651``: positions (N,3) metres, per-atom WK rows
+    (N,11), f0(0), f'/f'' and incident amplitude; pixel coordinates in metres.
+    ``pol`` = (p, ex, ey, ez). Returns complex128 (ny*nz,).
+    """
+    L = lib()
+    n = int(np.asarray(pos_m).shape[0])
+    P = int(ny) * int(nz)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    pos = f64(pos_m).reshape(n, 3)
+    wk = f32(wk).reshape(n, 11)
+    f0z, ar, ai, er, ei = (f32(v).reshape(n) for v in (f0z, anom_re, anom_im, amp_re, amp_im))
+    dwb = None if dw_b is None else f32(dw_b).reshape(n)
+    cx, cy, cz = (f64(v).reshape(P) for v in (cx, cy, cz))
+    out_r = np.zeros(P)
+    out_i = np.zeros(P)
+    nt = int(n_threads or os.cpu_count() or 1)
+    rc = L.mko_scatter_f64(
+        n, _p(pos, ctypes.c_double), _p(wk, ctypes.c_float), _p(f0z, ctypes.c_float),
+        int(bool(remove_forward)), _p(ar, ctypes.c_float), _p(ai, ctypes.c_float),
+        _p(er, ctypes.c_float), _p(ei, ctypes.c_float),
+        None if dwb is None else _p(dwb, ctypes.c_float),
+        int(ny), int(nz), _p(cx, ctypes.c_double), _p(cy, ctypes.c_double),
+        _p(cz, ctypes.c_double), float(k), int(bool(apply_pol)),
+        float(pol[0]), float(pol[1]), float(pol[2]), float(pol[3]), int(bool(decay)),
+        _p(out_r, ctypes.c_double), _p(out_i, ctypes.c_double), nt)
+    if rc != 0:
+        raise MemoryError("oracle scatter could not allocate its work buffers")
+    return out_r + 1j * out_i
+
+
+def prop_mul_f64(F, ky, kz, k, z, kga=None, kgy=0.0, kgz=0.0):
+    """Free-space transfer-function multiply (Beam.py:4747-4834), FP64, returns a copy."""
+    L = lib()
+    G = np.ascontiguousarray(F, dtype=np.complex128).copy()
+    nz, ny = G.shape
+    ky = np.ascontiguousarray(ky, dtype=np.float64)
+    kz = np.ascontiguousarray(kz, dtype=np.float64)
+    L.mko_prop_mul_f64(int(ny), int(nz), _p(ky, ctypes.c_double), _p(kz, ctypes.c_double),
+                       float(k), float(z), float(k if kga is None else kga), float(kgy),
+                       float(kgz), G.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return G
+
+
+# --------------------------------------------------------------------------
+# NumPy restatements of the host logic around the kernel
+# --------------------------------------------------------------------------
+def polarization_state(pol_perp_rate=0.5, pol_direction=None, pol_degree=None,
+                       direction=(1.0, 0.0, 0.0)):
+    """(p, ex, ey, ez) as ``beam._polarization_state`` (Beam.py:117-149, 31-47)."""
+    khat = np.asarray(direction, dtype=np.float64)
+    khat = khat / np.linalg.norm(khat)
+    rho = float(np.clip(pol_perp_rate, 0.0, 1.0))
+    p_rate = abs(2.0 * rho - 1.0)
+    e_rate = np.array([0.0, 1.0, 0.0]) if rho >= 0.5 else np.array([0.0, 0.0, 1.0])
+    p = p_rate if pol_degree is None else float(np.clip(pol_degree, 0.0, 1.0))
+    e = e_rate if pol_direction is None else np.asarray(pol_direction, dtype=np.float64).reshape(3)
+    e = e - np.dot(e, khat) * khat
+    if np.linalg.norm(e) < 1e-12:
+        for axis in (np.array([0.0, 1.0, 0.0]), np.array([0.0, 0.0, 1.0])):
+            e = axis - np.dot(axis, khat) * khat
+            if np.linalg.norm(e) >= 1e-12:
+                break
+    e = e / np.linalg.norm(e)
+    return float(p), float(e[0]), float(e[1]), float(e[2])
+
+
+def anomalous(energy, table):
+    """f' + i f'' by linear interpolation in energy, end segment extended
+    (Beam.py:569-597). ``table`` is (N,3) [E, f1, f2] float32."""
+    E = table[:, 0]
+    idx = int(np.searchsorted(E, energy))
+    idx = min(max(idx, 1), len(E) - 1)
+    E0, E1 = E[idx - 1], E[idx]
+    w = (energy - E0) / ((E1 - E0) if E1 > E0 else 1e-20)
+    f1 = table[idx - 1, 1] + (table[idx, 1] - table[idx - 1, 1]) * w
+    f2 = table[idx - 1, 2] + (table[idx, 2] - table[idx - 1, 2]) * w
+    return complex(f1, f2)
+
+
+def ein_bilinear(pos, E0, du, dv, uc, vc, e1=(0, 1, 0), e2=(0, 0, 1)):
+    """Per-atom incident amplitude by bilinear sampling of E0 with tau = phi = 0,
+    zero outside the grid (Beam.py:956-1045). pos (N,3) float32 Angstrom."""
+    pos = np.asarray(pos, dtype=np.float32)
+    e1 = np.asarray(e1, dtype=np.float32)
+    e2 = np.asarray(e2, dtype=np.float32)
+    N = pos.shape[0]
+    out = np.zeros(N, dtype=np.complex64)
+    NyB, NzB = E0.shape
+    au = pos[:, 0] * e1[0] + pos[:, 1] * e1[1] + pos[:, 2] * e1[2]
+    av = pos[:, 0] * e2[0] + pos[:, 1] * e2[1] + pos[:, 2] * e2[2]
+    iu = au / float(du) + float(uc)
+    iv = av / float(dv) + float(vc)
+    inb = (iu >= 0.0) & (iu <= NyB - 1) & (iv >= 0.0) & (iv <= NzB - 1)
+    if not np.any(inb):
+        return out
+    iu, iv = iu[inb], iv[inb]
+    i0 = np.floor(iu).astype(np.int64)
+    j0 = np.floor(iv).astype(np.int64)
+    i1 = np.clip(i0 + 1, 0, NyB - 1)
+    j1 = np.clip(j0 + 1, 0, NzB - 1)
+    fu = (iu - i0).astype(np.float32)
+    fv = (iv - j0).astype(np.float32)
+    Ef = np.asarray(E0, dtype=np.complex64).ravel()
+    val = (Ef[i0 * NzB + j0] * ((1 - fu) * (1 - fv)) + Ef[i0 * NzB + j1] * ((1 - fu) * fv)
+           + Ef[i1 * NzB + j0] * (fu * (1 - fv)) + Ef[i1 * NzB + j1] * (fu * fv))
+    out[inb] = val.astype(np.complex64)
+    return out
+
+
+def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV,
+                 f0_rows, f0_zero, f1f2_tables, E0, beam_grid, pol_state,
+                 remove_forward=False, apply_polarization=False,
+                 spherical_decay=False, dw_b=None, n_threads=None):
+    """Restatement of ``interact_beam_cpu`` (Beam.py:5773-5956) for E0-only
+    incident fields, returning complex128 (Nz, Ny).
+
+    chunks: iterable of (positions (N,3) float32 A, species labels (N,)).
+    beam_grid: (du, dv, uc, vc). f0_rows: element -> (11,) float32;
+    f0_zero: element -> float; f1f2_tables: element -> (M,3) float32.
+    dw_b: None or element -> B (A^2).
+    """
+    Ny, Nz = shape
+    lam = H_PLANCK / Q_E * C_LIGHT / float(energy_eV)
+    k = float(2.0 * np.pi / lam)
+    cx, cy, cz = (np.asarray(pixel_coords_A[i]).astype(np.float64) / 1e10 for i in range(3))
+    out = np.zeros(Ny * Nz, dtype=np.complex128)
+    R = np.asarray(rotation, dtype=np.float32)
+    T = np.asarray(translation, dtype=np.float32)
+    du, dv, uc, vc = beam_grid
+    for pos, spc in chunks:
+        pos = np.asarray(pos, dtype=np.float32)
+        spc = np.asarray(spc).astype(str)
+        n = pos.shape[0]
+        if n == 0:
+            continue
+        lab = (pos @ R.T + T).astype(np.float32)
+        amp = ein_bilinear(lab, E0, du, dv, uc, vc)
+        wk = np.zeros((n, 11), np.float32)
+        f0z = np.zeros(n, np.float32)
+        ar = np.zeros(n, np.float32)
+        ai = np.zeros(n, np.float32)
+        b = np.zeros(n, np.float32)
+        for el in np.unique(spc):
+            if el not in f0_rows:
+                continue
+            m = spc == el
+            wk[m] = f0_rows[el]
+            f0z[m] = float(f0_zero[el])
+            if el in f1f2_tables:
+                c = anomalous(energy_eV, f1f2_tables[el])
+                ar[m] = c.real
+                ai[m] = c.imag
+            if dw_b is not None:
+                b[m] = float(dw_b.get(el, 0.0))
+        out += scatter_f64(lab.astype(np.float64) / 1e10, wk, f0z, ar, ai,
+                           amp.real, amp.imag, cx, cy, cz, k, Ny, Nz,
+                           remove_forward=remove_forward, apply_pol=apply_polarization,
+                           pol=pol_state, decay=spherical_decay,
+                           dw_b=None if dw_b is None else b, n_threads=n_threads)
+    return out.reshape(Nz, Ny)

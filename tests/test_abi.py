@@ -1,0 +1,53 @@
+"""The C-ABI library builds, loads, and exports every entry point that
+include/mosaic_kin.h declares; argument checks that run before any CUDA call
+return their status codes without a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from mosaic_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "mosaic_kin.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\**\s*(mk_[a-z_0-9]+)\s*\(", src,
+                                 flags=re.M)))
+
+
+def test_header_declares_the_entry_points():
+    fns = declared_functions()
+    assert {"mk_version", "mk_last_error", "mk_sync_status", "mk_kin_plain_f64",
+            "mk_kin_split_f32", "mk_tiles_build", "mk_pixels_prepare"} <= set(fns)
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    so = _lib.build()
+    assert os.path.exists(so)
+    L = ctypes.CDLL(so)
+    for name in declared_functions():
+        assert hasattr(L, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_version_and_host_side_validation():
+    L = _lib.load()
+    assert L.mk_version() >= 10000
+    # null arguments are rejected before any CUDA call
+    assert L.mk_pixels_prepare(None, None, None) == _lib.MK_EINVAL
+    assert b"null" in L.mk_last_error()
+    assert L.mk_kin_split_f32(None, None, None, None, None, None, 0, None, 0, None) == _lib.MK_EINVAL
+    assert L.mk_kin_plain_f64(0, None, None, None, None, None, None, 0, None, 0, None, 0,
+                              None) == _lib.MK_EINVAL
+    assert L.mk_sum_workspace_size(1000, 3) == 1000 * 3 * 16
+    with pytest.raises(ValueError):
+        _lib.check(_lib.MK_EINVAL)
+    with pytest.raises(MemoryError):
+        _lib.check(_lib.MK_ENOMEM)
+    with pytest.raises(_lib.DeclineError):
+        _lib.check(_lib.MK_EDECLINE)

@@ -1,0 +1,90 @@
+"""Pin the CPU oracle to the reference: every fixture here was produced by
+running the reference itself (tests/golden/make_golden.py)."""
+import numpy as np
+
+import oracle
+
+
+def test_oracle_kernel_matches_reference_kernels(golden):
+    d = golden("kernel_cases.npz")
+    assert int(d["n"]) >= 18
+    for i in range(int(d["n"])):
+        p = f"c{i}_"
+        ny, nz, rf, ap, dc, k, pdeg, ex, ey, ez = d[p + "meta"]
+        a, amp, c = d[p + "anom"], d[p + "amp"], d[p + "cxyz"]
+        got = oracle.scatter_f64(d[p + "pos_m"], d[p + "wk"], d[p + "f0z"], a.real, a.imag,
+                                 amp.real, amp.imag, c[0], c[1], c[2], k, int(ny), int(nz), rf, ap,
+                                 (pdeg, ex, ey, ez), dc, n_threads=3)
+        m = np.abs(got).max()
+        # NumPy twin: same uncontracted double arithmetic, output rounded to float32.
+        assert np.abs(got - d[p + "out_numpy"]).max() / m <= 2e-7, i
+        # cffi kernel: built -O3 -march=native, which contracts FMAs and moves the
+        # ~1e10 rad absolute phase by ~1e-6 rad.
+        assert np.abs(got - d[p + "out_cffi"]).max() / m <= 1e-5, i
+
+
+def test_oracle_threads_do_not_change_result(golden):
+    d = golden("kernel_cases.npz")
+    p = "c1_"
+    ny, nz, rf, ap, dc, k, pdeg, ex, ey, ez = d[p + "meta"]
+    a, amp, c = d[p + "anom"], d[p + "amp"], d[p + "cxyz"]
+    args = (d[p + "pos_m"], d[p + "wk"], d[p + "f0z"], a.real, a.imag, amp.real, amp.imag,
+            c[0], c[1], c[2], k, int(ny), int(nz), rf, ap, (pdeg, ex, ey, ez), dc)
+    r1 = oracle.scatter_f64(*args, n_threads=1)
+    r4 = oracle.scatter_f64(*args, n_threads=4)
+    assert np.abs(r1 - r4).max() <= 1e-14 * np.abs(r1).max()
+
+
+def test_oracle_interact_matches_reference_interact_beam_cpu(golden):
+    e = golden("interact_cpu.npz")
+    t = golden("tables.npz")
+    from mosaic_gb300.tables import ScatteringTables
+    T = ScatteringTables()
+    chunks = [(e["pos0"], e["spc0"]), (e["pos1"], e["spc1"])]
+    labels = ["Na", "Cl", "Cu"]
+    for i in range(3):
+        rf, ap, dc = (bool(v) for v in e[f"flags{i}"])
+        got = oracle.interact_cpu(chunks, e["coords"], tuple(e["shape"]), e["rotation"],
+                                  e["translation"], float(e["energy"]), T.f0,
+                                  {l: T.f0_zero(l) for l in labels}, T.f1f2, e["E0"], e["grid"],
+                                  tuple(e["pol"]), remove_forward=rf, apply_polarization=ap,
+                                  spherical_decay=dc)
+        ref = e[f"out{i}"]
+        assert got.shape == ref.shape
+        assert np.abs(got - ref).max() / np.abs(ref).max() <= 1e-5, i
+    assert t["tab_f0"].shape[1] == 11
+
+
+def test_oracle_ein_bilinear_bit_exact(golden):
+    d = golden("ein.npz")
+    du, dv, uc, vc = d["grid"]
+    got = oracle.ein_bilinear(d["pos"], d["E0"], du, dv, uc, vc)
+    assert np.array_equal(got, d["ein"])
+    assert np.any(got == 0) and np.any(got != 0)   # some atoms fall outside the grid
+
+
+def test_oracle_polarization_and_anomalous(golden):
+    p = golden("polarization.npz")
+    for i in range(len(p["rho"])):
+        vec = None if np.isnan(p["vec"][i][0]) else p["vec"][i]
+        deg = None if np.isnan(p["deg"][i]) else float(p["deg"][i])
+        assert np.array_equal(np.array(oracle.polarization_state(p["rho"][i], vec, deg)),
+                              p["state"][i])
+    t = golden("tables.npz")
+    from mosaic_gb300.tables import ScatteringTables
+    T = ScatteringTables()
+    for i, el in enumerate(t["tab_elements"]):
+        for j, E in enumerate(t["tab_energies"]):
+            assert oracle.anomalous(float(E), T.f1f2[str(el)]) == t["tab_anom"][i, j]
+
+
+def test_oracle_prop_mul_matches_reference(golden):
+    d = golden("propagation.npz")
+    k = float(d["k"])
+    for i in range(3):
+        dd, z = d[f"mulcase{i}"]
+        got = oracle.prop_mul_f64(d["Fs"], d[f"ky{i}"], d[f"kz{i}"], k, z)
+        ref = d[f"mul{i}"]
+        # the reference evaluates the phase in float32 (cosf/sinf)
+        scale = np.abs(d["Fs"]).max()
+        assert np.abs(got - ref).max() / scale <= 5e-5, i
