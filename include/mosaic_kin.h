@@ -170,6 +170,13 @@ int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *sp, const mk_physi
                      const mk_pixels *px, const mk_launch *launch, double *out,
                      int accumulate, void *workspace, size_t ws_bytes, void *stream);
 
+/* --- diagnostics ------------------------------------------------------ */
+/* Launch a kernel whose bounded mbarrier wait is never satisfied: it gives
+ * up after limit_ns (<= 1 s), records a timeout, and mk_sync_status() then
+ * returns MK_ETIMEOUT. Exercises the error path of the tile-copy waits
+ * without faulting or hanging the GPU. No counterpart in the reference. */
+int mk_debug_wait_timeout(uint64_t limit_ns, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -152,6 +152,7 @@ SIGNATURES = {
     "mk_kin_plain_f64": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, ctypes.POINTER(MkSpecies),
                                         ctypes.POINTER(MkPhysics), ctypes.POINTER(MkPixels),
                                         ctypes.c_int, _vp, ctypes.c_int, _vp, ctypes.c_size_t, _vp]),
+    "mk_debug_wait_timeout": (ctypes.c_int, [ctypes.c_uint64, _vp]),
     "mk_split_plan": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkPixels),
                                      ctypes.POINTER(MkLaunch), ctypes.POINTER(ctypes.c_int)]),
     "mk_kin_split_f32": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkSpecies),

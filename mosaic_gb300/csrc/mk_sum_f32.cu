@@ -237,6 +237,34 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
     }
 }
 
+// Test hook for the bounded-wait path: one block waits on an mbarrier that
+// no copy and no thread ever completes, gives up after `limit_ns`, records
+// the timeout in the status word and returns. Nothing is in flight, so the
+// context stays usable.
+__global__ void mk_wait_probe_kernel(uint64_t limit_ns, int *status)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mk_mbar_init(&bar, 1);
+        mk_fence_barrier_init();
+    }
+    __syncthreads();
+    const bool ok = mk_mbar_wait_bounded(&bar, 0, limit_ns);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(status, MK_DEV_TIMEOUT_TMA);
+}
+
+extern "C" int mk_debug_wait_timeout(uint64_t limit_ns, void *stream)
+{
+    MK_REQUIRE(limit_ns > 0 && limit_ns <= 1000000000ull,
+               "mk_debug_wait_timeout: limit must be in (0, 1 s]");
+    mk_register_status_reader(mk_split_read_status);
+    int *status = nullptr;
+    MK_CHECK_CUDA(cudaGetSymbolAddress((void **)&status, g_split_status));
+    mk_wait_probe_kernel<<<1, 32, 0, mk_stream(stream)>>>(limit_ns, status);
+    MK_CHECK_CUDA(cudaGetLastError());
+    return MK_OK;
+}
+
 // out[p] (+)= scale * phasor[p] * sum_s partial[s][p], slices added in order in FP64.
 __global__ void mk_reduce_kernel(const double2 *__restrict__ partial, int slices, int n_pix,
                                  const double2 *__restrict__ phasor, double scale,

@@ -135,7 +135,148 @@ def nacl_screw_8m(cells=(160, 160, 40), npix=512, chunk_grid=(4, 4), b_A=3.99):
                          reflection="(002), G parallel to the dislocation line"))
 
 
-CONFIGS = {"fcc_cu_32k": fcc_cu_32k, "nacl_screw_8m": nacl_screw_8m}
+def random_rotations(n, rng):
+    """n rotation matrices uniform on SO(3) (unit quaternions, Shoemake)."""
+    u1, u2, u3 = rng.random((3, n))
+    q = np.stack([np.sqrt(1 - u1) * np.sin(2 * np.pi * u2), np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
+                  np.sqrt(u1) * np.sin(2 * np.pi * u3), np.sqrt(u1) * np.cos(2 * np.pi * u3)], 1)
+    x, y, z, w = q.T
+    return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], 1),
+                     np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], 1),
+                     np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], 1)], 1)
+
+
+def polycrystal_positions(box_A=600.0, n_grains=64, a=3.615, seed=2026, voxel_A=10.0,
+                          stacking_fault=True, device=None):
+    """Voronoi polycrystal of fcc grains filling a cube of side ``box_A``
+    centred on 0. Each grain: seeded centre, uniformly random orientation,
+    and (optionally) one intrinsic stacking fault -- the atoms on the far
+    side of the grain's (111) plane through its centre shifted by
+    (a/6)[1 1 -2] in the grain frame. Returns (N, 3) float32 and the grain id
+    per atom. Runs on the GPU through torch when ``device`` is a CUDA device."""
+    import torch
+    rng = np.random.default_rng(seed)
+    half = box_A / 2.0
+    seeds = rng.random((n_grains, 3)) * box_A - half
+    rots = random_rotations(n_grains, rng)
+    dev = torch.device(device) if device is not None else torch.device("cpu")
+    S = torch.tensor(seeds, dtype=torch.float64, device=dev)
+    nv = int(np.ceil(box_A / voxel_A))
+    g1 = (torch.arange(nv, dtype=torch.float64, device=dev) + 0.5) * (box_A / nv) - half
+    V = torch.stack(torch.meshgrid(g1, g1, g1, indexing="ij"), -1).reshape(-1, 3)
+    lab = torch.cdist(V, S).argmin(1)
+    basis = torch.tensor(fcc_basis(), dtype=torch.float64, device=dev)
+    out_pos, out_gid = [], []
+    margin = 2.0 * voxel_A
+    for g in range(n_grains):
+        Vg = V[lab == g]
+        if Vg.shape[0] == 0:
+            continue
+        lo = torch.clamp(Vg.min(0).values - margin, min=-half)
+        hi = torch.clamp(Vg.max(0).values + margin, max=half)
+        Rg = torch.tensor(rots[g], dtype=torch.float64, device=dev)
+        c = S[g]
+        corners = torch.stack([torch.stack([x, y, z]) for x in (lo[0], hi[0])
+                               for y in (lo[1], hi[1]) for z in (lo[2], hi[2])])
+        loc = (corners - c) @ Rg / a                      # grain-frame lattice coordinates
+        n0 = torch.floor(loc.min(0).values).long() - 1
+        n1 = torch.ceil(loc.max(0).values).long() + 1
+        rngs = [torch.arange(int(n0[i]), int(n1[i]) + 1, device=dev, dtype=torch.float64) for i in range(3)]
+        cells = torch.stack(torch.meshgrid(*rngs, indexing="ij"), -1).reshape(-1, 1, 3)
+        local = ((cells + basis[None]) * a).reshape(-1, 3)
+        x = local @ Rg.T + c
+        keep = ((x >= lo) & (x <= hi)).all(1)
+        x, local = x[keep], local[keep]
+        keep = torch.cdist(x, S).argmin(1) == g
+        x, local = x[keep], local[keep]
+        if stacking_fault:
+            nrm = torch.tensor([1.0, 1.0, 1.0], dtype=torch.float64, device=dev) / np.sqrt(3.0)
+            side = (local @ nrm) > 0
+            shift = torch.tensor([1.0, 1.0, -2.0], dtype=torch.float64, device=dev) * (a / 6.0)
+            x = x + side[:, None].double() * (Rg @ shift)[None]
+        out_pos.append(x.float().cpu().numpy())
+        out_gid.append(np.full(x.shape[0], g, dtype=np.int32))
+    return np.concatenate(out_pos), np.concatenate(out_gid)
+
+
+def cu_polycrystal_18m(box_A=600.0, n_grains=64, npix=1024, chunk_atoms=1_000_000, device=None,
+                       seed=2026):
+    """Large chunked polycrystal: 64 Voronoi fcc Cu grains in a 60 nm cube
+    (~18.3M atoms) in 1M-atom chunks, one stacking fault per grain; 1024^2
+    pixels at 0.5 m, 12 keV, centred at Cu(111)."""
+    a, E = 3.615, 12000.0
+    pos, gid = polycrystal_positions(box_A, n_grains, a, seed, device=device)
+    chunks = [(pos[i:i + chunk_atoms], (np.zeros(min(chunk_atoms, pos.shape[0] - i), np.uint8),
+                                        np.array(["Cu"])))
+              for i in range(0, pos.shape[0], chunk_atoms)]
+    sample = ChunkedSample(chunks, dimensions=(box_A,) * 3)
+    theta = bragg_theta(a / np.sqrt(3.0), E)
+    det = _detector((npix, npix), 5.5e5, 0.5e10, 2 * theta)
+    B = _beam(E, 2.5 * box_A * np.sqrt(3.0))
+    return Workload("cu_polycrystal_18m", sample, det, Stage(), B,
+                    dict(apply_polarization=True, spherical_decay=False, remove_forward=False),
+                    dict(a=a, energy_eV=E, theta_deg=np.degrees(theta), grains=n_grains,
+                         box_A=box_A, npix=npix, distance_m=0.5, pitch_um=55.0, seed=seed,
+                         stacking_fault="(a/6)[1 1 -2] beyond the grain's (111) plane"))
+
+
+def bump_field_crystal(cells=100, a=3.615, n_bumps=8, amp_A=0.3, width_A=50.0, seed=4):
+    """fcc Cu, [111] along z, displaced by a smooth field
+    u(r) = sum_b amp n_b exp(-|r - c_b|^2 / (2 width^2)), seeded centres
+    (uniform in the crystal) and unit directions."""
+    rng = np.random.default_rng(seed)
+    pos = lattice(a, (cells,) * 3, fcc_basis())
+    pos -= pos.mean(axis=0)
+    half = 0.5 * cells * a
+    centres = rng.random((n_bumps, 3)) * 2 * half - half
+    dirs = rng.standard_normal((n_bumps, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    u = np.zeros_like(pos)
+    for c, n in zip(centres, dirs):
+        r2 = ((pos - c) ** 2).sum(1)
+        u += amp_A * np.exp(-r2 / (2 * width_A ** 2))[:, None] * n[None]
+    pos = (pos + u) @ align_rotation([1, 1, 1], [0, 0, 1]).T
+    return pos.astype(np.float32), dict(centres=centres.tolist(), dirs=dirs.tolist(), seed=seed)
+
+
+def rocking_frames(theta_b, n_theta=181, half_range_deg=0.5, chi_offsets_deg=(-0.3, -0.1, 0.1, 0.3),
+                   roi_sides=(64, 128, 256, 512)):
+    """Frames of the rocking scan: mu = theta_B + dtheta (n_theta steps over
+    +-half_range) for every chi offset; ROI side cycles through roi_sides by
+    frame index."""
+    frames = []
+    for ci, chi in enumerate(chi_offsets_deg):
+        for ti in range(n_theta):
+            dth = -half_range_deg + ti * (2 * half_range_deg / (n_theta - 1))
+            f = len(frames)
+            frames.append(dict(mu=float(theta_b + np.radians(dth)), chi=float(np.radians(chi)),
+                               roi=int(roi_sides[f % len(roi_sides)])))
+    return frames
+
+
+def cu_bumps_scan_4m(cells=100, npix=512, n_theta=181, chi_offsets_deg=(-0.3, -0.1, 0.1, 0.3),
+                     roi_sides=(64, 128, 256, 512)):
+    """Batched scan: 4M-atom bump-field crystal, rocking scan of n_theta
+    steps over +-0.5 deg times the chi offsets, uneven ROIs."""
+    a, E = 3.615, 10000.0
+    pos, meta = bump_field_crystal(cells, a)
+    sample = ChunkedSample([(pos, (np.zeros(pos.shape[0], np.uint8), np.array(["Cu"])))])
+    theta = bragg_theta(a / np.sqrt(3.0), E)
+    det = _detector((npix, npix), 5.5e5, 1.0e10, 2 * theta)
+    st = Stage()
+    st.set_motor_value("mu", theta, degrees=False)
+    diag = float(np.linalg.norm(pos.max(0) - pos.min(0)))
+    B = _beam(E, max(1000.0, 2.5 * diag))
+    frames = rocking_frames(theta, n_theta, 0.5, chi_offsets_deg, roi_sides)
+    return Workload("cu_bumps_scan_4m", sample, det, st, B,
+                    dict(apply_polarization=True, spherical_decay=False, remove_forward=False),
+                    dict(a=a, energy_eV=E, theta_deg=np.degrees(theta), cells=cells, npix=npix,
+                         distance_m=1.0, pitch_um=55.0, frames=frames,
+                         chi_offsets_deg=list(chi_offsets_deg), roi_sides=list(roi_sides), **meta))
+
+
+CONFIGS = {"fcc_cu_32k": fcc_cu_32k, "nacl_screw_8m": nacl_screw_8m,
+           "cu_polycrystal_18m": cu_polycrystal_18m, "cu_bumps_scan_4m": cu_bumps_scan_4m}
 
 
 def build(name, **kw):
