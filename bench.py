@@ -216,7 +216,10 @@ def run_ours(args):
     tiles = engine.Tiles(atoms, B.k, B._kernel_tile_atoms, device=dev)
     pix = engine.Pixels(coords_m, ny, nz, phys, device=dev)
     third, fresnel, tol, diag = B.split_budget(tiles, pix.r0_min())
-    launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel))
+    if args.profile:
+        launch, tune_tbl = autotune.lookup(pix.n, tiles), []
+    else:
+        launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel))
     B._kernel_launch = launch
     amp_real = tiles.amp_is_real()
     split_times = []
@@ -257,6 +260,12 @@ def run_ours(args):
     split_ms = float(np.mean([a.elapsed_time(b) for a, b in split_times]))
     value = terms * world / (ms * 1e-3) / 1e9
     clocks = sampler.summary()
+    if args.profile:
+        # Kernel-profile run: one configuration, no side legs.
+        if rank == 0:
+            print(json.dumps({"profile": args.config, "ms_per_step": ms, "split_ms": split_ms,
+                              "value": value, "launch": launch, "fresnel": bool(fresnel)}))
+        return
 
     # End to end through the public entry point with host buffers.
     e2e_times = []
@@ -347,6 +356,8 @@ def main():
     ap.add_argument("--config", default="nacl_screw_8m")
     ap.add_argument("--fp64-subset", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="kernel-profile run: cached launch shape, timed steps only")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -12,7 +12,7 @@
  * with b the incident direction (+x in the lab frame). Two kernels:
  *   - mk_kin_plain_f64: the FP64 direct sum, term for term as the reference
  *     CPU kernel (drop-in and on-device oracle);
- *   - mk_kin_split_f32: the FP32 split-phase sum over Morton-ordered atom
+ *   - mk_kin_split_f32: the FP32 split-phase sum over Hilbert-ordered atom
  *     tiles with FP64 tile origins, Kahan-compensated across tiles and an
  *     FP64 cross-slice reduction.
  *
@@ -75,14 +75,30 @@ typedef struct {
  * mk_pixels_prepare (replaces the per-pixel prologue of Beam.py:716-746 and
  * pixel_phasor, Beam.py:9241-9255). */
 typedef struct {
-    int ny, nz;           /* detector shape; n_pix = ny * nz */
-    const double *xyz;    /* device (3, n_pix) pixel coordinates [m] */
+    int ny, nz;           /* detector (or ROI) shape; n_pix = ny * nz */
+    const double *xyz;    /* device (n_pix, 3) pixel coordinates [m] */
     double *r0;           /* device (n_pix) |P| */
-    double *qcut;         /* device (n_pix) forward-removal cut-off Q_cut [1/m] */
-    double *qc;           /* device (3, n_pix) (k / 2 pi)(b - u_hat) [cycles/m] */
-    float *uf;            /* device (4, n_pix) u_hat (x, y, z) and 1/|P| as float */
-    double *phasor;       /* device (2, n_pix) exp(i k |P|) */
+    double *q;            /* device (n_pix, 4): (k / 2 pi)(b - u_hat) [cycles/m], Q_cut [1/m] */
+    float *u;             /* device (n_pix, 4): u_hat (x, y, z) and 1/|P| as float */
+    double *phasor;       /* device (n_pix, 2) exp(i k |P|) */
 } mk_pixels;
+
+/* One frame of a batched launch (an exposure's pixels, or a scan step's
+ * ROI), as filled by mk_scan_plan and read by the kernel from device
+ * memory. The frames' pixels are consecutive in one set of mk_pixels
+ * arrays; b and e are the incident direction and polarization vector in the
+ * frame of the atoms (the sample frame for scans). 64 bytes. */
+typedef struct {
+    long long pix_off;    /* first pixel of the frame in the concatenated pixel arrays */
+    long long part_off;   /* first entry of its partial fields in the workspace */
+    long long item_off;   /* first work item of the frame */
+    int n_pix;            /* pixels in the frame */
+    int slices;           /* tile ranges summed separately (FP64 reduction) */
+    int tiles_per_slice;
+    int pix_blocks;       /* ceil(n_pix / (threads * pix_per_thread)) */
+    float b[3];
+    float e[3];
+} mk_frame_desc;
 
 /* Atom tiles for the split-phase kernel, filled by mk_tiles_build. Tiles
  * hold `tile_atoms` atoms of one species (the last tile of a species is
@@ -90,7 +106,7 @@ typedef struct {
 typedef struct {
     int n_tiles;
     int tile_atoms;       /* power of two, 128..4096 */
-    double *origin;       /* device (4, n_tiles): origin x, y, z [m], radius [m] */
+    double *origin;       /* device (n_tiles, 4): origin x, y, z [m], radius [m] */
     int *species;         /* device (n_tiles) species index */
     float *pos;           /* device (n_tiles*tile_atoms, 4): k/2pi (a - o) [cycles], |.|^2 */
     float *amp;           /* device (n_tiles*tile_atoms, 2): incident amplitude */
@@ -135,10 +151,12 @@ int mk_atoms_lab(int64_t n, const float *pos_in, const float *rot, const float *
 
 /* Bytes of workspace mk_tiles_build needs for n atoms. */
 size_t mk_tiles_workspace_size(int64_t n);
-/* Species-partitioned Morton order and tile build. Replaces _partition,
- * _morton_order_gpu, _chunk_origins_gpu and _stage (Beam.py:9297-9319,
- * 1204-1300, 9265-9294) with tiles of `tiles->tile_atoms` atoms whose origin
- * is the FP64 bounding-box centre.
+/* Species-partitioned space-filling order and tile build. Replaces
+ * _partition, _morton_order_gpu, _chunk_origins_gpu and _stage
+ * (Beam.py:9297-9319, 1204-1300, 9265-9294): atoms sorted by (species,
+ * Hilbert index) -- a Hilbert curve instead of the reference's Z-order, so
+ * no tile spans a Z-order jump -- then cut into tiles of `tiles->tile_atoms`
+ * atoms whose origin is the FP64 bounding-box centre.
  *   pos: device (n, 3) float64 [m]; species: device (n) int32 in [0, S);
  *   amp: device (n, 2) float32; counts: host (S) atoms per species.
  *   tiles->n_tiles must equal sum_s ceil(counts[s] / tile_atoms). */
@@ -159,16 +177,41 @@ int mk_kin_plain_f64(int64_t n, const double *pos, const int *species, const flo
                      int slices, double *out, int accumulate, void *workspace,
                      size_t ws_bytes, void *stream);
 
-/* Slice count mk_kin_split_f32 will use for this launch (resolves
- * launch->slices <= 0), so the caller can size the workspace. */
+/* Workspace bytes mk_kin_split_f32 needs for this launch (its work-item
+ * counter and the partial fields of the slices it will choose). */
 int mk_split_plan(const mk_tiles *tiles, const mk_pixels *px, const mk_launch *launch,
-                  int *slices_out);
+                  size_t *ws_bytes_out);
 
-/* FP32 split-phase sum over tiles (replaces the `mosaic_fast` kernel and its
- * dispatch, Beam.py:8114-8632, 9362-9496). Same output convention. */
+/* FP32 split-phase sum over tiles for one exposure (replaces the
+ * `mosaic_fast` kernel and its dispatch, Beam.py:8114-8632, 9362-9496).
+ * Same output convention as mk_kin_plain_f64. */
 int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *sp, const mk_physics *phys,
                      const mk_pixels *px, const mk_launch *launch, double *out,
                      int accumulate, void *workspace, size_t ws_bytes, void *stream);
+
+/* --- batched scans ------------------------------------------------------ */
+/* Plan a batched launch of n_frames frames (host only, no GPU work):
+ * frame_pixels (n_frames) pixels per frame; beam_dirs / pol_es (n_frames, 3)
+ * incident direction and polarization vector per frame in the sample frame.
+ * Fills frames_out (host, n_frames) and the totals of work items and
+ * partial-field entries. Copy frames_out to the device for mk_kin_scan_f32.
+ * Replaces the per-step loop of experiment.scan_nD (Experiment.py:285-336),
+ * which re-runs the whole exposure per step. */
+int mk_scan_plan(int n_frames, const int *frame_pixels, const double *beam_dirs,
+                 const double *pol_es, const mk_tiles *tiles, const mk_launch *launch,
+                 mk_frame_desc *frames_out, long long *n_items, long long *n_partial);
+size_t mk_scan_workspace_size(long long n_partial);
+
+/* All frames of a scan in one persistent launch plus the FP64 reduction:
+ * px holds the concatenated pixels of every frame (ny = total pixels,
+ * nz = 1), each frame's prologue prepared with its own beam direction;
+ * out (total pixels, 2) complex128 fields (r_e included);
+ * intensity_sums (n_frames) sum of |A|^2 per frame, or NULL. Only kernel
+ * launches and a memset: capturable in a CUDA graph when n_frames > 1. */
+int mk_kin_scan_f32(const mk_tiles *tiles, const mk_species *sp, const mk_physics *phys,
+                    const mk_pixels *px, int n_frames, const mk_frame_desc *frames_dev,
+                    long long n_items, long long n_partial, const mk_launch *launch, double *out,
+                    double *intensity_sums, void *workspace, size_t ws_bytes, void *stream);
 
 /* --- diagnostics ------------------------------------------------------ */
 /* Launch a kernel whose bounded mbarrier wait is never satisfied: it gives

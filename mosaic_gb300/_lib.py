@@ -123,7 +123,14 @@ class MkPhysics(ctypes.Structure):
 
 class MkPixels(ctypes.Structure):
     _fields_ = [("ny", ctypes.c_int), ("nz", ctypes.c_int), ("xyz", _vp), ("r0", _vp),
-                ("qcut", _vp), ("qc", _vp), ("uf", _vp), ("phasor", _vp)]
+                ("q", _vp), ("u", _vp), ("phasor", _vp)]
+
+
+class MkFrameDesc(ctypes.Structure):
+    _fields_ = [("pix_off", ctypes.c_longlong), ("part_off", ctypes.c_longlong),
+                ("item_off", ctypes.c_longlong), ("n_pix", ctypes.c_int), ("slices", ctypes.c_int),
+                ("tiles_per_slice", ctypes.c_int), ("pix_blocks", ctypes.c_int),
+                ("b", ctypes.c_float * 3), ("e", ctypes.c_float * 3)]
 
 
 class MkTiles(ctypes.Structure):
@@ -154,7 +161,15 @@ SIGNATURES = {
                                         ctypes.c_int, _vp, ctypes.c_int, _vp, ctypes.c_size_t, _vp]),
     "mk_debug_wait_timeout": (ctypes.c_int, [ctypes.c_uint64, _vp]),
     "mk_split_plan": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkPixels),
-                                     ctypes.POINTER(MkLaunch), ctypes.POINTER(ctypes.c_int)]),
+                                     ctypes.POINTER(MkLaunch), ctypes.POINTER(ctypes.c_size_t)]),
+    "mk_scan_plan": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, ctypes.POINTER(MkTiles),
+                                    ctypes.POINTER(MkLaunch), _vp, ctypes.POINTER(ctypes.c_longlong),
+                                    ctypes.POINTER(ctypes.c_longlong)]),
+    "mk_scan_workspace_size": (ctypes.c_size_t, [ctypes.c_longlong]),
+    "mk_kin_scan_f32": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkSpecies),
+                                       ctypes.POINTER(MkPhysics), ctypes.POINTER(MkPixels),
+                                       ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong,
+                                       ctypes.POINTER(MkLaunch), _vp, _vp, _vp, ctypes.c_size_t, _vp]),
     "mk_kin_split_f32": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkSpecies),
                                         ctypes.POINTER(MkPhysics), ctypes.POINTER(MkPixels),
                                         ctypes.POINTER(MkLaunch), _vp, ctypes.c_int, _vp,

@@ -10,28 +10,21 @@
 // origin and (ii) the per-pixel phasor exp(i k |P|).
 __global__ void mk_pixels_kernel(int ny, int nz, const double *__restrict__ xyz, double kappa,
                                  double k, double bx, double by, double bz, double *__restrict__ r0,
-                                 double *__restrict__ qcut, double *__restrict__ qc,
-                                 float *__restrict__ uf, double *__restrict__ phasor)
+                                 double4 *__restrict__ q, float4 *__restrict__ u,
+                                 double2 *__restrict__ phasor)
 {
     const int n = ny * nz;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const double tx = xyz[p], ty = xyz[n + p], tz = xyz[2 * n + p];
+    const double tx = xyz[3 * p], ty = xyz[3 * p + 1], tz = xyz[3 * p + 2];
     const double R = sqrt(tx * tx + ty * ty + tz * tz);
     double ux = 0.0, uy = 0.0, uz = 0.0;
     if (R > 0.0) { ux = tx / R; uy = ty / R; uz = tz / R; }
     r0[p] = R;
-    qc[p] = kappa * (bx - ux);
-    qc[n + p] = kappa * (by - uy);
-    qc[2 * n + p] = kappa * (bz - uz);
-    uf[p] = (float)ux;
-    uf[n + p] = (float)uy;
-    uf[2 * n + p] = (float)uz;
-    uf[3 * n + p] = R > 0.0 ? (float)(1.0 / R) : 0.f;
+    u[p] = make_float4((float)ux, (float)uy, (float)uz, R > 0.0 ? (float)(1.0 / R) : 0.f);
     double s, c;
     sincos(fmod(k * R, MK_TWO_PI), &s, &c);
-    phasor[2 * p] = c;
-    phasor[2 * p + 1] = s;
+    phasor[p] = make_double2(c, s);
     // Q_cut: half the pixel diagonal in Q from the right and upper neighbours,
     // edge pixels taking the inner one (compute_scattering_cffi, Beam.py:716-746).
     const int col = p % ny, row = p / ny;
@@ -40,21 +33,21 @@ __global__ void mk_pixels_kernel(int ny, int nz, const double *__restrict__ xyz,
     double q2 = 0.0;
     for (int j = 0; j < 2; ++j) {
         const int m = j ? nb1 : nb0;
-        const double rx = xyz[m], ry = xyz[n + m], rz = xyz[2 * n + m];
+        const double rx = xyz[3 * m], ry = xyz[3 * m + 1], rz = xyz[3 * m + 2];
         const double Rr = sqrt(rx * rx + ry * ry + rz * rz);
         double cd = (Rr > 0.0) ? (ux * rx + uy * ry + uz * rz) / Rr : 1.0;
         cd = fmin(1.0, fmax(-1.0, cd));
-        const double q = k * sqrt(fmax(0.0, 2.0 * (1.0 - cd)));
-        q2 += q * q;
+        const double qn = k * sqrt(fmax(0.0, 2.0 * (1.0 - cd)));
+        q2 += qn * qn;
     }
-    qcut[p] = 0.5 * sqrt(q2);
+    q[p] = make_double4(kappa * (bx - ux), kappa * (by - uy), kappa * (bz - uz), 0.5 * sqrt(q2));
 }
 
 extern "C" int mk_pixels_prepare(const mk_pixels *px, const mk_physics *phys, void *stream)
 {
     MK_REQUIRE(px && phys, "mk_pixels_prepare: null argument");
     MK_REQUIRE(px->ny > 0 && px->nz > 0, "mk_pixels_prepare: empty detector (%d x %d)", px->ny, px->nz);
-    MK_REQUIRE(px->xyz && px->r0 && px->qcut && px->qc && px->uf && px->phasor,
+    MK_REQUIRE(px->xyz && px->r0 && px->q && px->u && px->phasor,
                "mk_pixels_prepare: null pixel buffer");
     MK_REQUIRE(phys->k > 0.0, "mk_pixels_prepare: k must be positive");
     const int64_t n = (int64_t)px->ny * px->nz;
@@ -63,7 +56,8 @@ extern "C" int mk_pixels_prepare(const mk_pixels *px, const mk_physics *phys, vo
     const int th = 256;
     mk_pixels_kernel<<<(unsigned)((n + th - 1) / th), th, 0, mk_stream(stream)>>>(
         px->ny, px->nz, px->xyz, kappa, phys->k, phys->beam_dir[0], phys->beam_dir[1],
-        phys->beam_dir[2], px->r0, px->qcut, px->qc, px->uf, px->phasor);
+        phys->beam_dir[2], px->r0, reinterpret_cast<double4 *>(px->q),
+        reinterpret_cast<float4 *>(px->u), reinterpret_cast<double2 *>(px->phasor));
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
 }
@@ -192,9 +186,51 @@ __global__ void mk_bbox_kernel(int64_t n, const double *__restrict__ pos, unsign
     }
 }
 
-// Z-order key: species in bits 57..63, then 19 bits per axis interleaved
-// (x in bit 0 of each triple). A plain bit loop: the key is built once per
-// atom per call.
+// Position along a 3-D Hilbert curve of 2^19 cells per axis (the
+// axes-to-transpose construction of J. Skilling, "Programming the Hilbert
+// curve", AIP Conf. Proc. 707, 381 (2004)): undo the rotations/reflections
+// level by level, Gray-encode, then read the bits out MSB first, x first.
+// Unlike a Z-order (Morton) curve, consecutive cells are always face
+// neighbours, so a run of consecutive atoms never spans two distant corners
+// of the sample and every tile stays compact.
+#define MK_HILBERT_BITS 19
+
+__device__ __forceinline__ unsigned long long mk_hilbert3(uint32_t x, uint32_t y, uint32_t z)
+{
+    uint32_t X[3] = {x, y, z};
+    for (uint32_t Q = 1u << (MK_HILBERT_BITS - 1); Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = 1u << (MK_HILBERT_BITS - 1); Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    unsigned long long h = 0;
+    for (int b = MK_HILBERT_BITS - 1; b >= 0; --b) {
+        h = (h << 1) | ((X[0] >> b) & 1u);
+        h = (h << 1) | ((X[1] >> b) & 1u);
+        h = (h << 1) | ((X[2] >> b) & 1u);
+    }
+    return h;
+}
+
+// Sort key: species in bits 57..63, then the Hilbert index of the atom on an
+// isotropic grid over the bounding box (one cell size for all three axes,
+// so slabs and rods are not quantised anisotropically).
 __global__ void mk_keys_kernel(int64_t n, const double *__restrict__ pos,
                                const int *__restrict__ species,
                                const unsigned long long *__restrict__ bb,
@@ -202,22 +238,21 @@ __global__ void mk_keys_kernel(int64_t n, const double *__restrict__ pos,
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    double lo[3], span = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        lo[c] = mk_unordered(bb[c]);
+        span = fmax(span, mk_unordered(bb[3 + c]) - lo[c]);
+    }
+    if (!(span > 0.0)) span = 1.0;
     uint32_t q[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const double lo = mk_unordered(bb[c]), hi = mk_unordered(bb[3 + c]);
-        const double span = hi - lo > 0.0 ? hi - lo : 1.0;
-        double f = (pos[3 * i + c] - lo) / span;
+        double f = (pos[3 * i + c] - lo[c]) / span;
         f = fmin(fmax(f, 0.0), 1.0);
-        q[c] = (uint32_t)(f * 524287.0);   // 2^19 - 1
+        q[c] = (uint32_t)(f * (double)((1u << MK_HILBERT_BITS) - 1));
     }
-    unsigned long long code = 0;
-    for (int b = 0; b < 19; ++b) {
-        code |= (unsigned long long)((q[0] >> b) & 1u) << (3 * b);
-        code |= (unsigned long long)((q[1] >> b) & 1u) << (3 * b + 1);
-        code |= (unsigned long long)((q[2] >> b) & 1u) << (3 * b + 2);
-    }
-    keys[i] = ((unsigned long long)species[i] << 57) | code;
+    keys[i] = ((unsigned long long)species[i] << 57) | mk_hilbert3(q[0], q[1], q[2]);
     idx[i] = (int)i;
 }
 

@@ -1,4 +1,5 @@
-// FP32 split-phase kinematic sum over Morton-ordered atom tiles (sm_103a).
+// FP32 split-phase kinematic sum over Hilbert-ordered atom tiles (sm_103a),
+// one persistent kernel for single exposures and batched scans.
 //
 // The phase of atom a = o + d (o its tile origin) at pixel P splits as
 //   k (b.a + |P - a|) = k |P|                                 per pixel, FP64 phasor
@@ -9,7 +10,7 @@
 // u = P/|P|, u' = (P - o)/|P - o| = u - (o - (u.o) u)/|P| + O(|o|^2/|P|^2).
 // Everything is carried in cycles (phase / 2 pi). The dominant part of the
 // (tile, pixel) phase, (k/2pi)(b - u).o, is an FP64 dot product of the
-// per-pixel vector qc (from mk_pixels_prepare) with the FP64 tile origin,
+// per-pixel vector q (from mk_pixels_prepare) with the FP64 tile origin,
 // reduced mod 1 in FP64; the rest is small and FP32. Inside the tile the
 // term phase is w.D (+ the |d|^2 term when `FRESNEL`), w = b - u', D the
 // float32 offset in cycles: 3 FMA, a mod-1 reduction, and sin/cos on the MUFU.
@@ -17,9 +18,18 @@
 // The direction-dependent factor (f0 + f' + i f'') exp(-B s^2) sqrt(P_pol)
 // [R0/r] is evaluated once per (tile, pixel) at the tile direction u'; its
 // change across a tile is ~|d|/|P| relative. Per-tile sums are folded into
-// the per-pixel accumulators with Kahan compensation; slices of the tile
-// range write partial fields that an FP64 pass adds in a fixed order, so the
-// result does not depend on scheduling.
+// the per-pixel accumulators with Kahan compensation.
+//
+// Work decomposition: a frame (an exposure's pixels, or one scan step's ROI)
+// is cut into pixel blocks (threads x pixels-per-thread) times tile slices;
+// every (frame, pixel block, slice) is a work item. A persistent grid of
+// one wave of blocks pulls items from an atomic counter, so frames of
+// uneven size and the last partial wave cost no idle SMs. Each item writes
+// its partial field; an FP64 pass adds the slices of every pixel in a fixed
+// order, so the result does not depend on scheduling.
+//
+// Atom tiles reach shared memory by 1-D TMA bulk copies (cp.async.bulk),
+// double-buffered on two mbarriers; every wait is bounded (mk_common.cuh).
 #include <algorithm>
 
 #include "mk_common.cuh"
@@ -46,31 +56,34 @@ static int mk_split_read_status(cudaStream_t st)
 
 struct MkSplitArgs {
     MkSpecies sp;
-    int n_pix, n_tiles, tiles_per_slice, tile_atoms;
-    const double *qc;
-    const double *qcut;
-    const float *uf;
+    int n_tiles, tile_atoms, n_frames;
+    long long n_items;
+    mk_frame_desc f0;                // the frame when n_frames == 1
+    const mk_frame_desc *frames;     // device, n_frames (n_frames > 1)
+    unsigned long long *counter;
+    const double4 *q;                // per pixel (qx, qy, qz, qcut)
+    const float4 *u;                 // per pixel (ux, uy, uz, 1/|P|)
     const double4 *origin;
     const int *tspecies;
     const float4 *tpos;
     const float2 *tamp;
     double2 *partial;
     int *status;
-    float bx, by, bz;
     float kappa;       // k / 2 pi [cycles/m]
     float k;           // [1/m]
     float s2fac;       // (k 0.25e-10 / pi)^2: s^2 = s2fac |b - u'|^2 [1/A^2]
     int apply_pol, decay, remove_forward;
-    float pdeg, ex, ey, ez;
+    float pdeg;
 };
 
 #define TWO_PI_F 6.28318530717958647692f
 
-// Scattering factor of species s at direction u' = (upx, upy, upz); w = b - u'.
-__device__ __forceinline__ float2 mk_factor(const MkSplitArgs &A, int s, float wx, float wy,
-                                           float wz, float upx, float upy, float upz, float qcut,
+// Scattering factor of species s at direction u' = b - w.
+__device__ __forceinline__ float2 mk_factor(const MkSplitArgs &A, int s, const mk_frame_desc &F,
+                                           float wx, float wy, float wz, float qcut,
                                            float decay_ratio)
 {
+    const float upx = F.b[0] - wx, upy = F.b[1] - wy, upz = F.b[2] - wz;
     const float w2 = fmaf(wz, wz, fmaf(wy, wy, wx * wx));
     const float s2 = A.s2fac * w2;
     const float *wk = A.sp.wk[s];
@@ -85,8 +98,8 @@ __device__ __forceinline__ float2 mk_factor(const MkSplitArgs &A, int s, float w
     float scale = 1.f;
     if (A.sp.has_dw) scale = __expf(-A.sp.dwb[s] * s2);
     if (A.apply_pol) {
-        const float dotv = fmaf(A.bz, upz, fmaf(A.by, upy, A.bx * upx));
-        const float er = fmaf(A.ez, upz, fmaf(A.ey, upy, A.ex * upx));
+        const float dotv = fmaf(F.b[2], upz, fmaf(F.b[1], upy, F.b[0] * upx));
+        const float er = fmaf(F.e[2], upz, fmaf(F.e[1], upy, F.e[0] * upx));
         float P = 0.5f * (1.f - A.pdeg) * fmaf(dotv, dotv, 1.f) + A.pdeg * fmaf(-er, er, 1.f);
         P = fminf(1.f, fmaxf(0.f, P));
         scale *= sqrtf(P);
@@ -95,18 +108,25 @@ __device__ __forceinline__ float2 mk_factor(const MkSplitArgs &A, int s, float w
     return make_float2(fr * scale, fi * scale);
 }
 
+__device__ __forceinline__ void mk_issue_tile(const MkSplitArgs &A, float4 *s_pos, float2 *s_amp,
+                                              uint64_t *bar, int buf, int tile, int T,
+                                              uint32_t tile_bytes)
+{
+    mk_mbar_expect_tx(&bar[buf], tile_bytes);
+    mk_tma_load_1d(s_pos + buf * T, A.tpos + (size_t)tile * T, T * sizeof(float4), &bar[buf]);
+    mk_tma_load_1d(s_amp + buf * T, A.tamp + (size_t)tile * T, T * sizeof(float2), &bar[buf]);
+}
+
 template <int NT, int PIX, bool FRESNEL, bool CPLX>
 __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ MkSplitArgs A)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int T = A.tile_atoms;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    long long *s_item = reinterpret_cast<long long *>(smem + 64);
     float4 *s_pos = reinterpret_cast<float4 *>(smem + 128);     // [2][T]
     float2 *s_amp = reinterpret_cast<float2 *>(s_pos + 2 * T);   // [2][T]
     const int tid = threadIdx.x;
-    const int n = A.n_pix;
-    const int t_lo = blockIdx.y * A.tiles_per_slice;
-    const int t_hi = min(A.n_tiles, t_lo + A.tiles_per_slice);
     const uint32_t tile_bytes = (uint32_t)T * (uint32_t)(sizeof(float4) + sizeof(float2));
 
     if (tid == 0) {
@@ -115,125 +135,142 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
         mk_fence_barrier_init();
     }
     __syncthreads();
-    if (tid == 0) {
-        for (int b = 0; b < 2 && t_lo + b < t_hi; ++b) {
-            mk_mbar_expect_tx(&bar[b], tile_bytes);
-            mk_tma_load_1d(s_pos + b * T, A.tpos + (size_t)(t_lo + b) * T, T * sizeof(float4), &bar[b]);
-            mk_tma_load_1d(s_amp + b * T, A.tamp + (size_t)(t_lo + b) * T, T * sizeof(float2), &bar[b]);
+    unsigned it = 0;   // tiles consumed by this block: selects buffer and phase
+
+    for (;;) {
+        if (tid == 0) *s_item = (long long)atomicAdd(A.counter, 1ull);
+        __syncthreads();
+        const long long item = *s_item;
+        __syncthreads();                    // s_item may be rewritten next round
+        if (item >= A.n_items) break;
+
+        // item -> (frame, pixel block, slice)
+        int f = 0;
+        if (A.n_frames > 1) {
+            int lo = 0, hi = A.n_frames - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (A.frames[mid].item_off <= item) lo = mid; else hi = mid - 1;
+            }
+            f = lo;
         }
-    }
+        const mk_frame_desc F = A.n_frames > 1 ? A.frames[f] : A.f0;
+        const long long local = item - F.item_off;
+        const int pb = (int)(local % F.pix_blocks);
+        const int slice = (int)(local / F.pix_blocks);
+        const int t_lo = slice * F.tiles_per_slice;
+        const int t_hi = min(A.n_tiles, t_lo + F.tiles_per_slice);
+        if (tid == 0) {
+            mk_issue_tile(A, s_pos, s_amp, bar, it & 1, t_lo, T, tile_bytes);
+            if (t_lo + 1 < t_hi) mk_issue_tile(A, s_pos, s_amp, bar, (it + 1) & 1, t_lo + 1, T, tile_bytes);
+        }
 
-    int pix[PIX];
-    float accr[PIX], acci[PIX], cmpr[PIX], cmpi[PIX];
-#pragma unroll
-    for (int p = 0; p < PIX; ++p) {
-        pix[p] = blockIdx.x * (NT * PIX) + p * NT + tid;
-        accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
-    }
-
-    for (int t = t_lo, it = 0; t < t_hi; ++t, ++it) {
-        const int buf = it & 1;
-        const uint32_t parity = (uint32_t)(it >> 1) & 1u;
-        const double4 o = A.origin[t];
-        const float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
-        // Per (tile, pixel): w = b - u' in registers for the atom loop.
-        float wx[PIX], wy[PIX], wz[PIX], hq[PIX];
+        int pix[PIX];
+        float accr[PIX], acci[PIX], cmpr[PIX], cmpi[PIX];
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
-            const int q = min(pix[p], n - 1);
-            const float ux = A.uf[q], uy = A.uf[n + q], uz = A.uf[2 * n + q], iR = A.uf[3 * n + q];
-            const float uo = fmaf(uz, oz, fmaf(uy, oy, ux * ox));
-            const float upx = ux - (ox - uo * ux) * iR;
-            const float upy = uy - (oy - uo * uy) * iR;
-            const float upz = uz - (oz - uo * uz) * iR;
-            wx[p] = A.bx - upx;
-            wy[p] = A.by - upy;
-            wz[p] = A.bz - upz;
-            // 1 / (2 kappa |P - o|) for the |d|^2 term (D is in cycles).
-            hq[p] = FRESNEL ? 0.5f * iR / (A.kappa * fmaf(-uo, iR, 1.f)) : 0.f;
+            pix[p] = pb * (NT * PIX) + p * NT + tid;
+            accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
         }
-        const bool ok = mk_mbar_wait_bounded(&bar[buf], parity, MK_WAIT_LIMIT_NS);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                atomicExch(A.status, MK_DEV_TIMEOUT_TMA);
-                // Let any copy still in flight land before the block's shared
-                // memory is released (bounded as well).
-                mk_mbar_wait_bounded(&bar[0], 0, MK_WAIT_LIMIT_NS / 2);
-                mk_mbar_wait_bounded(&bar[1], 0, MK_WAIT_LIMIT_NS / 2);
-            }
-            return;
-        }
-        const float4 *P = s_pos + buf * T;
-        const float2 *E = s_amp + buf * T;
-        float csr[PIX], csi[PIX];
-#pragma unroll
-        for (int p = 0; p < PIX; ++p) csr[p] = csi[p] = 0.f;
-#pragma unroll 4
-        for (int j = 0; j < T; ++j) {
-            const float4 a = P[j];
-            const float2 e = E[j];
-            float db = 0.f;
-            if (FRESNEL) db = fmaf(a.z, A.bz, fmaf(a.y, A.by, a.x * A.bx));
+
+        for (int t = t_lo; t < t_hi; ++t, ++it) {
+            const int buf = it & 1;
+            const uint32_t parity = (it >> 1) & 1u;
+            const double4 o = A.origin[t];
+            const float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
+            // Per (tile, pixel): w = b - u' in registers for the atom loop.
+            float wx[PIX], wy[PIX], wz[PIX], hq[PIX];
 #pragma unroll
             for (int p = 0; p < PIX; ++p) {
-                float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
-                if (FRESNEL) {
-                    const float sp = db - lin;
-                    lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
+                const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
+                const float4 uu = A.u[g];
+                const float uo = fmaf(uu.z, oz, fmaf(uu.y, oy, uu.x * ox));
+                wx[p] = F.b[0] - (uu.x - (ox - uo * uu.x) * uu.w);
+                wy[p] = F.b[1] - (uu.y - (oy - uo * uu.y) * uu.w);
+                wz[p] = F.b[2] - (uu.z - (oz - uo * uu.z) * uu.w);
+                // 1 / (2 kappa |P - o|) for the |d|^2 term (D is in cycles).
+                hq[p] = FRESNEL ? 0.5f * uu.w / (A.kappa * fmaf(-uo, uu.w, 1.f)) : 0.f;
+            }
+            const bool ok = mk_mbar_wait_bounded(&bar[buf], parity, MK_WAIT_LIMIT_NS);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicExch(A.status, MK_DEV_TIMEOUT_TMA);
+                    // Let any copy still in flight land before the block's
+                    // shared memory is released (bounded as well).
+                    mk_mbar_wait_bounded(&bar[buf ^ 1], ((it + 1) >> 1) & 1u, MK_WAIT_LIMIT_NS / 2);
                 }
-                const float r = lin - rintf(lin);
-                float sn, cs;
-                __sincosf(r * TWO_PI_F, &sn, &cs);
-                if (CPLX) {
-                    csr[p] = fmaf(e.x, cs, fmaf(-e.y, sn, csr[p]));
-                    csi[p] = fmaf(e.x, sn, fmaf(e.y, cs, csi[p]));
-                } else {
-                    csr[p] = fmaf(e.x, cs, csr[p]);
-                    csi[p] = fmaf(e.x, sn, csi[p]);
+                return;
+            }
+            const float4 *P = s_pos + buf * T;
+            const float2 *E = s_amp + buf * T;
+            float csr[PIX], csi[PIX];
+#pragma unroll
+            for (int p = 0; p < PIX; ++p) csr[p] = csi[p] = 0.f;
+#pragma unroll 4
+            for (int j = 0; j < T; ++j) {
+                const float4 a = P[j];
+                const float2 e = E[j];
+                float db = 0.f;
+                if (FRESNEL) db = fmaf(a.z, F.b[2], fmaf(a.y, F.b[1], a.x * F.b[0]));
+#pragma unroll
+                for (int p = 0; p < PIX; ++p) {
+                    float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
+                    if (FRESNEL) {
+                        const float sp = db - lin;
+                        lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
+                    }
+                    const float r = lin - rintf(lin);
+                    float sn, cs;
+                    __sincosf(r * TWO_PI_F, &sn, &cs);
+                    if (CPLX) {
+                        csr[p] = fmaf(e.x, cs, fmaf(-e.y, sn, csr[p]));
+                        csi[p] = fmaf(e.x, sn, fmaf(e.y, cs, csi[p]));
+                    } else {
+                        csr[p] = fmaf(e.x, cs, csr[p]);
+                        csi[p] = fmaf(e.x, sn, csi[p]);
+                    }
                 }
             }
+            __syncthreads();   // every thread is done with buffer `buf`
+            if (tid == 0 && t + 2 < t_hi) {
+                mk_fence_proxy_async();
+                mk_issue_tile(A, s_pos, s_amp, bar, buf, t + 2, T, tile_bytes);
+            }
+            // Fold: tile sum x factor x exp(2 pi i phi0), Kahan-compensated.
+            const int s = A.tspecies[t];
+            const float oo = fmaf(oz, oz, fmaf(oy, oy, ox * ox));
+#pragma unroll
+            for (int p = 0; p < PIX; ++p) {
+                const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
+                const float4 uu = A.u[g];
+                const double4 qq = A.q[g];
+                const float uo = fmaf(uu.z, oz, fmaf(uu.y, oy, uu.x * ox));
+                const double q0 = qq.x * o.x + qq.y * o.y + qq.z * o.z;
+                float ph = (float)(q0 - rint(q0)) + A.kappa * 0.5f * fmaf(-uo, uo, oo) * uu.w;
+                ph -= rintf(ph);
+                float s0, c0;
+                __sincosf(ph * TWO_PI_F, &s0, &c0);
+                const float2 Fc = mk_factor(A, s, F, wx[p], wy[p], wz[p], (float)qq.w,
+                                            1.f / fmaf(-uo, uu.w, 1.f));
+                const float gr = Fc.x * c0 - Fc.y * s0, gi = Fc.x * s0 + Fc.y * c0;
+                const float tr = csr[p] * gr - csi[p] * gi;
+                const float ti = csr[p] * gi + csi[p] * gr;
+                float y = tr - cmpr[p];
+                float z = accr[p] + y;
+                cmpr[p] = (z - accr[p]) - y;
+                accr[p] = z;
+                y = ti - cmpi[p];
+                z = acci[p] + y;
+                cmpi[p] = (z - acci[p]) - y;
+                acci[p] = z;
+            }
         }
-        __syncthreads();   // every thread is done with buffer `buf`
-        if (tid == 0 && t + 2 < t_hi) {
-            mk_fence_proxy_async();
-            mk_mbar_expect_tx(&bar[buf], tile_bytes);
-            mk_tma_load_1d(s_pos + buf * T, A.tpos + (size_t)(t + 2) * T, T * sizeof(float4), &bar[buf]);
-            mk_tma_load_1d(s_amp + buf * T, A.tamp + (size_t)(t + 2) * T, T * sizeof(float2), &bar[buf]);
-        }
-        // Fold: tile sum x factor x exp(2 pi i phi0), Kahan-compensated.
-        const int s = A.tspecies[t];
-        const float oo = fmaf(oz, oz, fmaf(oy, oy, ox * ox));
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
-            const int q = min(pix[p], n - 1);
-            const float ux = A.uf[q], uy = A.uf[n + q], uz = A.uf[2 * n + q], iR = A.uf[3 * n + q];
-            const float uo = fmaf(uz, oz, fmaf(uy, oy, ux * ox));
-            const double q0 = A.qc[q] * o.x + A.qc[n + q] * o.y + A.qc[2 * n + q] * o.z;
-            float ph = (float)(q0 - rint(q0)) + A.kappa * 0.5f * fmaf(-uo, uo, oo) * iR;
-            ph -= rintf(ph);
-            float s0, c0;
-            __sincosf(ph * TWO_PI_F, &s0, &c0);
-            const float2 F = mk_factor(A, s, wx[p], wy[p], wz[p], A.bx - wx[p], A.by - wy[p],
-                                       A.bz - wz[p], (float)A.qcut[q],
-                                       1.f / fmaf(-uo, iR, 1.f));
-            const float gr = F.x * c0 - F.y * s0, gi = F.x * s0 + F.y * c0;
-            const float tr = csr[p] * gr - csi[p] * gi;
-            const float ti = csr[p] * gi + csi[p] * gr;
-            float y = tr - cmpr[p];
-            float z = accr[p] + y;
-            cmpr[p] = (z - accr[p]) - y;
-            accr[p] = z;
-            y = ti - cmpi[p];
-            z = acci[p] + y;
-            cmpi[p] = (z - acci[p]) - y;
-            acci[p] = z;
+            if (pix[p] < F.n_pix)
+                A.partial[F.part_off + (long long)slice * F.n_pix + pix[p]] =
+                    make_double2((double)accr[p] - (double)cmpr[p], (double)acci[p] - (double)cmpi[p]);
         }
-    }
-#pragma unroll
-    for (int p = 0; p < PIX; ++p) {
-        if (pix[p] < n)
-            A.partial[(size_t)blockIdx.y * n + pix[p]] =
-                make_double2((double)accr[p] - (double)cmpr[p], (double)acci[p] - (double)cmpi[p]);
     }
 }
 
@@ -265,21 +302,35 @@ extern "C" int mk_debug_wait_timeout(uint64_t limit_ns, void *stream)
     return MK_OK;
 }
 
-// out[p] (+)= scale * phasor[p] * sum_s partial[s][p], slices added in order in FP64.
-__global__ void mk_reduce_kernel(const double2 *__restrict__ partial, int slices, int n_pix,
+// out[g] (+)= scale * phasor[g] * sum_s partial[frame][s][p]: the slices of
+// every pixel added in order in FP64; frames found by binary search.
+__global__ void mk_reduce_kernel(const double2 *__restrict__ partial, long long n_total,
+                                 int n_frames, mk_frame_desc f0,
+                                 const mk_frame_desc *__restrict__ frames,
                                  const double2 *__restrict__ phasor, double scale,
                                  double2 *__restrict__ out, int accumulate)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pix) return;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_total) return;
+    int f = 0;
+    if (n_frames > 1) {
+        int lo = 0, hi = n_frames - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (frames[mid].pix_off <= g) lo = mid; else hi = mid - 1;
+        }
+        f = lo;
+    }
+    const mk_frame_desc F = n_frames > 1 ? frames[f] : f0;
+    const long long p = g - F.pix_off;
     double re = 0.0, im = 0.0;
-    for (int s = 0; s < slices; ++s) {
-        const double2 v = partial[(size_t)s * n_pix + p];
+    for (int s = 0; s < F.slices; ++s) {
+        const double2 v = partial[F.part_off + (long long)s * F.n_pix + p];
         re += v.x;
         im += v.y;
     }
     if (phasor) {
-        const double2 e = phasor[p];
+        const double2 e = phasor[g];
         const double r2 = re * e.x - im * e.y, i2 = re * e.y + im * e.x;
         re = r2;
         im = i2;
@@ -287,18 +338,45 @@ __global__ void mk_reduce_kernel(const double2 *__restrict__ partial, int slices
     re *= scale;
     im *= scale;
     if (accumulate) {
-        const double2 o = out[p];
+        const double2 o = out[g];
         re += o.x;
         im += o.y;
     }
-    out[p] = make_double2(re, im);
+    out[g] = make_double2(re, im);
+}
+
+// sums[f] = sum over the frame's pixels of |A|^2, one block per frame,
+// fixed-order tree reduction.
+__global__ void mk_frame_intensity_kernel(const double2 *__restrict__ field, int n_frames,
+                                          const mk_frame_desc *__restrict__ frames, mk_frame_desc f0,
+                                          double *__restrict__ sums)
+{
+    __shared__ double red[256];
+    const int f = blockIdx.x;
+    const mk_frame_desc F = n_frames > 1 ? frames[f] : f0;
+    double acc = 0.0;
+    for (int p = threadIdx.x; p < F.n_pix; p += blockDim.x) {
+        const double2 v = field[F.pix_off + p];
+        acc += v.x * v.x + v.y * v.y;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[f] = red[0];
 }
 
 int mk_launch_reduce(const double2 *partial, int slices, int n_pix, const double2 *phasor,
                      double scale, double2 *out, int accumulate, cudaStream_t st)
 {
-    mk_reduce_kernel<<<(n_pix + 255) / 256, 256, 0, st>>>(partial, slices, n_pix, phasor, scale, out,
-                                                          accumulate);
+    mk_frame_desc F;
+    memset(&F, 0, sizeof(F));
+    F.n_pix = n_pix;
+    F.slices = slices;
+    mk_reduce_kernel<<<(n_pix + 255) / 256, 256, 0, st>>>(partial, n_pix, 1, F, nullptr, phasor,
+                                                          scale, out, accumulate);
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
 }
@@ -334,78 +412,187 @@ static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx)
 
 static size_t mk_split_smem(int T) { return 128 + (size_t)2 * T * (sizeof(float4) + sizeof(float2)); }
 
-// Slices so that the grid fills the GPU in whole waves: minimise
-// waves(slices) x tiles-per-slice over the feasible range.
-static int mk_auto_slices(int blocks_x, int n_tiles, int resident)
-{
-    int best = 1;
-    double best_cost = 1e300;
-    const int cap = std::max(1, std::min(n_tiles, 8192));
-    for (int s = 1; s <= cap; ++s) {
-        const int per = (n_tiles + s - 1) / s;
-        const int s_eff = (n_tiles + per - 1) / per;
-        if (s_eff != s) continue;
-        const double blocks = (double)blocks_x * s;
-        const double waves = std::ceil(blocks / resident);
-        const double cost = waves * per + 0.02 * s;   // small bias against extra partials
-        if (cost < best_cost) {
-            best_cost = cost;
-            best = s;
-        }
-    }
-    return best;
-}
+struct MkLaunchShape {
+    mk_split_fn fn;
+    int resident;      // blocks that fit the GPU at once
+};
 
-extern "C" size_t mk_sum_workspace_size(int n_pix, int slices)
+static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShape *out)
 {
-    if (n_pix <= 0 || slices <= 0) return 256;
-    return sizeof(double2) * (size_t)n_pix * (size_t)slices;
-}
-
-static int mk_split_config(const mk_tiles *tiles, const mk_pixels *px, const mk_launch *launch,
-                           int cplx, int fresnel, mk_split_fn *fn_out, int *slices_out,
-                           int *per_out)
-{
-    const int n_pix = px->ny * px->nz;
-    mk_split_fn fn = mk_pick(launch->threads, launch->pix_per_thread, fresnel != 0, cplx != 0);
-    MK_REQUIRE(fn, "mk_kin_split_f32: unsupported launch shape threads=%d pix=%d", launch->threads,
+    mk_split_fn fn = mk_pick(launch->threads, launch->pix_per_thread, launch->fresnel != 0,
+                             launch->amp_real == 0);
+    MK_REQUIRE(fn, "split kernel: unsupported launch shape threads=%d pix=%d", launch->threads,
                launch->pix_per_thread);
-    const size_t smem = mk_split_smem(tiles->tile_atoms);
+    const size_t smem = mk_split_smem(tile_atoms);
     MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
-    const int blocks_x = (n_pix + launch->threads * launch->pix_per_thread - 1) /
-                         (launch->threads * launch->pix_per_thread);
-    int slices = launch->slices;
-    if (slices <= 0) {
-        int dev = 0, sms = 152, bps = 1;
-        MK_CHECK_CUDA(cudaGetDevice(&dev));
-        MK_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        MK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void *)fn,
-                                                                    launch->threads, smem));
-        MK_REQUIRE(bps >= 1, "mk_kin_split_f32: launch shape does not fit on an SM");
-        slices = mk_auto_slices(blocks_x, tiles->n_tiles, sms * bps);
-    }
-    slices = std::max(1, std::min(slices, tiles->n_tiles));
-    const int per = (tiles->n_tiles + slices - 1) / slices;
-    *slices_out = (tiles->n_tiles + per - 1) / per;
-    *per_out = per;
-    *fn_out = fn;
+    int dev = 0, sms = 0, bps = 0;
+    MK_CHECK_CUDA(cudaGetDevice(&dev));
+    MK_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void *)fn,
+                                                                launch->threads, smem));
+    MK_REQUIRE(bps >= 1, "split kernel: launch shape does not fit on an SM");
+    out->fn = fn;
+    out->resident = sms * bps;
     return MK_OK;
 }
 
-extern "C" int mk_split_plan(const mk_tiles *tiles, const mk_pixels *px, const mk_launch *launch,
-                             int *slices_out)
+// Slice count for one frame so that the items fill the resident grid many
+// times over (load balance) while keeping items long enough that the
+// per-item TMA pipeline start is negligible.
+static int mk_frame_slices(int pix_blocks, int n_tiles, int resident, long long total_blocks)
 {
-    MK_REQUIRE(tiles && px && launch && slices_out, "mk_split_plan: null argument");
+    const long long target = 24LL * resident;
+    long long s = (target + total_blocks - 1) / std::max<long long>(total_blocks, 1);
+    s = std::max<long long>(1, std::min<long long>(s, std::max(1, n_tiles / 4)));
+    return (int)std::min<long long>(s, n_tiles);
+}
+
+extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const double *beam_dirs,
+                            const double *pol_es, const mk_tiles *tiles, const mk_launch *launch,
+                            mk_frame_desc *frames_out, long long *n_items_out,
+                            long long *n_partial_out)
+{
+    MK_REQUIRE(n_frames >= 1 && frame_pixels && beam_dirs && tiles && launch && frames_out &&
+                   n_items_out && n_partial_out,
+               "mk_scan_plan: null argument or no frames");
+    MK_REQUIRE(tiles->n_tiles >= 1, "mk_scan_plan: no tiles");
+    MkLaunchShape sh;
+    int rc = mk_launch_shape(tiles->tile_atoms, launch, &sh);
+    if (rc != MK_OK) return rc;
+    const int ppb = launch->threads * launch->pix_per_thread;
+    long long total_blocks = 0;
+    for (int f = 0; f < n_frames; ++f) {
+        MK_REQUIRE(frame_pixels[f] >= 1, "mk_scan_plan: frame %d has no pixels", f);
+        total_blocks += (frame_pixels[f] + ppb - 1) / ppb;
+    }
+    long long pix_off = 0, part_off = 0, item_off = 0;
+    for (int f = 0; f < n_frames; ++f) {
+        mk_frame_desc &F = frames_out[f];
+        memset(&F, 0, sizeof(F));
+        F.n_pix = frame_pixels[f];
+        F.pix_blocks = (F.n_pix + ppb - 1) / ppb;
+        int s = launch->slices > 0 ? std::min(launch->slices, tiles->n_tiles)
+                                   : mk_frame_slices(F.pix_blocks, tiles->n_tiles, sh.resident, total_blocks);
+        F.tiles_per_slice = (tiles->n_tiles + s - 1) / s;
+        F.slices = (tiles->n_tiles + F.tiles_per_slice - 1) / F.tiles_per_slice;
+        F.pix_off = pix_off;
+        F.part_off = part_off;
+        F.item_off = item_off;
+        for (int c = 0; c < 3; ++c) {
+            F.b[c] = (float)beam_dirs[3 * f + c];
+            F.e[c] = pol_es ? (float)pol_es[3 * f + c] : 0.f;
+        }
+        pix_off += F.n_pix;
+        part_off += (long long)F.slices * F.n_pix;
+        item_off += (long long)F.slices * F.pix_blocks;
+    }
+    *n_items_out = item_off;
+    *n_partial_out = part_off;
+    return MK_OK;
+}
+
+extern "C" size_t mk_scan_workspace_size(long long n_partial)
+{
+    return 256 + sizeof(double2) * (size_t)std::max<long long>(n_partial, 1);
+}
+
+static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_physics *phys,
+                        const mk_pixels *px, long long n_total, int n_frames,
+                        const mk_frame_desc &f0, const mk_frame_desc *frames_dev,
+                        long long n_items, long long n_partial, const mk_launch *launch,
+                        double *out, double *sums, int accumulate, void *workspace,
+                        size_t ws_bytes, cudaStream_t st)
+{
+    MK_REQUIRE(px->q && px->u && px->phasor, "split kernel: pixels not prepared");
+    MK_REQUIRE(tiles->origin && tiles->species && tiles->pos && tiles->amp,
+               "split kernel: null tile buffer");
+    MK_REQUIRE(((uintptr_t)tiles->pos & 15) == 0 && ((uintptr_t)tiles->amp & 15) == 0,
+               "split kernel: tile arrays must be 16-byte aligned");
+    const int T = tiles->tile_atoms;
+    MK_REQUIRE(T >= 128 && T <= 4096 && (T & (T - 1)) == 0, "split kernel: bad tile_atoms %d", T);
+    const size_t need = mk_scan_workspace_size(n_partial);
+    if (!workspace || ws_bytes < need) {
+        mk_set_error("split kernel: workspace %zu bytes, need %zu", ws_bytes, need);
+        return MK_ENOMEM;
+    }
+    MkSplitArgs A;
+    memset(&A, 0, sizeof(A));
+    int rc = mk_species_pack(spc, &A.sp);
+    if (rc != MK_OK) return rc;
+    MkLaunchShape sh;
+    rc = mk_launch_shape(T, launch, &sh);
+    if (rc != MK_OK) return rc;
+    mk_register_status_reader(mk_split_read_status);
+    int *status = nullptr;
+    MK_CHECK_CUDA(cudaGetSymbolAddress((void **)&status, g_split_status));
+    char *w = static_cast<char *>(workspace);
+    A.counter = reinterpret_cast<unsigned long long *>(w);
+    A.partial = reinterpret_cast<double2 *>(w + 256);
+    A.n_tiles = tiles->n_tiles;
+    A.tile_atoms = T;
+    A.n_frames = n_frames;
+    A.n_items = n_items;
+    A.f0 = f0;
+    A.frames = frames_dev;
+    A.q = reinterpret_cast<const double4 *>(px->q);
+    A.u = reinterpret_cast<const float4 *>(px->u);
+    A.origin = reinterpret_cast<const double4 *>(tiles->origin);
+    A.tspecies = tiles->species;
+    A.tpos = reinterpret_cast<const float4 *>(tiles->pos);
+    A.tamp = reinterpret_cast<const float2 *>(tiles->amp);
+    A.status = status;
+    A.kappa = (float)(phys->k / MK_TWO_PI);
+    A.k = (float)phys->k;
+    const double sf = phys->k * 0.25e-10 / MK_PI;
+    A.s2fac = (float)(sf * sf);
+    A.apply_pol = phys->apply_pol;
+    A.decay = phys->spherical_decay;
+    A.remove_forward = phys->remove_forward;
+    A.pdeg = (float)phys->pol_deg;
+    MK_CHECK_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned long long), st));
+    const long long grid = std::min<long long>(n_items, sh.resident);
+    sh.fn<<<(unsigned)grid, launch->threads, mk_split_smem(T), st>>>(A);
+    MK_CHECK_CUDA(cudaGetLastError());
+    const unsigned rb = (unsigned)((n_total + 255) / 256);
+    mk_reduce_kernel<<<rb, 256, 0, st>>>(A.partial, n_total, n_frames, f0, frames_dev,
+                                         reinterpret_cast<const double2 *>(px->phasor), MK_R_E,
+                                         reinterpret_cast<double2 *>(out), accumulate);
+    MK_CHECK_CUDA(cudaGetLastError());
+    if (sums) {
+        mk_frame_intensity_kernel<<<n_frames, 256, 0, st>>>(reinterpret_cast<const double2 *>(out),
+                                                            n_frames, frames_dev, f0, sums);
+        MK_CHECK_CUDA(cudaGetLastError());
+    }
+    return MK_OK;
+}
+
+static int mk_single_plan(const mk_tiles *tiles, const mk_physics *phys, const mk_pixels *px,
+                          const mk_launch *launch, mk_frame_desc *F, long long *n_items,
+                          long long *n_partial)
+{
+    const int n_pix = px->ny * px->nz;
+    return mk_scan_plan(1, &n_pix, phys->beam_dir, phys->pol_e, tiles, launch, F, n_items, n_partial);
+}
+
+extern "C" int mk_split_plan(const mk_tiles *tiles, const mk_pixels *px, const mk_launch *launch,
+                             size_t *ws_bytes_out)
+{
+    MK_REQUIRE(tiles && px && launch && ws_bytes_out, "mk_split_plan: null argument");
     MK_REQUIRE(px->ny > 0 && px->nz > 0, "mk_split_plan: bad detector shape");
     if (tiles->n_tiles <= 0) {
-        *slices_out = 0;
+        *ws_bytes_out = mk_scan_workspace_size(0);
         return MK_OK;
     }
-    mk_split_fn fn;
-    int per;
-    const int fresnel = launch->fresnel < 0 ? 1 : launch->fresnel;
-    return mk_split_config(tiles, px, launch, launch->amp_real ? 0 : 1, fresnel, &fn, slices_out, &per);
+    mk_physics ph;
+    memset(&ph, 0, sizeof(ph));
+    ph.beam_dir[0] = 1.0;
+    mk_frame_desc F;
+    long long ni, np;
+    int rc = mk_single_plan(tiles, &ph, px, launch, &F, &ni, &np);
+    if (rc != MK_OK) return rc;
+    *ws_bytes_out = mk_scan_workspace_size(np);
+    return MK_OK;
 }
 
 extern "C" int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *spc,
@@ -416,70 +603,41 @@ extern "C" int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *spc,
     MK_REQUIRE(tiles && spc && phys && px && launch && out, "mk_kin_split_f32: null argument");
     const int64_t np64 = (int64_t)px->ny * px->nz;
     MK_REQUIRE(px->ny > 0 && px->nz > 0 && np64 < (1ll << 31), "mk_kin_split_f32: bad detector shape");
-    MK_REQUIRE(px->qc && px->qcut && px->uf && px->phasor, "mk_kin_split_f32: pixels not prepared");
     MK_REQUIRE(phys->k > 0.0, "mk_kin_split_f32: k must be positive");
-    const int T = tiles->tile_atoms;
-    MK_REQUIRE(T >= 128 && T <= 4096 && (T & (T - 1)) == 0, "mk_kin_split_f32: bad tile_atoms %d", T);
-    const int n_pix = (int)np64;
     cudaStream_t st = mk_stream(stream);
     if (tiles->n_tiles <= 0) {
-        if (!accumulate) MK_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)n_pix, st));
+        if (!accumulate) MK_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)np64, st));
         return MK_OK;
     }
-    MK_REQUIRE(tiles->origin && tiles->species && tiles->pos && tiles->amp,
-               "mk_kin_split_f32: null tile buffer");
-    MK_REQUIRE(((uintptr_t)tiles->pos & 15) == 0 && ((uintptr_t)tiles->amp & 15) == 0,
-               "mk_kin_split_f32: tile arrays must be 16-byte aligned");
-    MkSplitArgs A;
-    int rc = mk_species_pack(spc, &A.sp);
+    mk_frame_desc F;
+    long long n_items, n_partial;
+    int rc = mk_single_plan(tiles, phys, px, launch, &F, &n_items, &n_partial);
     if (rc != MK_OK) return rc;
-    mk_register_status_reader(mk_split_read_status);
-    const int fresnel = launch->fresnel < 0 ? 1 : launch->fresnel;
-    const int cplx = launch->amp_real ? 0 : 1;
-    mk_split_fn fn;
-    int slices, per;
-    rc = mk_split_config(tiles, px, launch, cplx, fresnel, &fn, &slices, &per);
-    if (rc != MK_OK) return rc;
-    const size_t need = mk_sum_workspace_size(n_pix, slices);
-    if (!workspace || ws_bytes < need) {
-        mk_set_error("mk_kin_split_f32: workspace %zu bytes, need %zu (slices=%d)", ws_bytes, need,
-                     slices);
-        return MK_ENOMEM;
+    return mk_run_split(tiles, spc, phys, px, np64, 1, F, nullptr, n_items, n_partial, launch, out,
+                        nullptr, accumulate, workspace, ws_bytes, st);
+}
+
+extern "C" int mk_kin_scan_f32(const mk_tiles *tiles, const mk_species *spc,
+                               const mk_physics *phys, const mk_pixels *px, int n_frames,
+                               const mk_frame_desc *frames_dev, long long n_items,
+                               long long n_partial, const mk_launch *launch, double *out,
+                               double *intensity_sums, void *workspace, size_t ws_bytes,
+                               void *stream)
+{
+    MK_REQUIRE(tiles && spc && phys && px && launch && out && frames_dev,
+               "mk_kin_scan_f32: null argument");
+    MK_REQUIRE(n_frames >= 1 && n_items >= 1 && n_partial >= 1, "mk_kin_scan_f32: empty plan");
+    MK_REQUIRE(tiles->n_tiles >= 1, "mk_kin_scan_f32: no tiles");
+    MK_REQUIRE(phys->k > 0.0, "mk_kin_scan_f32: k must be positive");
+    const long long n_total = (long long)px->ny * px->nz;
+    mk_frame_desc dummy;
+    memset(&dummy, 0, sizeof(dummy));
+    if (n_frames == 1) {
+        // a one-frame plan still lives on the device; the kernel then needs
+        // it by value: read it back once (not capturable, so scans pass >1)
+        MK_CHECK_CUDA(cudaMemcpy(&dummy, frames_dev, sizeof(dummy), cudaMemcpyDeviceToHost));
     }
-    int *status = nullptr;
-    MK_CHECK_CUDA(cudaGetSymbolAddress((void **)&status, g_split_status));
-    A.n_pix = n_pix;
-    A.n_tiles = tiles->n_tiles;
-    A.tiles_per_slice = per;
-    A.tile_atoms = T;
-    A.qc = px->qc;
-    A.qcut = px->qcut;
-    A.uf = px->uf;
-    A.origin = reinterpret_cast<const double4 *>(tiles->origin);
-    A.tspecies = tiles->species;
-    A.tpos = reinterpret_cast<const float4 *>(tiles->pos);
-    A.tamp = reinterpret_cast<const float2 *>(tiles->amp);
-    A.partial = static_cast<double2 *>(workspace);
-    A.status = status;
-    A.bx = (float)phys->beam_dir[0];
-    A.by = (float)phys->beam_dir[1];
-    A.bz = (float)phys->beam_dir[2];
-    A.kappa = (float)(phys->k / MK_TWO_PI);
-    A.k = (float)phys->k;
-    const double sf = phys->k * 0.25e-10 / MK_PI;
-    A.s2fac = (float)(sf * sf);
-    A.apply_pol = phys->apply_pol;
-    A.decay = phys->spherical_decay;
-    A.remove_forward = phys->remove_forward;
-    A.pdeg = (float)phys->pol_deg;
-    A.ex = (float)phys->pol_e[0];
-    A.ey = (float)phys->pol_e[1];
-    A.ez = (float)phys->pol_e[2];
-    const int blocks_x = (n_pix + launch->threads * launch->pix_per_thread - 1) /
-                         (launch->threads * launch->pix_per_thread);
-    dim3 grid(blocks_x, slices);
-    fn<<<grid, launch->threads, mk_split_smem(T), st>>>(A);
-    MK_CHECK_CUDA(cudaGetLastError());
-    return mk_launch_reduce(A.partial, slices, n_pix, reinterpret_cast<const double2 *>(px->phasor),
-                            MK_R_E, reinterpret_cast<double2 *>(out), accumulate, st);
+    return mk_run_split(tiles, spc, phys, px, n_total, n_frames, dummy,
+                        n_frames > 1 ? frames_dev : nullptr, n_items, n_partial, launch, out,
+                        intensity_sums, 0, workspace, ws_bytes, mk_stream(stream));
 }

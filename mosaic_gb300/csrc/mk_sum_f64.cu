@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(F64_NT) mk_plain_f64_kernel(
     int64_t n, int64_t atoms_per_slice, const double *__restrict__ pos,
     const int *__restrict__ species, const float2 *__restrict__ amp, int n_pix,
     const double *__restrict__ xyz, const double *__restrict__ r0v,
-    const double *__restrict__ qcutv, const __grid_constant__ MkPlainArgs A,
+    const double4 *__restrict__ qv, const __grid_constant__ MkPlainArgs A,
     double2 *__restrict__ partial)
 {
     __shared__ double s_pos[F64_ATOMS][3];
@@ -50,9 +50,9 @@ __global__ void __launch_bounds__(F64_NT) mk_plain_f64_kernel(
     const bool live = p < n_pix;
     for (int i = threadIdx.x; i < MK_MAX_SPECIES * 11; i += F64_NT)
         s_wk[i / 11][i % 11] = A.sp.wk[i / 11][i % 11];
-    const double cx = live ? xyz[p] : 0.0, cy = live ? xyz[n_pix + p] : 0.0,
-                 cz = live ? xyz[2 * n_pix + p] : 0.0;
-    const double R0 = live ? r0v[p] : 0.0, qcut = live ? qcutv[p] : 0.0;
+    const double cx = live ? xyz[3 * p] : 0.0, cy = live ? xyz[3 * p + 1] : 0.0,
+                 cz = live ? xyz[3 * p + 2] : 0.0;
+    const double R0 = live ? r0v[p] : 0.0, qcut = live ? qv[p].w : 0.0;
     const double s_fac = 0.25e-10 / MK_PI;
     double acc_r = 0.0, acc_i = 0.0;
     const int64_t a_lo = (int64_t)blockIdx.y * atoms_per_slice;
@@ -117,6 +117,12 @@ __global__ void __launch_bounds__(F64_NT) mk_plain_f64_kernel(
     if (live) partial[(size_t)blockIdx.y * n_pix + p] = make_double2(acc_r, acc_i);
 }
 
+extern "C" size_t mk_sum_workspace_size(int n_pix, int slices)
+{
+    if (n_pix <= 0 || slices <= 0) return 256;
+    return sizeof(double2) * (size_t)n_pix * (size_t)slices;
+}
+
 static int mk_plain_slices(int64_t n, int n_pix, int want)
 {
     if (want > 0) return (int)std::min<int64_t>(want, std::max<int64_t>(1, (n + F64_ATOMS - 1) / F64_ATOMS));
@@ -139,7 +145,7 @@ extern "C" int mk_kin_plain_f64(int64_t n, const double *pos, const int *species
     const int64_t np64 = (int64_t)px->ny * px->nz;
     MK_REQUIRE(px->ny > 0 && px->nz > 0 && np64 < (1ll << 31), "mk_kin_plain_f64: bad detector shape");
     MK_REQUIRE(n == 0 || (pos && species && amp), "mk_kin_plain_f64: null atom buffer");
-    MK_REQUIRE(px->xyz && px->r0 && px->qcut, "mk_kin_plain_f64: pixels not prepared");
+    MK_REQUIRE(px->xyz && px->r0 && px->q, "mk_kin_plain_f64: pixels not prepared");
     MK_REQUIRE(phys->k > 0.0, "mk_kin_plain_f64: k must be positive");
     const int n_pix = (int)np64;
     MkPlainArgs A;
@@ -171,7 +177,8 @@ extern "C" int mk_kin_plain_f64(int64_t n, const double *pos, const int *species
     double2 *part = static_cast<double2 *>(workspace);
     mk_plain_f64_kernel<<<grid, F64_NT, 0, st>>>(n, per, pos, species,
                                                  reinterpret_cast<const float2 *>(amp), n_pix,
-                                                 px->xyz, px->r0, px->qcut, A, part);
+                                                 px->xyz, px->r0,
+                                                 reinterpret_cast<const double4 *>(px->q), A, part);
     MK_CHECK_CUDA(cudaGetLastError());
     return mk_launch_reduce(part, ns_eff, n_pix, nullptr, 1.0, reinterpret_cast<double2 *>(out),
                             accumulate, st);

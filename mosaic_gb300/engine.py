@@ -90,27 +90,44 @@ def physics(k, beam_dir=(1.0, 0.0, 0.0), apply_pol=False, pol=(0.0, 0.0, 1.0, 0.
 
 
 class Pixels:
-    """Detector pixels on the device plus their per-pixel prologue."""
+    """Detector pixels on the device plus their per-pixel prologue.
 
-    def __init__(self, xyz_m, ny, nz, phys, device="cuda", stream=None):
+    ``xyz_m`` is (3, P) in metres (the detector's layout), host or device.
+    With ``frames`` (a list of (ny, nz, beam_dir) per frame whose pixels are
+    consecutive in xyz_m) every frame's prologue uses its own direction."""
+
+    def __init__(self, xyz_m, ny, nz, phys, device="cuda", stream=None, frames=None):
         L = _require_cuda()
         P = int(ny) * int(nz)
         if isinstance(xyz_m, torch.Tensor):
-            self.xyz = xyz_m.to(device=device, dtype=torch.float64).reshape(3, P).contiguous()
+            x = xyz_m.to(device=device, dtype=torch.float64).reshape(3, P)
         else:
-            xyz = torch.as_tensor(np.ascontiguousarray(xyz_m, dtype=np.float64).reshape(3, P))
-            self.xyz = xyz.to(device, non_blocking=False)
+            x = torch.as_tensor(np.ascontiguousarray(xyz_m, dtype=np.float64).reshape(3, P)).to(device)
+        self.xyz = x.t().contiguous()                    # (P, 3)
         dd = dict(dtype=torch.float64, device=device)
         self.r0 = torch.empty(P, **dd)
-        self.qcut = torch.empty(P, **dd)
-        self.qc = torch.empty((3, P), **dd)
-        self.uf = torch.empty((4, P), dtype=torch.float32, device=device)
+        self.q = torch.empty((P, 4), **dd)
+        self.u = torch.empty((P, 4), dtype=torch.float32, device=device)
         self.phasor = torch.empty((P, 2), **dd)
         self.ny, self.nz, self.n = int(ny), int(nz), P
         self.abi = MkPixels(self.ny, self.nz, self.xyz.data_ptr(), self.r0.data_ptr(),
-                            self.qcut.data_ptr(), self.qc.data_ptr(), self.uf.data_ptr(),
-                            self.phasor.data_ptr())
-        check(L.mk_pixels_prepare(ctypes.byref(self.abi), ctypes.byref(phys), _stream_handle(stream)))
+                            self.q.data_ptr(), self.u.data_ptr(), self.phasor.data_ptr())
+        sh = _stream_handle(stream)
+        if frames is None:
+            check(L.mk_pixels_prepare(ctypes.byref(self.abi), ctypes.byref(phys), sh))
+            return
+        off = 0
+        for fny, fnz, bdir in frames:
+            m = int(fny) * int(fnz)
+            sub = MkPixels(int(fny), int(fnz), self.xyz[off:].data_ptr(), self.r0[off:].data_ptr(),
+                           self.q[off:].data_ptr(), self.u[off:].data_ptr(),
+                           self.phasor[off:].data_ptr())
+            ph = MkPhysics.from_buffer_copy(phys)
+            ph.beam_dir[:] = [float(v) for v in bdir]
+            check(L.mk_pixels_prepare(ctypes.byref(sub), ctypes.byref(ph), sh))
+            off += m
+        if off != P:
+            raise ValueError(f"frames cover {off} pixels, xyz has {P}")
 
     def r0_min(self):
         return float(self.r0.min())
@@ -214,10 +231,10 @@ def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None,
     cfg = dict(DEFAULT_LAUNCH, **(launch or {}))
     ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
                   int(tiles.amp_is_real() if amp_real is None else bool(amp_real)))
-    ns = ctypes.c_int(0)
+    wsb = ctypes.c_size_t(0)
     check(L.mk_split_plan(ctypes.byref(tiles.abi), ctypes.byref(pix.abi), ctypes.byref(ln),
-                          ctypes.byref(ns)))
-    ws_n = L.mk_sum_workspace_size(pix.n, max(ns.value, 1))
+                          ctypes.byref(wsb)))
+    ws_n = int(wsb.value)
     ws = torch.empty(ws_n, dtype=torch.uint8, device=pix.xyz.device)
     if out is None:
         out = torch.zeros((pix.n, 2), dtype=torch.float64, device=pix.xyz.device)

@@ -1,0 +1,216 @@
+"""Batched scans: every step of a motor scan in one persistent launch.
+
+The reference runs a scan as one full exposure per step
+(experiment.scan_nD, Experiment.py:285-336): reload and re-stage every chunk,
+transform the atoms to the lab, sort, plan and launch, per frame. Here the
+atoms are staged once, in the SAMPLE frame, and each frame f only changes
+what is cheap to change -- its pixels, incident direction and polarization
+vector, all moved into the sample frame by the inverse stage transform:
+
+    P'_f = R_f^T (P_f - t_f),   b_f = R_f^T x,   e_f = R_f^T e.
+
+k (b_f . a + |P'_f - a|) is then exactly the phase of atom a at pixel P_f
+with the sample at (R_f, t_f). All frames (each with its own ROI, of any
+size) become work items of one persistent kernel (``mk_kin_scan_f32``);
+the launch sequence can be captured in a CUDA graph and replayed.
+
+The incident amplitude must not depend on the frame: the beam profile must
+be uniform and cover the sample in every frame (checked; otherwise run the
+frames one by one through ``beam.atomic_scattering_kinematic``).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib, engine
+from ._lib import MkFrameDesc, MkLaunch, check
+
+
+@dataclass
+class Frame:
+    """One scan step: sample rotation/translation (sample -> lab, A), lab
+    pixel coordinates (3, P) in A of its ROI, and the ROI shape (ny, nz)."""
+    rotation: np.ndarray
+    translation: np.ndarray
+    pixels: np.ndarray
+    shape: tuple
+
+
+def roi_indices(det_shape, side, centre=None):
+    """Pixel indices (iz*Ny + iy) of a square ROI of ``side`` pixels centred
+    on the detector (or on ``centre`` = (iy, iz)), clipped to the detector."""
+    ny, nz = int(det_shape[0]), int(det_shape[1])
+    sy, sz = min(int(side), ny), min(int(side), nz)
+    cy, cz = (ny // 2, nz // 2) if centre is None else centre
+    y0 = int(np.clip(cy - sy // 2, 0, ny - sy))
+    z0 = int(np.clip(cz - sz // 2, 0, nz - sz))
+    iz, iy = np.mgrid[z0:z0 + sz, y0:y0 + sy]
+    return (iz * ny + iy).ravel(), (sy, sz)
+
+
+class BatchedScan:
+    """All frames of a scan as one launch over atoms staged once.
+
+    Args:
+        beam: a configured ``mosaic_gb300.beam``.
+        sample: chunk-API sample (thermal displacement applied on load).
+        frames: list of Frame.
+        apply_polarization, spherical_decay, remove_forward: as in
+            ``atomic_scattering_kinematic``.
+        launch: split-kernel launch shape (None: autotuned or default).
+    """
+
+    def __init__(self, beam, sample, frames, apply_polarization=False, spherical_decay=False,
+                 remove_forward=False, launch=None, device="cuda"):
+        self.L = engine._require_cuda()
+        self.beam = beam
+        self.frames = list(frames)
+        if not self.frames:
+            raise ValueError("a scan needs at least one frame")
+        beam._require_forward_beam()
+        dev = torch.device(device)
+        pos, idx, labels = beam.collect_atoms(sample)
+        self._check_uniform_beam(pos)
+        table = engine.SpeciesTable.build(labels or ["H"], beam.tables, beam._energy,
+                                          beam._debye_waller)
+        # atoms in the sample frame, incident amplitude 1
+        self.atoms = engine.atoms_lab(pos, idx, np.eye(3), np.zeros(3), table, device=dev)
+        self.table = table
+        self.tiles = engine.Tiles(self.atoms, beam.k, beam._kernel_tile_atoms, device=dev)
+        pol = beam._polarization_state()
+        e_lab = np.array(pol[1:4], dtype=np.float64)
+        b_lab = np.array([1.0, 0.0, 0.0])
+        xyz, fr, bdirs, pols = [], [], [], []
+        for f in self.frames:
+            R = np.asarray(f.rotation, dtype=np.float64)
+            t = np.asarray(f.translation, dtype=np.float64)
+            P = np.asarray(f.pixels, dtype=np.float64)
+            xyz.append((R.T @ (P - t[:, None])) / 1e10)
+            b = R.T @ b_lab
+            fr.append((int(f.shape[0]), int(f.shape[1]), b))
+            bdirs.append(b)
+            pols.append(R.T @ e_lab)
+        self.frame_pixels = np.array([int(s[0]) * int(s[1]) for s in fr], dtype=np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.frame_pixels)]).astype(np.int64)
+        n_total = int(self.offsets[-1])
+        self.phys = beam.physics(apply_polarization, spherical_decay, remove_forward, pol=pol)
+        self.pix = engine.Pixels(np.concatenate(xyz, axis=1), n_total, 1, self.phys, device=dev,
+                                 frames=fr)
+        third, fresnel, tol, diag = beam.split_budget(self.tiles, self.pix.r0_min())
+        if third > tol:
+            raise _lib.DeclineError(_lib.MK_EDECLINE,
+                                    f"scan geometry outside the split-phase error budget "
+                                    f"({third:.2e} rad > {tol:.0e})")
+        self.diag = diag
+        cfg = dict(engine.DEFAULT_LAUNCH, **(launch or beam._kernel_launch or {}))
+        self.launch = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]),
+                               int(fresnel), int(self.tiles.amp_is_real()))
+        nf = len(self.frames)
+        desc = (MkFrameDesc * nf)()
+        n_items, n_part = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        bd = np.ascontiguousarray(np.array(bdirs, dtype=np.float64))
+        pe = np.ascontiguousarray(np.array(pols, dtype=np.float64))
+        check(self.L.mk_scan_plan(nf, self.frame_pixels.ctypes.data, bd.ctypes.data, pe.ctypes.data,
+                                  ctypes.byref(self.tiles.abi), ctypes.byref(self.launch),
+                                  ctypes.cast(desc, ctypes.c_void_p), ctypes.byref(n_items),
+                                  ctypes.byref(n_part)))
+        self.n_items, self.n_partial = int(n_items.value), int(n_part.value)
+        raw = np.frombuffer(bytes(desc), dtype=np.uint8).copy()
+        self.frames_dev = torch.as_tensor(raw).to(dev)
+        self.ws_bytes = int(self.L.mk_scan_workspace_size(self.n_partial))
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        self.out = torch.zeros((n_total, 2), dtype=torch.float64, device=dev)
+        self.sums = torch.zeros(nf, dtype=torch.float64, device=dev)
+        self._graph = None
+        self.terms = float(self.atoms.n) * n_total
+
+    def _check_uniform_beam(self, pos):
+        B = self.beam
+        if not str(B._beam_profile).startswith("uniform") and B._beam_profile != "uniform":
+            raise NotImplementedError("batched scans need a uniform beam profile; run the frames "
+                                      "one by one through atomic_scattering_kinematic")
+        if not np.all(np.abs(B._beam_E0_map) == 1.0):
+            raise NotImplementedError("batched scans need a uniform beam map")
+        if pos.shape[0]:
+            rmax = float(np.sqrt((pos.astype(np.float64) ** 2).sum(1)).max())
+            for f in self.frames:
+                c = np.asarray(f.translation, dtype=np.float64)
+                half_u = 0.5 * B._beam_size[0] - abs(c[1])
+                half_v = 0.5 * B._beam_size[1] - abs(c[2])
+                if rmax >= min(half_u, half_v) - max(B._beam_du, B._beam_dv):
+                    raise NotImplementedError(
+                        "the beam does not cover the sample in every frame; batched scans need "
+                        "a frame-independent incident amplitude")
+
+    def run(self, stream=None):
+        """Launch the whole scan (asynchronous); returns (fields, sums) on device."""
+        sp = self.table.abi()
+        check(self.L.mk_kin_scan_f32(ctypes.byref(self.tiles.abi), ctypes.byref(sp),
+                                     ctypes.byref(self.phys), ctypes.byref(self.pix.abi),
+                                     len(self.frames), self.frames_dev.data_ptr(), self.n_items,
+                                     self.n_partial, ctypes.byref(self.launch), self.out.data_ptr(),
+                                     self.sums.data_ptr(), self.ws.data_ptr(), self.ws_bytes,
+                                     engine._stream_handle(stream)))
+        return self.out, self.sums
+
+    def capture(self):
+        """Capture run() in a CUDA graph (frames > 1); replay() then re-runs it."""
+        if len(self.frames) < 2:
+            raise ValueError("graph capture needs at least two frames")
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.run(s)                 # warm-up outside the capture
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run(torch.cuda.current_stream())
+        self._graph = g
+        return g
+
+    def replay(self):
+        if self._graph is None:
+            self.capture()
+        self._graph.replay()
+        return self.out, self.sums
+
+    def frame_field(self, f):
+        """Complex128 (nz, ny) field of frame f (host)."""
+        ny, nz = self.frames[f].shape
+        a, b = int(self.offsets[f]), int(self.offsets[f + 1])
+        return torch.view_as_complex(self.out[a:b]).cpu().numpy().reshape(int(nz), int(ny))
+
+    def sum_intensity(self):
+        return self.sums.cpu().numpy()
+
+
+def frames_from_motors(stage, detector, steps, rois=None):
+    """Frames for a list of motor settings.
+
+    steps: list of dicts {motor name: value (radians for rotations, A for
+    translations)} applied to ``stage`` (restored afterwards); ``rois``:
+    per-step ROI side (int) or None for the full detector."""
+    saved = stage._motor_value.copy()
+    out = []
+    try:
+        for i, st in enumerate(steps):
+            stage._motor_value[:] = saved
+            for name, v in st.items():
+                stage._motor_value[stage.motor_index(name)] = float(v)
+            R, t = stage.get_rotation().copy(), stage.get_translation().copy()
+            coords = np.asarray(detector.pixel_coordinates)
+            if rois is not None and rois[i] is not None:
+                sel, shape = roi_indices(detector.shape, rois[i])
+                coords = coords[:, sel]
+            else:
+                shape = tuple(detector.shape)
+            out.append(Frame(R, t, coords, shape))
+    finally:
+        stage._motor_value[:] = saved
+        stage.get_rotation()
+        stage.get_translation()
+    return out

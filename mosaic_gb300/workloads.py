@@ -275,7 +275,15 @@ def cu_bumps_scan_4m(cells=100, npix=512, n_theta=181, chi_offsets_deg=(-0.3, -0
                          chi_offsets_deg=list(chi_offsets_deg), roi_sides=list(roi_sides), **meta))
 
 
-CONFIGS = {"fcc_cu_32k": fcc_cu_32k, "nacl_screw_8m": nacl_screw_8m,
+def nacl_screw_2m():
+    """Quarter-size precision case (80 x 80 x 40 cells = 2,048,000 atoms, 256^2
+    pixels) for kernel profiles: the same per-term work as nacl_screw_8m."""
+    w = nacl_screw_8m(cells=(80, 80, 40), npix=256, chunk_grid=(2, 2))
+    w.name = "nacl_screw_2m"
+    return w
+
+
+CONFIGS = {"fcc_cu_32k": fcc_cu_32k, "nacl_screw_8m": nacl_screw_8m, "nacl_screw_2m": nacl_screw_2m,
            "cu_polycrystal_18m": cu_polycrystal_18m, "cu_bumps_scan_4m": cu_bumps_scan_4m}
 
 

@@ -79,7 +79,10 @@ def _golden_beam(e):
     B = Beam()
     B.create_beam(float(e["energy"]), beam_size=(70.0, 60.0), beam_samples=(64, 48),
                   beam_profile="gaussian", gaussian_waist=(30.0, 25.0), pol_perp_rate=0.9)
-    assert np.array_equal(B._beam_E0_map, e["E0"])
+    # The Gaussian profile goes through np.exp, whose last bit differs between
+    # libm builds (x86 vs Arm): use the reference's own map.
+    assert np.allclose(B._beam_E0_map, e["E0"], rtol=1e-6, atol=0)
+    B.set_wavefield(e["E0"])
     return B
 
 
@@ -137,9 +140,9 @@ def test_fcc_cu_32k_split_vs_plain(cuda):
     B._use_fast_kernel = False
     a64 = B.atomic_scattering_kinematic(w.sample, w.detector, w.stage, return_double=True, **w.sc_kwargs)
     assert rel_intensity(a32, a64) <= 1e-4, rel_intensity(a32, a64)
-    I = np.abs(a64) ** 2
-    # the Bragg peak is on the detector and far above the background
-    assert I.max() > 1e3 * np.median(I)
+    # The detector (7 mrad) sits inside the (111) peak of the 72 A crystal
+    # (~17 mrad wide): every pixel sees the coherent sum, |A| ~ r_e N f(111).
+    assert np.abs(a64).min() / 2.81794092e-15 > 0.5 * w.n_atoms * 15.0
     sel = np.s_[56:72, 56:72]
     ny, nz = w.detector.shape
     iz, iy = np.mgrid[56:72, 56:72]

@@ -92,7 +92,8 @@ def test_beam_grid_and_wavefield(golden):
     B = Beam()
     B.create_beam(12000.0, beam_size=(70.0, 60.0), beam_samples=(64, 48),
                   beam_profile="gaussian", gaussian_waist=(30.0, 25.0), pol_perp_rate=0.9)
-    assert np.array_equal(B._beam_E0_map, e["E0"])
+    # exact on the machine that made the fixture; np.exp's last bit may differ elsewhere
+    assert np.allclose(B._beam_E0_map, e["E0"], rtol=1e-6, atol=0)
     assert np.array_equal(np.array(B._beam_grid()), e["grid"])
     assert np.array_equal(np.array(B._polarization_state()), e["pol"])
     assert B._wavelength == float(e["wavelength"])
