@@ -228,9 +228,11 @@ __device__ __forceinline__ unsigned long long mk_hilbert3(uint32_t x, uint32_t y
     return h;
 }
 
-// Sort key: species in bits 57..63, then the Hilbert index of the atom on an
-// isotropic grid over the bounding box (one cell size for all three axes,
-// so slabs and rods are not quantised anisotropically).
+// Sort key: species in bits 57..63, then the Hilbert index of the atom on a
+// grid that spans the bounding box along each axis separately. A grid with
+// one cell size for all axes would leave most of the curve's cube empty for
+// a slab or a rod, and the curve's excursions through the empty part would
+// put far-apart atoms next to each other in the order.
 __global__ void mk_keys_kernel(int64_t n, const double *__restrict__ pos,
                                const int *__restrict__ species,
                                const unsigned long long *__restrict__ bb,
@@ -238,17 +240,13 @@ __global__ void mk_keys_kernel(int64_t n, const double *__restrict__ pos,
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double lo[3], span = 0.0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        lo[c] = mk_unordered(bb[c]);
-        span = fmax(span, mk_unordered(bb[3 + c]) - lo[c]);
-    }
-    if (!(span > 0.0)) span = 1.0;
     uint32_t q[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        double f = (pos[3 * i + c] - lo[c]) / span;
+        const double lo = mk_unordered(bb[c]);
+        double span = mk_unordered(bb[3 + c]) - lo;
+        if (!(span > 0.0)) span = 1.0;
+        double f = (pos[3 * i + c] - lo) / span;
         f = fmin(fmax(f, 0.0), 1.0);
         q[c] = (uint32_t)(f * (double)((1u << MK_HILBERT_BITS) - 1));
     }

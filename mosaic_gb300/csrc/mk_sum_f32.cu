@@ -77,6 +77,17 @@ struct MkSplitArgs {
 };
 
 #define TWO_PI_F 6.28318530717958647692f
+// 1.5 * 2^23: for |x| < 2^22, (x + C) - C is x rounded to the nearest
+// integer (round-to-nearest-even of the FP32 add), two full-rate FMA-pipe
+// adds instead of rintf, whose FRND shares the quarter-rate pipe with the
+// MUFU sin/cos (measured 16 per clock per SM for each on sm_103).
+#define MK_ROUND_MAGIC 12582912.0f
+
+// x - nearest integer(x), exact in FP32 for |x| < 2^22.
+__device__ __forceinline__ float mk_frac_nearest(float x)
+{
+    return __fsub_rn(x, __fsub_rn(__fadd_rn(x, MK_ROUND_MAGIC), MK_ROUND_MAGIC));
+}
 
 // Scattering factor of species s at direction u' = b - w.
 __device__ __forceinline__ float2 mk_factor(const MkSplitArgs &A, int s, const mk_frame_desc &F,
@@ -219,7 +230,7 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                         const float sp = db - lin;
                         lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
                     }
-                    const float r = lin - rintf(lin);
+                    const float r = mk_frac_nearest(lin);
                     float sn, cs;
                     __sincosf(r * TWO_PI_F, &sn, &cs);
                     if (CPLX) {

@@ -138,6 +138,14 @@ class Detector:
             c = c / np.linalg.norm(c, axis=0, keepdims=True) * self._distance
         self._pixel_coordinates = c
 
+    def position_detector_relative(self, distance, two_theta, eta, degrees=True):
+        """Move by increments; reuses the absolute setter (Detector.py:593-618)."""
+        dtt = np.deg2rad(two_theta) if degrees else float(two_theta)
+        det = np.deg2rad(eta) if degrees else float(eta)
+        self.position_detector_absolute(float(self._distance) + float(distance),
+                                        float(self._two_theta) + dtt, float(self._eta) + det,
+                                        degrees=False)
+
     def input_pixel_values(self, pixel_values):
         self._pixel_values = pixel_values
         self._pixel_intensity = None
@@ -214,7 +222,36 @@ class Stage:
         self.get_translation()
 
     def motor_index(self, name):
+        if name not in self._motor_name:
+            raise ValueError(f"Unknown stage motor '{name}'. Stage motors: {self._motor_name}")
         return self._motor_name.index(name)
+
+    get_motor_index = motor_index
+
+    def set_single_motor_value_relative(self, name, value, degrees=True):
+        """Add ``value`` to one motor (degrees for rotations when ``degrees``)."""
+        i = self.motor_index(name)
+        v = float(value)
+        if self._motor_type[i] == "R" and degrees:
+            v = np.deg2rad(v)
+        self._motor_value[i] += v
+        self.get_rotation()
+        self.get_translation()
+
+    def set_single_motor_value_absolute(self, name, value, degrees=True):
+        self.set_motor_value(name, value, degrees)
+
+    @property
+    def motor_value(self):
+        return self._motor_value
+
+    @property
+    def motor_names(self):
+        return list(self._motor_name)
+
+    @property
+    def motor_types(self):
+        return [str(t) for t in self._motor_type]
 
     def set_motor_value(self, name, value, degrees=True):
         i = self.motor_index(name)
