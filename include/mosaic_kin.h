@@ -189,6 +189,29 @@ int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *sp, const mk_physi
                      const mk_pixels *px, const mk_launch *launch, double *out,
                      int accumulate, void *workspace, size_t ws_bytes, void *stream);
 
+/* Size of the fixed scratch array behind mk_kin_split_f32_noalloc: 32 MiB,
+ * held in every GPU that loads this library until the process exits. */
+#define MK_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* mk_kin_split_f32 for callers that cannot allocate device memory -- for
+ * example a host application whose own pool owns all device memory and
+ * hands this library only the buffers it computes on, or code recording a
+ * CUDA graph, where allocating would fail or break the capture. Same
+ * arguments and result as mk_kin_split_f32, without the workspace: the
+ * scratch (a work counter and the per-slice partial fields) lives in one
+ * fixed file-scope device array of MK_NOALLOC_SCRATCH_BYTES, and the call
+ * allocates nothing (no cudaMalloc, no cudaFree, no allocating library
+ * call). If the partial fields of its usual slice count do not fit, it uses
+ * fewer slices; a detector of more than (MK_NOALLOC_SCRATCH_BYTES - 256)/16
+ * pixels (about 2.1M) is rejected with MK_ENOMEM. The first call on a device
+ * looks up the array's device address, so make it before any stream
+ * capture. Every call shares the array: calls that may overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller. No counterpart in the reference. */
+int mk_kin_split_f32_noalloc(const mk_tiles *tiles, const mk_species *sp,
+                             const mk_physics *phys, const mk_pixels *px,
+                             const mk_launch *launch, double *out, int accumulate, void *stream);
+
 /* --- batched scans ------------------------------------------------------ */
 /* Plan a batched launch of n_frames frames (host only, no GPU work):
  * frame_pixels (n_frames) pixels per frame; beam_dirs / pol_es (n_frames, 3)

@@ -162,6 +162,9 @@ SIGNATURES = {
     "mk_debug_wait_timeout": (ctypes.c_int, [ctypes.c_uint64, _vp]),
     "mk_split_plan": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkPixels),
                                      ctypes.POINTER(MkLaunch), ctypes.POINTER(ctypes.c_size_t)]),
+    "mk_kin_split_f32_noalloc": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkSpecies),
+                                                ctypes.POINTER(MkPhysics), ctypes.POINTER(MkPixels),
+                                                ctypes.POINTER(MkLaunch), _vp, ctypes.c_int, _vp]),
     "mk_scan_plan": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, ctypes.POINTER(MkTiles),
                                     ctypes.POINTER(MkLaunch), _vp, ctypes.POINTER(ctypes.c_longlong),
                                     ctypes.POINTER(ctypes.c_longlong)]),

@@ -31,6 +31,7 @@
 // Atom tiles reach shared memory by 1-D TMA bulk copies (cp.async.bulk),
 // double-buffered on two mbarriers; every wait is bounded (mk_common.cuh).
 #include <algorithm>
+#include <mutex>
 
 #include "mk_common.cuh"
 
@@ -626,6 +627,77 @@ extern "C" int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *spc,
     if (rc != MK_OK) return rc;
     return mk_run_split(tiles, spc, phys, px, np64, 1, F, nullptr, n_items, n_partial, launch, out,
                         nullptr, accumulate, workspace, ws_bytes, st);
+}
+
+// ------------------------------------------------------ allocation-free entry
+// Scratch of mk_kin_split_f32_noalloc: one fixed array in every GPU that
+// loads this library, held until the process exits. Its device address is
+// looked up once per device (host code cannot use the symbol itself: on the
+// host it names a shadow object, not device memory).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MK_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[256];
+
+static int mk_noalloc_scratch(void **out)
+{
+    int dev = 0;
+    MK_CHECK_CUDA(cudaGetDevice(&dev));
+    MK_REQUIRE(dev >= 0 && dev < 256, "mk_kin_split_f32_noalloc: device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            mk_set_error("mk_kin_split_f32_noalloc: cannot resolve the scratch array on device %d: %s",
+                         dev, cudaGetErrorString(e));
+            return MK_ECUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return MK_OK;
+}
+
+extern "C" int mk_kin_split_f32_noalloc(const mk_tiles *tiles, const mk_species *spc,
+                                        const mk_physics *phys, const mk_pixels *px,
+                                        const mk_launch *launch, double *out, int accumulate,
+                                        void *stream)
+{
+    MK_REQUIRE(tiles && spc && phys && px && launch && out,
+               "mk_kin_split_f32_noalloc: null argument");
+    const int64_t np64 = (int64_t)px->ny * px->nz;
+    MK_REQUIRE(px->ny > 0 && px->nz > 0 && np64 < (1ll << 31),
+               "mk_kin_split_f32_noalloc: bad detector shape");
+    MK_REQUIRE(phys->k > 0.0, "mk_kin_split_f32_noalloc: k must be positive");
+    // Even one slice needs 16 bytes per pixel of partial field.
+    const long long max_partial = (long long)((MK_NOALLOC_SCRATCH_BYTES - 256) / sizeof(double2));
+    if (np64 > max_partial) {
+        mk_set_error("mk_kin_split_f32_noalloc: %lld pixels need %lld bytes of scratch, more than "
+                     "the fixed %u bytes; use mk_kin_split_f32 with a workspace",
+                     (long long)np64, 256 + 16 * (long long)np64, (unsigned)MK_NOALLOC_SCRATCH_BYTES);
+        return MK_ENOMEM;
+    }
+    cudaStream_t st = mk_stream(stream);
+    if (tiles->n_tiles <= 0) {
+        if (!accumulate) MK_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)np64, st));
+        return MK_OK;
+    }
+    void *scratch = nullptr;
+    int rc = mk_noalloc_scratch(&scratch);
+    if (rc != MK_OK) return rc;
+    mk_frame_desc F;
+    long long n_items, n_partial;
+    rc = mk_single_plan(tiles, phys, px, launch, &F, &n_items, &n_partial);
+    if (rc != MK_OK) return rc;
+    if (n_partial > max_partial) {   // fewer slices: the partial fields must fit the array
+        mk_launch capped = *launch;
+        capped.slices = (int)std::max<long long>(1, max_partial / np64);
+        rc = mk_single_plan(tiles, phys, px, &capped, &F, &n_items, &n_partial);
+        if (rc != MK_OK) return rc;
+    }
+    return mk_run_split(tiles, spc, phys, px, np64, 1, F, nullptr, n_items, n_partial, launch, out,
+                        nullptr, accumulate, scratch, MK_NOALLOC_SCRATCH_BYTES, st);
 }
 
 extern "C" int mk_kin_scan_f32(const mk_tiles *tiles, const mk_species *spc,

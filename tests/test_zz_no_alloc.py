@@ -1,0 +1,73 @@
+"""The allocation-free entry point mk_kin_split_f32_noalloc.
+
+It serves callers that may not allocate device memory themselves through
+this library -- an application whose memory pool owns the GPU and passes
+in only the buffers to compute on, or code that is recording a CUDA graph.
+The test calls it through the C ABI and compares it with the workspace
+entry point mk_kin_split_f32 on the same inputs and launch shape, on two
+calls in a row (the shared scratch keeps the previous call's contents, so
+the second call checks that nothing stale leaks into the result). It builds
+its own inputs, so it runs the same alone in a fresh process or after the
+rest of the suite; it is collected last so that a failure here cannot stop
+a run before the other tests.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from mosaic_gb300 import _lib, engine, workloads
+from mosaic_gb300._lib import MkLaunch, MkPixels
+
+pytestmark = pytest.mark.gpu
+
+# the tolerance of the FP32 path's parity tests; identical launch shapes make
+# the two entry points agree far below it
+TOL = 1e-4
+
+
+def _inputs(device):
+    w = workloads.fcc_cu_32k(cells=10, npix=48)
+    B = w.beam
+    phys = B.physics(**w.sc_kwargs)
+    atoms = B.stage_atoms(w.sample, w.stage, device=device)
+    tiles = engine.Tiles(atoms, B.k, 256, device=device)
+    coords = np.asarray(w.detector.pixel_coordinates, dtype=np.float64) / 1e10
+    pix = engine.Pixels(coords, *w.detector.shape, phys, device=device)
+    return atoms.table, phys, tiles, pix
+
+
+def test_noalloc_entry_matches_workspace_entry(cuda):
+    L = _lib.load()
+    table, phys, tiles, pix = _inputs(cuda)
+    cfg = dict(pix_per_thread=4, threads=128, slices=3)
+    ref = engine.run_split(tiles, pix, phys, table, launch=cfg, fresnel=1, amp_real=False)
+    engine.sync()
+    ln = MkLaunch(4, 128, 3, 1, 0)
+    sp = table.abi()
+    scale = float(torch.abs(ref).max())
+    for call in range(2):
+        out = torch.full((pix.n, 2), float("nan"), dtype=torch.float64, device=cuda)
+        rc = L.mk_kin_split_f32_noalloc(ctypes.byref(tiles.abi), ctypes.byref(sp),
+                                        ctypes.byref(phys), ctypes.byref(pix.abi),
+                                        ctypes.byref(ln), out.data_ptr(), 0,
+                                        engine._stream_handle())
+        _lib.check(rc)
+        engine.sync()
+        assert torch.isfinite(out).all(), call
+        err = float(torch.abs(out - ref).max()) / scale
+        assert err <= TOL, (call, err)
+
+
+def test_noalloc_entry_rejects_oversized_detector(cuda):
+    L = _lib.load()
+    table, phys, tiles, pix = _inputs(cuda)
+    big = MkPixels(3000, 1000, pix.abi.xyz, pix.abi.r0, pix.abi.q, pix.abi.u, pix.abi.phasor)
+    ln = MkLaunch(4, 128, 0, 1, 0)
+    sp = table.abi()
+    rc = L.mk_kin_split_f32_noalloc(ctypes.byref(tiles.abi), ctypes.byref(sp), ctypes.byref(phys),
+                                    ctypes.byref(big), ctypes.byref(ln), pix.abi.q, 0,
+                                    engine._stream_handle())
+    assert rc == _lib.MK_ENOMEM
+    assert b"scratch" in L.mk_last_error()
