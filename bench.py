@@ -154,6 +154,41 @@ def cpu_baseline(w, chunks=4, m=32, threads=None, reps=1):
                       f"{threads} threads, {best:.2f} s"}
 
 
+def scan_leg(args, dev):
+    """Batched scan (BASELINE config 4): the first `scan_frames` frames of the
+    4M-atom rocking x chi scan (ROI sides cycling 64/128/256/512), all in one
+    persistent launch captured in a CUDA graph; frames/s over graph replays."""
+    import torch
+
+    from mosaic_gb300 import workloads
+    from mosaic_gb300.scan import BatchedScan, frames_from_motors
+
+    w = workloads.cu_bumps_scan_4m()
+    fr = w.meta["frames"][: args.scan_frames]
+    frames = frames_from_motors(w.stage, w.detector, [dict(mu=f["mu"], chi=f["chi"]) for f in fr],
+                                [f["roi"] for f in fr])
+    t0 = time.perf_counter()
+    scan = BatchedScan(w.beam, w.sample, frames, **w.sc_kwargs)
+    setup_s = time.perf_counter() - t0
+    scan.capture()
+    torch.cuda.synchronize()
+    reps = 2
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        scan.replay()
+    e1.record()
+    e1.synchronize()
+    s = e0.elapsed_time(e1) * 1e-3 / reps
+    npx = int(scan.frame_pixels.sum())
+    return {"workload": "cu_bumps_scan_4m", "frames": len(frames), "frames_total_in_config": 724,
+            "atoms": scan.atoms.n, "pixels": npx, "terms": scan.terms,
+            "frames_per_s": len(frames) / s, "terms_per_s": scan.terms / s, "seconds": s,
+            "setup_seconds": setup_s, "graph": True,
+            "note": "first frames of the 181 theta x 4 chi rocking scan; ROI sides 64/128/256/512 by "
+                    "frame index; atoms staged once, all frames one persistent launch"}
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -219,7 +254,8 @@ def run_ours(args):
     if args.profile:
         launch, tune_tbl = autotune.lookup(pix.n, tiles), []
     else:
-        launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel))
+        launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel),
+                                         fresnel_radius=diag["fresnel_radius_m"])
     B._kernel_launch = launch
     amp_real = tiles.amp_is_real()
     split_times = []
@@ -233,7 +269,7 @@ def run_ours(args):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
         out = engine.run_split(t, p, phys, table, launch=launch, fresnel=int(fresnel),
-                               amp_real=amp_real)
+                               amp_real=amp_real, fresnel_radius=diag["fresnel_radius_m"])
         if record:
             e1.record()
             split_times.append((e0, e1))
@@ -310,6 +346,7 @@ def run_ours(args):
     achieved = terms / (split_ms * 1e-3)
     gpu_launches = args.steps * 8
 
+    scan = scan_leg(args, dev) if (rank == 0 and args.scan_frames > 0) else None
     if rank == 0:
         cpu = cpu_baseline(w) if not args.no_cpu else None
         line = {
@@ -341,6 +378,7 @@ def run_ours(args):
             "autotune": [[float(t), c] for t, c in tune_tbl] if tune_tbl else [],
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "scan": scan,
         }
         print(json.dumps(line))
     if world > 1:
@@ -356,6 +394,8 @@ def main():
     ap.add_argument("--config", default="nacl_screw_8m")
     ap.add_argument("--fp64-subset", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scan-frames", type=int, default=48,
+                    help="frames of the batched-scan leg (0: skip)")
     ap.add_argument("--profile", action="store_true",
                     help="kernel-profile run: cached launch shape, timed steps only")
     args = ap.parse_args()

@@ -121,6 +121,8 @@ typedef struct {
                              (the caller checks k r_tile^2 / 2 R0_min against its budget);
                              -1: keep it */
     int amp_real;         /* 1: every incident amplitude is real (skips two FMAs a term) */
+    double fresnel_radius_m; /* with fresnel != 0: only tiles whose radius exceeds this keep
+                                the |d|^2 term (0: every tile) */
 } mk_launch;
 
 /* --- library ---------------------------------------------------------- */

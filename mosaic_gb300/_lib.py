@@ -140,7 +140,8 @@ class MkTiles(ctypes.Structure):
 
 class MkLaunch(ctypes.Structure):
     _fields_ = [("pix_per_thread", ctypes.c_int), ("threads", ctypes.c_int),
-                ("slices", ctypes.c_int), ("fresnel", ctypes.c_int), ("amp_real", ctypes.c_int)]
+                ("slices", ctypes.c_int), ("fresnel", ctypes.c_int), ("amp_real", ctypes.c_int),
+                ("fresnel_radius_m", ctypes.c_double)]
 
 
 # name -> (restype, argtypes)

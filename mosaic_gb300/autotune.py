@@ -78,7 +78,8 @@ def lookup(n_pix, tiles):
     return dict(DEFAULT)
 
 
-def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, reps=3):
+def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, reps=3,
+         fresnel_radius=0.0):
     """Time every candidate on a probe of the tiles; cache and return the winner."""
     amp_real = tiles.amp_is_real() if amp_real is None else bool(amp_real)
     probe = engine.TilesView(tiles, min(tiles.n_tiles, PROBE_TILES))
@@ -86,13 +87,14 @@ def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, rep
     for pix_pt, nt in (candidates or CANDIDATES):
         cfg = dict(pix_per_thread=pix_pt, threads=nt, slices=0)
         try:
-            engine.run_split(probe, pix, phys, table, launch=cfg, fresnel=fresnel, amp_real=amp_real)
+            engine.run_split(probe, pix, phys, table, launch=cfg, fresnel=fresnel, amp_real=amp_real,
+                             fresnel_radius=fresnel_radius)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             for _ in range(reps):
                 engine.run_split(probe, pix, phys, table, launch=cfg, fresnel=fresnel,
-                                 amp_real=amp_real)
+                                 amp_real=amp_real, fresnel_radius=fresnel_radius)
             e1.record()
             e1.synchronize()
             results.append((e0.elapsed_time(e1) / reps, cfg))

@@ -249,12 +249,16 @@ class beam:
         k = self.k
         r = tiles.max_radius()
         o = tiles.max_origin_norm()
-        third = k * (r ** 3 + o ** 3 + 3 * o * o * r) / max(r0_min, 1e-30) ** 2
-        fresnel_term = k * r * r / (2.0 * max(r0_min, 1e-30))
+        r0 = max(r0_min, 1e-30)
+        third = k * (r ** 3 + o ** 3 + 3 * o * o * r) / r0 ** 2
+        fresnel_term = k * r * r / (2.0 * r0)
         tol = min(float(self._kernel_phase_tol_rad), float(self._phase_tol_rad))
+        # tiles of radius above this keep the |d|^2 term, the rest drop it
+        fresnel_radius = float(np.sqrt(2.0 * r0 * tol / k))
         return third, fresnel_term > tol, tol, dict(tile_radius_m=r, origin_max_m=o,
                                                     third_order_rad=third,
-                                                    fresnel_rad=fresnel_term)
+                                                    fresnel_rad=fresnel_term,
+                                                    fresnel_radius_m=fresnel_radius)
 
     def scatter_device(self, atoms, pix, phys, out=None, accumulate=False, launch=None):
         """Run the configured sum on staged atoms/pixels; float64 (P, 2) on the device."""
@@ -265,7 +269,8 @@ class beam:
             if third <= tol and excursion < 1e-6:
                 cfg = launch or self._kernel_launch or tuned_launch(pix.n, tiles)
                 res = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg,
-                                       fresnel=int(fresnel), out=out, accumulate=accumulate)
+                                       fresnel=int(fresnel), out=out, accumulate=accumulate,
+                                       fresnel_radius=diag["fresnel_radius_m"])
                 self.last_run = dict(path="split_f32", n_tiles=tiles.n_tiles, fresnel=fresnel,
                                      launch=dict(cfg), **diag)
                 return res

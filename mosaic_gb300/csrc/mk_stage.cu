@@ -193,7 +193,9 @@ __global__ void mk_bbox_kernel(int64_t n, const double *__restrict__ pos, unsign
 // Unlike a Z-order (Morton) curve, consecutive cells are always face
 // neighbours, so a run of consecutive atoms never spans two distant corners
 // of the sample and every tile stays compact.
-#define MK_HILBERT_BITS 19
+#define MK_HILBERT_BITS 17   // per axis inside one cube: 51 bits
+#define MK_MAX_CUBES 128     // 7 bits of cube index
+#define MK_KEY_BITS 62       // + 4 bits of species (MK_MAX_SPECIES = 16)
 
 __device__ __forceinline__ unsigned long long mk_hilbert3(uint32_t x, uint32_t y, uint32_t z)
 {
@@ -228,11 +230,14 @@ __device__ __forceinline__ unsigned long long mk_hilbert3(uint32_t x, uint32_t y
     return h;
 }
 
-// Sort key: species in bits 57..63, then the Hilbert index of the atom on a
-// grid that spans the bounding box along each axis separately. A grid with
-// one cell size for all axes would leave most of the curve's cube empty for
-// a slab or a rod, and the curve's excursions through the empty part would
-// put far-apart atoms next to each other in the order.
+// Sort key: species in bits 58..61, then a row of cubes, then the Hilbert
+// index inside the atom's cube. The bounding box is cut into cubes whose
+// side is its shortest extent (enlarged until at most MK_MAX_CUBES), taken
+// x fastest. The curve runs from a cube's (0,0,0) corner to its (max,0,0)
+// corner, so consecutive cubes along x join without a jump; only row ends
+// do. One cube size for all axes keeps tiles round, and filling every cube
+// keeps the curve out of empty space (where its excursions would put
+// far-apart atoms next to each other in the order).
 __global__ void mk_keys_kernel(int64_t n, const double *__restrict__ pos,
                                const int *__restrict__ species,
                                const unsigned long long *__restrict__ bb,
@@ -240,17 +245,32 @@ __global__ void mk_keys_kernel(int64_t n, const double *__restrict__ pos,
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t q[3];
+    double lo[3], span[3], side = 0.0;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const double lo = mk_unordered(bb[c]);
-        double span = mk_unordered(bb[3 + c]) - lo;
-        if (!(span > 0.0)) span = 1.0;
-        double f = (pos[3 * i + c] - lo) / span;
-        f = fmin(fmax(f, 0.0), 1.0);
+        lo[c] = mk_unordered(bb[c]);
+        span[c] = mk_unordered(bb[3 + c]) - lo[c];
+        if (span[c] > 0.0 && (side == 0.0 || span[c] < side)) side = span[c];
+    }
+    if (!(side > 0.0)) side = 1.0;
+    int nc[3];
+    for (;;) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nc[c] = max(1, (int)ceil(span[c] / side - 1e-9));
+        if (nc[0] * nc[1] * nc[2] <= MK_MAX_CUBES) break;
+        side *= 1.25;
+    }
+    uint32_t q[3];
+    int cube[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double t = (pos[3 * i + c] - lo[c]) / side;
+        cube[c] = min(nc[c] - 1, max(0, (int)floor(t)));
+        const double f = fmin(fmax(t - cube[c], 0.0), 1.0);
         q[c] = (uint32_t)(f * (double)((1u << MK_HILBERT_BITS) - 1));
     }
-    keys[i] = ((unsigned long long)species[i] << 57) | mk_hilbert3(q[0], q[1], q[2]);
+    const unsigned long long ci = (unsigned long long)((cube[2] * nc[1] + cube[1]) * nc[0] + cube[0]);
+    keys[i] = ((unsigned long long)species[i] << 58) | (ci << 51) | mk_hilbert3(q[0], q[1], q[2]);
     idx[i] = (int)i;
 }
 
@@ -356,7 +376,7 @@ static size_t mk_cub_temp_bytes(int64_t n)
     size_t tb = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, tb, (unsigned long long *)nullptr,
                                     (unsigned long long *)nullptr, (int *)nullptr, (int *)nullptr,
-                                    (int)n, 0, 61);
+                                    (int)n, 0, MK_KEY_BITS);
     return tb;
 }
 
@@ -426,8 +446,8 @@ extern "C" int mk_tiles_build(int64_t n, const double *pos, const int *species, 
     mk_bbox_kernel<<<nb, th, 0, st>>>(n, pos, bb);
     mk_keys_kernel<<<(unsigned)((n + th - 1) / th), th, 0, st>>>(n, pos, species, bb, k_in, i_in);
     MK_CHECK_CUDA(cudaGetLastError());
-    MK_CHECK_CUDA(cub::DeviceRadixSort::SortPairs(w, temp, k_in, k_out, i_in, i_out, (int)n, 0, 61,
-                                                  st));
+    MK_CHECK_CUDA(cub::DeviceRadixSort::SortPairs(w, temp, k_in, k_out, i_in, i_out, (int)n, 0,
+                                                  MK_KEY_BITS, st));
     if (tiles_needed > 0) {
         mk_tile_kernel<256><<<tiles_needed, 256, 0, st>>>(
             M, k / MK_TWO_PI, pos, reinterpret_cast<const float2 *>(amp), i_out,

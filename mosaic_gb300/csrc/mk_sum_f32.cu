@@ -75,6 +75,7 @@ struct MkSplitArgs {
     float s2fac;       // (k 0.25e-10 / pi)^2: s^2 = s2fac |b - u'|^2 [1/A^2]
     int apply_pol, decay, remove_forward;
     float pdeg;
+    float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
 };
 
 #define TWO_PI_F 6.28318530717958647692f
@@ -127,6 +128,43 @@ __device__ __forceinline__ void mk_issue_tile(const MkSplitArgs &A, float4 *s_po
     mk_mbar_expect_tx(&bar[buf], tile_bytes);
     mk_tma_load_1d(s_pos + buf * T, A.tpos + (size_t)tile * T, T * sizeof(float4), &bar[buf]);
     mk_tma_load_1d(s_amp + buf * T, A.tamp + (size_t)tile * T, T * sizeof(float2), &bar[buf]);
+}
+
+// The terms of one tile against PIX pixels: csr/csi += E_j exp(2 pi i phase).
+// FR adds the |d|^2 term of the in-tile distance (db = D.b per atom).
+template <int PIX, bool FR, bool CPLX>
+__device__ __forceinline__ void mk_tile_terms(const float4 *__restrict__ P,
+                                              const float2 *__restrict__ E, int T,
+                                              const float (&wx)[PIX], const float (&wy)[PIX],
+                                              const float (&wz)[PIX], const float (&hq)[PIX],
+                                              float bx, float by, float bz, float (&csr)[PIX],
+                                              float (&csi)[PIX])
+{
+#pragma unroll 4
+    for (int j = 0; j < T; ++j) {
+        const float4 a = P[j];
+        const float2 e = E[j];
+        float db = 0.f;
+        if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
+#pragma unroll
+        for (int p = 0; p < PIX; ++p) {
+            float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
+            if (FR) {
+                const float sp = db - lin;
+                lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
+            }
+            const float r = mk_frac_nearest(lin);
+            float sn, cs;
+            __sincosf(r * TWO_PI_F, &sn, &cs);
+            if (CPLX) {
+                csr[p] = fmaf(e.x, cs, fmaf(-e.y, sn, csr[p]));
+                csi[p] = fmaf(e.x, sn, fmaf(e.y, cs, csi[p]));
+            } else {
+                csr[p] = fmaf(e.x, cs, csr[p]);
+                csi[p] = fmaf(e.x, sn, csi[p]);
+            }
+        }
+    }
 }
 
 template <int NT, int PIX, bool FRESNEL, bool CPLX>
@@ -218,31 +256,12 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
             float csr[PIX], csi[PIX];
 #pragma unroll
             for (int p = 0; p < PIX; ++p) csr[p] = csi[p] = 0.f;
-#pragma unroll 4
-            for (int j = 0; j < T; ++j) {
-                const float4 a = P[j];
-                const float2 e = E[j];
-                float db = 0.f;
-                if (FRESNEL) db = fmaf(a.z, F.b[2], fmaf(a.y, F.b[1], a.x * F.b[0]));
-#pragma unroll
-                for (int p = 0; p < PIX; ++p) {
-                    float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
-                    if (FRESNEL) {
-                        const float sp = db - lin;
-                        lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
-                    }
-                    const float r = mk_frac_nearest(lin);
-                    float sn, cs;
-                    __sincosf(r * TWO_PI_F, &sn, &cs);
-                    if (CPLX) {
-                        csr[p] = fmaf(e.x, cs, fmaf(-e.y, sn, csr[p]));
-                        csi[p] = fmaf(e.x, sn, fmaf(e.y, cs, csi[p]));
-                    } else {
-                        csr[p] = fmaf(e.x, cs, csr[p]);
-                        csi[p] = fmaf(e.x, sn, csi[p]);
-                    }
-                }
-            }
+            // The |d|^2 term only for tiles wide enough to need it (uniform
+            // across the block: no divergence).
+            if (FRESNEL && (float)o.w > A.fres_r)
+                mk_tile_terms<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
+            else
+                mk_tile_terms<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
             __syncthreads();   // every thread is done with buffer `buf`
             if (tid == 0 && t + 2 < t_hi) {
                 mk_fence_proxy_async();
@@ -562,6 +581,7 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
     A.decay = phys->spherical_decay;
     A.remove_forward = phys->remove_forward;
     A.pdeg = (float)phys->pol_deg;
+    A.fres_r = launch->fresnel_radius_m > 0.0 ? (float)launch->fresnel_radius_m : 0.f;
     MK_CHECK_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned long long), st));
     const long long grid = std::min<long long>(n_items, sh.resident);
     sh.fn<<<(unsigned)grid, launch->threads, mk_split_smem(T), st>>>(A);

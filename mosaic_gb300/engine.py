@@ -225,12 +225,15 @@ DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0)
 
 
 def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None, fresnel=-1,
-              amp_real=None, out=None, accumulate=False, stream=None):
-    """FP32 split-phase sum; returns float64 (P, 2) (a view of `out` if given)."""
+              amp_real=None, out=None, accumulate=False, stream=None, fresnel_radius=0.0):
+    """FP32 split-phase sum; returns float64 (P, 2) (a view of `out` if given).
+    With ``fresnel`` set, only tiles wider than ``fresnel_radius`` [m] keep the
+    |d|^2 term (0: all tiles)."""
     L = _require_cuda()
     cfg = dict(DEFAULT_LAUNCH, **(launch or {}))
     ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
-                  int(tiles.amp_is_real() if amp_real is None else bool(amp_real)))
+                  int(tiles.amp_is_real() if amp_real is None else bool(amp_real)),
+                  float(fresnel_radius))
     wsb = ctypes.c_size_t(0)
     check(L.mk_split_plan(ctypes.byref(tiles.abi), ctypes.byref(pix.abi), ctypes.byref(ln),
                           ctypes.byref(wsb)))

@@ -108,7 +108,8 @@ class BatchedScan:
         self.diag = diag
         cfg = dict(engine.DEFAULT_LAUNCH, **(launch or beam._kernel_launch or {}))
         self.launch = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]),
-                               int(fresnel), int(self.tiles.amp_is_real()))
+                               int(fresnel), int(self.tiles.amp_is_real()),
+                               float(diag["fresnel_radius_m"]))
         nf = len(self.frames)
         desc = (MkFrameDesc * nf)()
         n_items, n_part = ctypes.c_longlong(0), ctypes.c_longlong(0)
