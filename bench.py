@@ -154,6 +154,26 @@ def cpu_baseline(w, chunks=4, m=32, threads=None, reps=1):
                       f"{threads} threads, {best:.2f} s"}
 
 
+def probe_pipes(dev):
+    """Per-clock per-SM throughput of the MUFU (sin+cos), FRND and FFMA pipes
+    on this GPU (mk_probe_throughput)."""
+    import ctypes
+
+    import torch
+
+    from mosaic_gb300 import _lib, engine
+    L = _lib.load()
+    ws_n = int(L.mk_probe_workspace_size())
+    ws = torch.empty(ws_n, dtype=torch.uint8, device=dev)
+    out = {}
+    for kind, name, iters in ((1, "sincos", 2048), (2, "frnd", 2048), (3, "ffma", 16384)):
+        v = ctypes.c_double(0.0)
+        _lib.check(L.mk_probe_throughput(kind, iters, ws.data_ptr(), ws_n, ctypes.byref(v),
+                                         engine._stream_handle()))
+        out[name] = float(v.value)
+    return out
+
+
 def scan_leg(args, dev):
     """Batched scan (BASELINE config 4): the first `scan_frames` frames of the
     4M-atom rocking x chi scan (ROI sides cycling 64/128/256/512), all in one
@@ -342,7 +362,10 @@ def run_ours(args):
     peaks, peak_src = _peaks()
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     clk = float(peaks.get("sm_max_mhz", 2070.0))
-    peak_terms = min(MUFU_PER_CLK_SM / MUFU_PER_TERM, FP32_PER_CLK_SM / FP32_PER_TERM) * n_sm * clk * 1e6
+    pipes = probe_pipes(dev)
+    mufu = pipes.get("sincos", MUFU_PER_CLK_SM)
+    fma = pipes.get("ffma", FP32_PER_CLK_SM)
+    peak_terms = min(mufu / MUFU_PER_TERM, fma / FP32_PER_TERM) * n_sm * clk * 1e6
     achieved = terms / (split_ms * 1e-3)
     gpu_launches = args.steps * 8
 
@@ -365,8 +388,11 @@ def run_ours(args):
             "gpu_launches": gpu_launches,
             "roofline": {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak_terms / 1e9,
                          "unit": "Gterm/s", "frac": achieved / peak_terms, "traffic": None,
-                         "peak_source": f"{MUFU_PER_CLK_SM} sin/cos per clk per SM / 2 per term x "
-                                        f"{n_sm} SMs x {clk:.0f} MHz ({peak_src} max clock)",
+                         "peak_source": f"min(MUFU sin/cos {mufu:.2f}/clk/SM / 2 per term, FFMA "
+                                        f"{fma:.1f}/clk/SM / 12 per term), both measured on this "
+                                        f"GPU by mk_probe_throughput, x {n_sm} SMs x {clk:.0f} MHz "
+                                        f"({peak_src} max clock)",
+                         "pipe_probe_ops_per_clk_per_sm": pipes,
                          "split_kernel_ms": split_ms},
             "fp64_plain": {"value": fp64_rate, "unit": "Gatom*pixel/s",
                            "subset": f"central {m}x{m} pixels, all atoms",

@@ -238,7 +238,59 @@ int mk_kin_scan_f32(const mk_tiles *tiles, const mk_species *sp, const mk_physic
                     long long n_items, long long n_partial, const mk_launch *launch, double *out,
                     double *intensity_sums, void *workspace, size_t ws_bytes, void *stream);
 
+/* --- free-space propagation ------------------------------------------- */
+/* Replaces the pad / prop_mul_kernel / crop steps of
+ * _angular_spectrum_propagate_gpu (Beam.py:7829-7943, 4747-4834); the FFTs
+ * between them are the caller's (cuFFT). Arrays are interleaved complex64.
+ * mk_prop_pad: (nz, ny) -> (nz2, ny2) placed at (z0, y0); mode 0 replicates
+ * the edges, mode 1 fills with (cval_re, cval_im). */
+int mk_prop_pad(const float *field, int ny, int nz, float *padded, int ny2, int nz2, int y0,
+                int z0, int mode, float cval_re, float cval_im, void *stream);
+/* In-place multiply of the (nz2, ny2) spectrum (FFT order, pitches dy, dz [m])
+ * by the propagator over z [m] with the carrier (k_axis, k_perp_y, k_perp_z)
+ * removed; k_axis = k for a forward beam. Phase formed in FP64. */
+int mk_prop_mul(float *spectrum, int ny2, int nz2, double dy, double dz, double k, double z,
+                double k_axis, double k_perp_y, double k_perp_z, void *stream);
+/* Centre crop (nz, ny) at (z0, y0) of the inverse transform times `scale`,
+ * fused with |A|^2: writes field (complex64) and/or intensity (float32). */
+int mk_prop_crop_abs2(const float *grid, int ny2, int nz2, int y0, int z0, int ny, int nz,
+                      float scale, float *field, float *intensity, void *stream);
+
+/* --- scan surrogate (BF16 MLP) ------------------------------------------ */
+/* No counterpart in the reference: the learned part of the scan path. BF16
+ * operands, FP32 accumulation on the tensor cores (mma.sync m16n8k16).
+ * C[M,N] (+)= A[M,K] B[K,N]: A(m,k) at A[m*sam + k*sak], B(k,n) at
+ * B[k*sbk + n*sbn] (bf16); C float32 row stride ldc (or NULL); Cb bf16 copy
+ * row stride ldcb (or NULL); flags: 1 accumulate into C, 2 add bias[n],
+ * 4 ReLU. */
+int mk_gemm_bf16(int M, int N, int K, const void *A, long long sam, long long sak, const void *B,
+                 long long sbk, long long sbn, float *C, long long ldc, const float *bias,
+                 int flags, void *Cb, long long ldcb, void *stream);
+/* Inputs of the network: (x, y) and sin/cos(2 pi f_j x), sin/cos(2 pi f_j y),
+ * f_j = 2^(j/2)/2, j < n_freq, zero-padded to `width` bf16 columns. */
+int mk_fourier_features(int n, const float *xy, int n_freq, int width, void *out, void *stream);
+int mk_relu_backward(long long n, const float *grad, const float *pre, float *gout,
+                     void *gout_bf16, void *stream);
+int mk_bias_grad(int M, int N, const float *g, float *db, void *stream);
+/* MSE over n entries: grad = 2(y - t)/n (float and/or bf16), partial sums of
+ * squares per 256-block in `partials` (ceil(n/256) doubles). */
+int mk_mse(long long n, const float *y, const float *t, float *grad, void *grad_bf16,
+           double *partials, void *stream);
+/* Adam step `step` (1-based) on FP32 master weights w, moments m, v; writes
+ * the bf16 copy w_bf16 (or NULL). */
+int mk_adam(long long n, float *w, const float *g, float *m, float *v, void *w_bf16, float lr,
+            float beta1, float beta2, float eps, int step, float weight_decay, void *stream);
+
 /* --- diagnostics ------------------------------------------------------ */
+/* Pipe-throughput microbenchmark (no counterpart in the reference): results
+ * per clock per SM of kind 0 MUFU sine, 1 MUFU sine+cosine (two results per
+ * call), 2 FRND (rintf), 3 FFMA, over one wave of blocks; `iters` loop trips
+ * of eight chains per thread. Synchronises `stream`. Workspace of
+ * mk_probe_workspace_size() bytes (device). Gives the split kernel's roofline
+ * denominator on the GPU at hand. */
+size_t mk_probe_workspace_size(void);
+int mk_probe_throughput(int kind, int iters, void *workspace, size_t ws_bytes,
+                        double *ops_per_clk_per_sm, void *stream);
 /* Launch a kernel whose bounded mbarrier wait is never satisfied: it gives
  * up after limit_ns (<= 1 s), records a timeout, and mk_sync_status() then
  * returns MK_ETIMEOUT. Exercises the error path of the tile-copy waits

@@ -161,6 +161,28 @@ SIGNATURES = {
                                         ctypes.POINTER(MkPhysics), ctypes.POINTER(MkPixels),
                                         ctypes.c_int, _vp, ctypes.c_int, _vp, ctypes.c_size_t, _vp]),
     "mk_debug_wait_timeout": (ctypes.c_int, [ctypes.c_uint64, _vp]),
+    "mk_probe_workspace_size": (ctypes.c_size_t, []),
+    "mk_probe_throughput": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_double), _vp]),
+    "mk_gemm_bf16": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_longlong,
+                                    ctypes.c_longlong, _vp, ctypes.c_longlong, ctypes.c_longlong,
+                                    _vp, ctypes.c_longlong, _vp, ctypes.c_int, _vp,
+                                    ctypes.c_longlong, _vp]),
+    "mk_fourier_features": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+    "mk_relu_backward": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp]),
+    "mk_bias_grad": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    "mk_mse": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "mk_adam": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
+                               ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int,
+                               ctypes.c_float, _vp]),
+    "mk_prop_pad": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                   ctypes.c_float, _vp]),
+    "mk_prop_mul": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, _vp]),
+    "mk_prop_crop_abs2": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_float, _vp, _vp, _vp]),
     "mk_split_plan": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkPixels),
                                      ctypes.POINTER(MkLaunch), ctypes.POINTER(ctypes.c_size_t)]),
     "mk_kin_split_f32_noalloc": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkSpecies),

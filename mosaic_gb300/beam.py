@@ -349,6 +349,40 @@ class beam:
         detector.input_pixel_values(final)
 
 
+    # --------------------------------------------------------- propagation
+    def wavefield_propagation(self, detector, optics, use_gpu=True, step_max=None, pad_factor=1.0,
+                              padding_mode="edge", pad_constant=0.0, save_field=True):
+        """Propagate the detector field through an optics stack
+        (Beam.py:8024-8095): free-space segments run on the GPU
+        (``propagation.propagate``); ``optics`` is a reference optics object
+        or a ``propagation.FreeSpaceStack``."""
+        from . import propagation
+        if not use_gpu:
+            raise RuntimeError("wavefield_propagation: use_gpu=False is not supported")
+        dy, dz = np.asarray(detector.pixel_size, dtype=np.float64) * 1e-10
+        E = detector.pixel_values
+        if E is None:
+            raise ValueError("detector.pixel_values is None. Run atomic_direct_interaction() first "
+                             "to populate the detector field before calling wavefield_propagation().")
+        if self._wavelength is None:
+            raise ValueError("Beam wavelength is not set. Call create_beam() first.")
+
+        def free_space(F, dym, dzm, z):
+            return propagation.propagate(F, dym, dzm, z, self._wavelength, step_max=step_max,
+                                         pad_factor=pad_factor, padding_mode=padding_mode,
+                                         pad_constant=pad_constant)
+
+        E = optics.apply_stack(field=E, dx=dy, dy=dz, wavelength=self._wavelength,
+                               propagate_free_space=free_space, use_gpu=True)
+        if isinstance(E, torch.Tensor):
+            E = E.cpu().numpy()
+        E = np.asarray(E).astype(np.complex64)
+        if save_field:
+            detector.input_pixel_values(E)
+            return None
+        return E
+
+
 def tuned_launch(n_pix, tiles):
     """Launch shape for the split kernel: the autotuner's cached winner, or
     the default when none is cached."""
