@@ -65,7 +65,7 @@ class BatchedScan:
     """
 
     def __init__(self, beam, sample, frames, apply_polarization=False, spherical_decay=False,
-                 remove_forward=False, launch=None, device="cuda"):
+                 remove_forward=False, launch=None, device="cuda", staged=None):
         self.L = engine._require_cuda()
         self.beam = beam
         self.frames = list(frames)
@@ -73,14 +73,22 @@ class BatchedScan:
             raise ValueError("a scan needs at least one frame")
         beam._require_forward_beam()
         dev = torch.device(device)
-        pos, idx, labels = beam.collect_atoms(sample)
-        self._check_uniform_beam(pos)
-        table = engine.SpeciesTable.build(labels or ["H"], beam.tables, beam._energy,
-                                          beam._debye_waller)
-        # atoms in the sample frame, incident amplitude 1
-        self.atoms = engine.atoms_lab(pos, idx, np.eye(3), np.zeros(3), table, device=dev)
-        self.table = table
-        self.tiles = engine.Tiles(self.atoms, beam.k, beam._kernel_tile_atoms, device=dev)
+        if staged is not None:
+            # reuse the atoms and tiles of an earlier scan of the same sample
+            self._rmax = staged._rmax
+            self._check_uniform_beam(None)
+            self.atoms, self.table, self.tiles = staged.atoms, staged.table, staged.tiles
+        else:
+            pos, idx, labels = beam.collect_atoms(sample)
+            self._rmax = (float(np.sqrt((pos.astype(np.float64) ** 2).sum(1)).max())
+                          if pos.shape[0] else 0.0)
+            self._check_uniform_beam(None)
+            table = engine.SpeciesTable.build(labels or ["H"], beam.tables, beam._energy,
+                                              beam._debye_waller)
+            # atoms in the sample frame, incident amplitude 1
+            self.atoms = engine.atoms_lab(pos, idx, np.eye(3), np.zeros(3), table, device=dev)
+            self.table = table
+            self.tiles = engine.Tiles(self.atoms, beam.k, beam._kernel_tile_atoms, device=dev)
         pol = beam._polarization_state()
         e_lab = np.array(pol[1:4], dtype=np.float64)
         b_lab = np.array([1.0, 0.0, 0.0])
@@ -136,8 +144,8 @@ class BatchedScan:
                                       "one by one through atomic_scattering_kinematic")
         if not np.all(np.abs(B._beam_E0_map) == 1.0):
             raise NotImplementedError("batched scans need a uniform beam map")
-        if pos.shape[0]:
-            rmax = float(np.sqrt((pos.astype(np.float64) ** 2).sum(1)).max())
+        if self._rmax > 0.0:
+            rmax = self._rmax
             for f in self.frames:
                 c = np.asarray(f.translation, dtype=np.float64)
                 half_u = 0.5 * B._beam_size[0] - abs(c[1])
