@@ -267,8 +267,9 @@ int mk_gemm_bf16(int M, int N, int K, const void *A, long long sam, long long sa
                  long long sbk, long long sbn, float *C, long long ldc, const float *bias,
                  int flags, void *Cb, long long ldcb, void *stream);
 /* Inputs of the network: (x, y) and sin/cos(2 pi f_j x), sin/cos(2 pi f_j y),
- * f_j = 2^(j/2)/2, j < n_freq, zero-padded to `width` bf16 columns. */
-int mk_fourier_features(int n, const float *xy, int n_freq, int width, void *out, void *stream);
+ * f_j = f0 ratio^j, j < n_freq, zero-padded to `width` bf16 columns. */
+int mk_fourier_features(int n, const float *xy, int n_freq, float f0, float ratio, int width,
+                        void *out, void *stream);
 int mk_relu_backward(long long n, const float *grad, const float *pre, float *gout,
                      void *gout_bf16, void *stream);
 int mk_bias_grad(int M, int N, const float *g, float *db, void *stream);

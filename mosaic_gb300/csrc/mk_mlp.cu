@@ -126,9 +126,9 @@ extern "C" int mk_gemm_bf16(int M, int N, int K, const void *A, long long sam, l
 }
 
 // features[b] = [x, y, sin(2 pi f_j x), cos(2 pi f_j x), sin(2 pi f_j y), cos(2 pi f_j y)]_j,
-// f_j = 2^(j/2) / 2 (j = 0 .. nf-1), zero-padded to `width` columns, bf16.
-__global__ void mk_fourier_kernel(int n, const float *__restrict__ xy, int nf, int width,
-                                  __nv_bfloat16 *__restrict__ out)
+// f_j = f0 ratio^j (j = 0 .. nf-1), zero-padded to `width` columns, bf16.
+__global__ void mk_fourier_kernel(int n, const float *__restrict__ xy, int nf, float f0,
+                                  float ratio, int width, __nv_bfloat16 *__restrict__ out)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
@@ -136,8 +136,8 @@ __global__ void mk_fourier_kernel(int n, const float *__restrict__ xy, int nf, i
     __nv_bfloat16 *o = out + (size_t)b * width;
     o[0] = __float2bfloat16(x);
     o[1] = __float2bfloat16(y);
-    for (int j = 0; j < nf; ++j) {
-        const float f = 0.5f * exp2f(0.5f * (float)j);
+    float f = f0;
+    for (int j = 0; j < nf; ++j, f *= ratio) {
         float sx, cx, sy, cy;
         sincospif(2.f * f * x, &sx, &cx);
         sincospif(2.f * f * y, &sy, &cy);
@@ -149,13 +149,14 @@ __global__ void mk_fourier_kernel(int n, const float *__restrict__ xy, int nf, i
     for (int c = 2 + 4 * nf; c < width; ++c) o[c] = __float2bfloat16(0.f);
 }
 
-extern "C" int mk_fourier_features(int n, const float *xy, int n_freq, int width, void *out,
-                                   void *stream)
+extern "C" int mk_fourier_features(int n, const float *xy, int n_freq, float f0, float ratio,
+                                   int width, void *out, void *stream)
 {
-    MK_REQUIRE(n > 0 && xy && out && n_freq >= 0 && width >= 2 + 4 * n_freq,
+    MK_REQUIRE(n > 0 && xy && out && n_freq >= 0 && width >= 2 + 4 * n_freq && f0 > 0.f &&
+                   ratio >= 1.f,
                "mk_fourier_features: bad arguments");
     mk_fourier_kernel<<<(n + 127) / 128, 128, 0, mk_stream(stream)>>>(
-        n, xy, n_freq, width, static_cast<__nv_bfloat16 *>(out));
+        n, xy, n_freq, f0, ratio, width, static_cast<__nv_bfloat16 *>(out));
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
 }

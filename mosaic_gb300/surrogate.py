@@ -149,15 +149,20 @@ class MLP:
         return torch.cat(outs)
 
 
-def fourier_features(xy, n_freq=16, device="cuda"):
-    """(n, 2) coordinates in [-1, 1] -> (n, width) bf16 network inputs."""
+def fourier_features(xy, n_freq=16, device="cuda", f_max=4.0, f_min=0.25):
+    """(n, 2) coordinates in [-1, 1] -> (n, width) bf16 network inputs with
+    ``n_freq`` frequencies geometrically spaced from f_min to f_max cycles per
+    unit. f_max must stay below the Nyquist limit of the training grid
+    (n_train_per_axis / 4 cycles per unit): higher features only alias
+    between training frames."""
     L = engine._require_cuda()
     xy = torch.as_tensor(np.ascontiguousarray(xy, dtype=np.float32)).to(device)
     width = 2 + 4 * int(n_freq)
     width = (width + 7) // 8 * 8
+    ratio = (f_max / f_min) ** (1.0 / max(int(n_freq) - 1, 1)) if n_freq > 1 else 1.0
     out = torch.empty((int(xy.shape[0]), width), dtype=torch.bfloat16, device=device)
-    check(L.mk_fourier_features(int(xy.shape[0]), _p(xy), int(n_freq), width, _p(out),
-                                engine._stream_handle()))
+    check(L.mk_fourier_features(int(xy.shape[0]), _p(xy), int(n_freq), float(f_min),
+                                float(max(ratio, 1.0)), width, _p(out), engine._stream_handle()))
     return out
 
 
@@ -209,6 +214,8 @@ class SurrogateScan:
     def exact(self, idx):
         """Exact intensities (len(idx), roi*roi) of the given frames, one batched launch."""
         idx = np.asarray(idx)
+        if idx.size == 0:
+            return torch.zeros((0, self.roi * self.roi), dtype=torch.float32, device=self.dev)
         frames = frames_from_motors(self.stage, self.detector, [self.steps[i] for i in idx],
                                     [self.roi] * len(idx))
         if len(frames) == 1:               # a one-frame batch still goes through the scan path
@@ -236,7 +243,9 @@ class SurrogateScan:
         logI = torch.log(I_train + eps)
         mu, sd = logI.mean(0, keepdim=True), logI.std(0, keepdim=True).clamp_min(1e-3)
         T = ((logI - mu) / sd).contiguous()
-        feats = fourier_features(self.xy, self.n_freq, self.dev)
+        # highest feature frequency: half the Nyquist limit of the training grid
+        n_axis = min(len(np.unique(self.ij[tr, 0])), len(np.unique(self.ij[tr, 1])))
+        feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=max(0.5, n_axis / 8.0))
         t0 = time.perf_counter()
         self.net = MLP(feats.shape[1], T.shape[1], self.hidden, self.n_hidden, self.seed, self.dev)
         self.losses = self.net.fit(feats[torch.as_tensor(tr, device=self.dev)], T,
@@ -282,7 +291,8 @@ class SurrogateScan:
         if verify:
             rng = np.random.default_rng(self.seed + 1)
             unjudged = np.setdiff1d(np.arange(len(pred_idx)), np.concatenate([judged, fb]))
-            pick = rng.choice(unjudged, size=min(int(verify), unjudged.size), replace=False)
+            pick = rng.choice(unjudged, size=min(int(verify), unjudged.size), replace=False) \
+                if unjudged.size else np.zeros(0, np.int64)
             I_true = self.exact(pred_idx[pick])
             res["verify_err"] = frame_rel_error(I_pred[torch.as_tensor(pick, device=self.dev)],
                                                 I_true).cpu().numpy()
