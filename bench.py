@@ -40,6 +40,10 @@ PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 MUFU_PER_CLK_SM = 16        # sin/cos results per clock per SM (MUFU)
 FP32_PER_CLK_SM = 128
 MUFU_PER_TERM, FP32_PER_TERM = 2, 12   # canonical split-phase term
+# pixel-pair form: one sin/cos per two terms; per pair 22 FP32-pipe ops (two
+# 3-term dot products, rounding 2, scale 1, delta^2 1, cos/sin polynomials 6,
+# amplitude 2, four accumulators 4)
+MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR = 1, 11
 
 
 def _dist():
@@ -271,11 +275,16 @@ def run_ours(args):
     tiles = engine.Tiles(atoms, B.k, B._kernel_tile_atoms, device=dev)
     pix = engine.Pixels(coords_m, ny, nz, phys, device=dev)
     third, fresnel, tol, diag = B.split_budget(tiles, pix.r0_min())
+    pair_delta = engine.pair_delta(tiles, pix, B.k)
+    diag["pair_delta_rad"] = pair_delta
+    pairs_ok = pair_delta <= engine.PAIR_DELTA_MAX and not args.no_pairs
     if args.profile:
-        launch, tune_tbl = autotune.lookup(pix.n, tiles), []
+        launch, tune_tbl = autotune.lookup(pix.n, tiles, pairs_ok), []
     else:
         launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel),
-                                         fresnel_radius=diag["fresnel_radius_m"])
+                                         fresnel_radius=diag["fresnel_radius_m"], pairs_ok=pairs_ok)
+    if launch.get("pairs"):
+        launch = dict(launch, pair_short_radius_m=engine.pair_short_radius(tiles, pix, B.k))
     B._kernel_launch = launch
     amp_real = tiles.amp_is_real()
     split_times = []
@@ -365,7 +374,13 @@ def run_ours(args):
     pipes = probe_pipes(dev)
     mufu = pipes.get("sincos", MUFU_PER_CLK_SM)
     fma = pipes.get("ffma", FP32_PER_CLK_SM)
+    # canonical term (2 MUFU + 12 FP32) for the roofline, whatever form runs;
+    # the pixel-pair form's own bound beside it
+    paired = bool(launch.get("pairs", 0))
     peak_terms = min(mufu / MUFU_PER_TERM, fma / FP32_PER_TERM) * n_sm * clk * 1e6
+    bound = "mufu" if mufu / MUFU_PER_TERM <= fma / FP32_PER_TERM else "fp32"
+    mufu_pt, fp32_pt = (MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR) if paired else (MUFU_PER_TERM, FP32_PER_TERM)
+    form_peak = min(mufu / mufu_pt, fma / fp32_pt) * n_sm * clk * 1e6
     achieved = terms / (split_ms * 1e-3)
     gpu_launches = args.steps * 8
 
@@ -386,12 +401,17 @@ def run_ours(args):
             "e2e": {"value": terms * world / e2e_s / 1e9, "unit": "Gatom*pixel/s",
                     "seconds": e2e_s, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": gpu_launches,
-            "roofline": {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak_terms / 1e9,
+            "roofline": {"bound": bound, "achieved": achieved / 1e9, "peak": peak_terms / 1e9,
                          "unit": "Gterm/s", "frac": achieved / peak_terms, "traffic": None,
-                         "peak_source": f"min(MUFU sin/cos {mufu:.2f}/clk/SM / 2 per term, FFMA "
-                                        f"{fma:.1f}/clk/SM / 12 per term), both measured on this "
+                         "peak_source": f"canonical term: min(MUFU sin/cos {mufu:.2f}/clk/SM / "
+                                        f"{MUFU_PER_TERM} per term, FP32 {fma:.1f}/clk/SM / "
+                                        f"{FP32_PER_TERM} per term), both pipes measured on this "
                                         f"GPU by mk_probe_throughput, x {n_sm} SMs x {clk:.0f} MHz "
                                         f"({peak_src} max clock)",
+                         "form": {"name": "pixel pairs (one sin/cos per two terms)" if paired
+                                  else "one sin/cos per term",
+                                  "mufu_per_term": mufu_pt, "fp32_per_term": fp32_pt,
+                                  "peak": form_peak / 1e9, "frac": achieved / form_peak},
                          "pipe_probe_ops_per_clk_per_sm": pipes,
                          "split_kernel_ms": split_ms},
             "fp64_plain": {"value": fp64_rate, "unit": "Gatom*pixel/s",
@@ -420,6 +440,8 @@ def main():
     ap.add_argument("--config", default="nacl_screw_8m")
     ap.add_argument("--fp64-subset", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-pairs", action="store_true",
+                    help="one sin/cos per term (the pixel-pair form off)")
     ap.add_argument("--scan-frames", type=int, default=48,
                     help="frames of the batched-scan leg (0: skip)")
     ap.add_argument("--profile", action="store_true",

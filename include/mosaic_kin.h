@@ -123,6 +123,13 @@ typedef struct {
     int amp_real;         /* 1: every incident amplitude is real (skips two FMAs a term) */
     double fresnel_radius_m; /* with fresnel != 0: only tiles whose radius exceeds this keep
                                 the |d|^2 term (0: every tile) */
+    int pairs;            /* 1: pixels 2j, 2j+1 of every frame share one MUFU sin/cos (their
+                             phase difference on FMA-pipe polynomials); the caller checks that
+                             the half difference pi |D| |w_a - w_b| stays below 0.5 rad for
+                             every tile (pix_per_thread even) */
+    double pair_short_radius_m; /* with pairs: tiles up to this radius keep the half
+                             difference below 0.07 rad and use the short polynomial
+                             (0: none does) */
 } mk_launch;
 
 /* --- library ---------------------------------------------------------- */
@@ -277,6 +284,10 @@ int mk_bias_grad(int M, int N, const float *g, float *db, void *stream);
  * squares per 256-block in `partials` (ceil(n/256) doubles). */
 int mk_mse(long long n, const float *y, const float *t, float *grad, void *grad_bf16,
            double *partials, void *stream);
+/* The same with entry (i, j) of the row-major (n / n_col, n_col) arrays
+ * weighted by col_w[j]: grad = 2 w (y - t)/n, partial sums of w (y - t)^2. */
+int mk_mse_weighted(long long n, int n_col, const float *y, const float *t, const float *col_w,
+                    float *grad, void *grad_bf16, double *partials, void *stream);
 /* Adam step `step` (1-based) on FP32 master weights w, moments m, v; writes
  * the bf16 copy w_bf16 (or NULL). */
 int mk_adam(long long n, float *w, const float *g, float *m, float *v, void *w_bf16, float lr,

@@ -141,7 +141,8 @@ class MkTiles(ctypes.Structure):
 class MkLaunch(ctypes.Structure):
     _fields_ = [("pix_per_thread", ctypes.c_int), ("threads", ctypes.c_int),
                 ("slices", ctypes.c_int), ("fresnel", ctypes.c_int), ("amp_real", ctypes.c_int),
-                ("fresnel_radius_m", ctypes.c_double)]
+                ("fresnel_radius_m", ctypes.c_double), ("pairs", ctypes.c_int),
+                ("pair_short_radius_m", ctypes.c_double)]
 
 
 # name -> (restype, argtypes)
@@ -173,6 +174,8 @@ SIGNATURES = {
     "mk_relu_backward": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp]),
     "mk_bias_grad": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     "mk_mse": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "mk_mse_weighted": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _vp, _vp, _vp, _vp, _vp,
+                                       _vp, _vp]),
     "mk_adam": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int,
                                ctypes.c_float, _vp]),

@@ -1,7 +1,9 @@
 """Autotuner for the split-phase kernel's launch shape.
 
-Candidates are (pixels per thread, threads per block); the slice count is
-then chosen inside the library to fill whole waves of the GPU. Each candidate
+Candidates are (pixels per thread, threads per block, pixel pairs); the
+slice count is then chosen inside the library to fill whole waves of the GPU.
+Pair candidates (one sin/cos shared by two neighbouring pixels) are only
+tried where the caller says the geometry allows them. Each candidate
 is timed with CUDA events on a probe -- the first ``PROBE_TILES`` tiles
 against every pixel, the same per-term work as the full problem -- and the
 winner is cached per (device, detector-size bucket, tile size, kernel source
@@ -20,7 +22,8 @@ import torch
 from . import engine
 
 CANDIDATES = [(4, 128), (4, 256), (2, 256), (8, 128), (2, 128), (8, 64), (4, 64), (1, 256)]
-DEFAULT = dict(pix_per_thread=4, threads=128, slices=0)
+PAIR_CANDIDATES = [(4, 128), (4, 256), (8, 128), (2, 256), (8, 64)]
+DEFAULT = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
 PROBE_TILES = 96
 _mem = {}
 _lock = threading.Lock()
@@ -38,10 +41,10 @@ def _src_hash():
         return hashlib.sha1(fh.read()).hexdigest()[:12]
 
 
-def _key(n_pix, tiles):
+def _key(n_pix, tiles, pairs_ok=False):
     dev = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
     bucket = 1 << max(0, (int(n_pix) - 1).bit_length())
-    return f"{dev}|{bucket}|{tiles.tile_atoms}|{_src_hash()}"
+    return f"{dev}|{bucket}|{tiles.tile_atoms}|{'p' if pairs_ok else 's'}|{_src_hash()}"
 
 
 def _load():
@@ -67,33 +70,43 @@ def _store(key, val):
             pass
 
 
-def lookup(n_pix, tiles):
-    key = _key(n_pix, tiles)
+def lookup(n_pix, tiles, pairs_ok=False):
+    key = _key(n_pix, tiles, pairs_ok)
     if key in _mem:
         return dict(_mem[key])
     d = _load().get(key)
     if d:
         _mem[key] = d
         return dict(d)
-    return dict(DEFAULT)
+    return dict(DEFAULT, pairs=int(bool(pairs_ok)))
 
 
 def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, reps=3,
-         fresnel_radius=0.0):
+         fresnel_radius=0.0, pairs_ok=False):
     """Time every candidate on a probe of the tiles; cache and return the winner."""
     amp_real = tiles.amp_is_real() if amp_real is None else bool(amp_real)
     probe = engine.TilesView(tiles, min(tiles.n_tiles, PROBE_TILES))
+    if candidates is None:
+        candidates = [(p, t, 0) for p, t in CANDIDATES]
+        if pairs_ok:
+            candidates += [(p, t, 1) for p, t in PAIR_CANDIDATES]
+    short_r = engine.pair_short_radius(tiles, pix, phys.k) if pairs_ok else 0.0
     results = []
-    for pix_pt, nt in (candidates or CANDIDATES):
-        cfg = dict(pix_per_thread=pix_pt, threads=nt, slices=0)
+    for cand in candidates:
+        pix_pt, nt = cand[0], cand[1]
+        pr = int(cand[2]) if len(cand) > 2 else 0
+        if pr and not pairs_ok:
+            continue
+        cfg = dict(pix_per_thread=pix_pt, threads=nt, slices=0, pairs=pr)
+        run_cfg = dict(cfg, pair_short_radius_m=short_r)
         try:
-            engine.run_split(probe, pix, phys, table, launch=cfg, fresnel=fresnel, amp_real=amp_real,
-                             fresnel_radius=fresnel_radius)
+            engine.run_split(probe, pix, phys, table, launch=run_cfg, fresnel=fresnel,
+                             amp_real=amp_real, fresnel_radius=fresnel_radius)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             for _ in range(reps):
-                engine.run_split(probe, pix, phys, table, launch=cfg, fresnel=fresnel,
+                engine.run_split(probe, pix, phys, table, launch=run_cfg, fresnel=fresnel,
                                  amp_real=amp_real, fresnel_radius=fresnel_radius)
             e1.record()
             e1.synchronize()
@@ -103,7 +116,7 @@ def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, rep
     if not results:
         return dict(DEFAULT), []
     best = min(results, key=lambda r: r[0])[1]
-    key = _key(pix.n, tiles)
+    key = _key(pix.n, tiles, pairs_ok)
     _mem[key] = best
     _store(key, best)
     return dict(best), results

@@ -267,12 +267,18 @@ class beam:
             third, fresnel, tol, diag = self.split_budget(tiles, pix.r0_min())
             excursion = 2.0 * diag["tile_radius_m"] / max(pix.r0_min(), 1e-30)
             if third <= tol and excursion < 1e-6:
-                cfg = launch or self._kernel_launch or tuned_launch(pix.n, tiles)
+                delta = engine.pair_delta(tiles, pix, self.k)
+                pairs_ok = delta <= engine.PAIR_DELTA_MAX
+                cfg = dict(launch or self._kernel_launch or tuned_launch(pix.n, tiles, pairs_ok))
+                if not pairs_ok:
+                    cfg["pairs"] = 0
+                elif cfg.get("pairs"):
+                    cfg["pair_short_radius_m"] = engine.pair_short_radius(tiles, pix, self.k)
                 res = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg,
                                        fresnel=int(fresnel), out=out, accumulate=accumulate,
                                        fresnel_radius=diag["fresnel_radius_m"])
                 self.last_run = dict(path="split_f32", n_tiles=tiles.n_tiles, fresnel=fresnel,
-                                     launch=dict(cfg), **diag)
+                                     launch=dict(cfg), pair_delta_rad=delta, **diag)
                 return res
             self.last_run = dict(path="plain_f64", declined="split-phase error budget", **diag)
         else:
@@ -383,8 +389,8 @@ class beam:
         return E
 
 
-def tuned_launch(n_pix, tiles):
+def tuned_launch(n_pix, tiles, pairs_ok=False):
     """Launch shape for the split kernel: the autotuner's cached winner, or
     the default when none is cached."""
     from . import autotune
-    return autotune.lookup(n_pix, tiles)
+    return autotune.lookup(n_pix, tiles, pairs_ok)

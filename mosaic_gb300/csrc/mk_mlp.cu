@@ -202,9 +202,12 @@ extern "C" int mk_bias_grad(int M, int N, const float *g, float *db, void *strea
     return MK_OK;
 }
 
-// Mean squared error over the n entries: grad = 2 (y - t) / n (float and
-// bf16), per-block partial sums of (y - t)^2 into part[blockIdx.x].
-__global__ void mk_mse_kernel(long long n, const float *__restrict__ y, const float *__restrict__ t,
+// Mean squared error over the n entries, each weighted by its column's
+// weight when col_w is given (row-major, n_col columns):
+// grad = 2 w (y - t) / n (float and bf16), per-block partial sums of
+// w (y - t)^2 into part[blockIdx.x].
+__global__ void mk_mse_kernel(long long n, int n_col, const float *__restrict__ y,
+                              const float *__restrict__ t, const float *__restrict__ col_w,
                               float *__restrict__ grad, __nv_bfloat16 *__restrict__ gb,
                               double *__restrict__ part)
 {
@@ -213,10 +216,11 @@ __global__ void mk_mse_kernel(long long n, const float *__restrict__ y, const fl
     double sq = 0.0;
     if (i < n) {
         const float d = y[i] - t[i];
-        const float gv = 2.f * d / (float)n;
+        const float w = col_w ? col_w[i % n_col] : 1.f;
+        const float gv = 2.f * w * d / (float)n;
         if (grad) grad[i] = gv;
         if (gb) gb[i] = __float2bfloat16(gv);
-        sq = (double)d * d;
+        sq = (double)w * d * d;
     }
     red[threadIdx.x] = sq;
     __syncthreads();
@@ -232,7 +236,19 @@ extern "C" int mk_mse(long long n, const float *y, const float *t, float *grad, 
 {
     MK_REQUIRE(n > 0 && y && t && partials, "mk_mse: bad arguments");
     mk_mse_kernel<<<(unsigned)((n + 255) / 256), 256, 0, mk_stream(stream)>>>(
-        n, y, t, grad, static_cast<__nv_bfloat16 *>(grad_bf16), partials);
+        n, 1, y, t, nullptr, grad, static_cast<__nv_bfloat16 *>(grad_bf16), partials);
+    MK_CHECK_CUDA(cudaGetLastError());
+    return MK_OK;
+}
+
+extern "C" int mk_mse_weighted(long long n, int n_col, const float *y, const float *t,
+                               const float *col_w, float *grad, void *grad_bf16,
+                               double *partials, void *stream)
+{
+    MK_REQUIRE(n > 0 && n_col > 0 && n % n_col == 0 && y && t && col_w && partials,
+               "mk_mse_weighted: bad arguments");
+    mk_mse_kernel<<<(unsigned)((n + 255) / 256), 256, 0, mk_stream(stream)>>>(
+        n, n_col, y, t, col_w, grad, static_cast<__nv_bfloat16 *>(grad_bf16), partials);
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
 }

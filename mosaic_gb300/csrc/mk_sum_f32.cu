@@ -76,6 +76,7 @@ struct MkSplitArgs {
     int apply_pol, decay, remove_forward;
     float pdeg;
     float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
+    float pair_short_r; // PAIR kernels: tiles up to this radius [m] use the short polynomial
 };
 
 #define TWO_PI_F 6.28318530717958647692f
@@ -167,7 +168,73 @@ __device__ __forceinline__ void mk_tile_terms(const float4 *__restrict__ P,
     }
 }
 
-template <int NT, int PIX, bool FRESNEL, bool CPLX>
+// Pixel pairs (a, b) that are neighbours on the detector: with
+// sigma = D.(w_a + w_b)/2 (cycles) and delta = pi D.(w_a - w_b) (radians),
+//   exp(2 pi i D.w_a) = exp(2 pi i sigma) exp(+i delta),
+//   exp(2 pi i D.w_b) = exp(2 pi i sigma) exp(-i delta).
+// sigma takes the MUFU sin/cos; delta is small (|delta| <= pi |D| |w_a - w_b|,
+// bounded by the host), so cos/sin(delta) are Taylor polynomials on the FMA
+// pipe, with the atom's (real) amplitude e folded into their coefficients:
+//   SHORT (|delta| <= MK_PAIR_SHORT_DELTA): e cos = e - (e/2) d^2,
+//         e sin = delta (e - (e/6) d^2); truncation below delta^4/24 = 1e-6;
+//   long  (|delta| <= 0.5): through d^6 and d^5; below delta^7/7! = 1.6e-6.
+// One MUFU sin/cos for two terms instead of two. Sums kept as
+// P = sum e e^{i sigma} cos(delta) and Q = i sum e e^{i sigma} sin(delta);
+// pixel a = P + Q, pixel b = P - Q.
+#define MK_PAIR_SHORT_DELTA 0.07f
+template <int NPAIR, bool FR, bool CPLX, bool SHORT>
+__device__ __forceinline__ void mk_tile_terms_pair(
+    const float4 *__restrict__ P, const float2 *__restrict__ E, int T, const float (&sx)[NPAIR],
+    const float (&sy)[NPAIR], const float (&sz)[NPAIR], const float (&dx)[NPAIR],
+    const float (&dy)[NPAIR], const float (&dz)[NPAIR], const float (&hq)[NPAIR], float bx,
+    float by, float bz, float (&pr)[NPAIR], float (&pi)[NPAIR], float (&qr)[NPAIR],
+    float (&qi)[NPAIR])
+{
+#pragma unroll 4
+    for (int j = 0; j < T; ++j) {
+        const float4 a = P[j];
+        const float2 e = E[j];
+        float db = 0.f;
+        if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
+        // per-atom polynomial coefficients (amplitude folded in when real)
+        const float e0 = CPLX ? 1.f : e.x;
+        const float c2 = -0.5f * e0, s2 = (-1.f / 6.f) * e0;
+        const float c4 = SHORT ? 0.f : (1.f / 24.f) * e0, s4 = SHORT ? 0.f : (1.f / 120.f) * e0;
+        const float c6 = SHORT ? 0.f : (-1.f / 720.f) * e0;
+#pragma unroll
+        for (int q = 0; q < NPAIR; ++q) {
+            float sig = fmaf(a.z, sz[q], fmaf(a.y, sy[q], a.x * sx[q]));
+            if (FR) {
+                const float sp = db - sig;
+                sig = fmaf(fmaf(-sp, sp, a.w), hq[q], sig);
+            }
+            const float del = fmaf(a.z, dz[q], fmaf(a.y, dy[q], a.x * dx[q]));
+            const float r = mk_frac_nearest(sig);
+            float sn, cs;
+            __sincosf(r * TWO_PI_F, &sn, &cs);
+            const float d2 = del * del;
+            float cd, sd;
+            if (SHORT) {
+                cd = fmaf(d2, c2, e0);
+                sd = del * fmaf(d2, s2, e0);
+            } else {
+                cd = fmaf(d2, fmaf(d2, fmaf(d2, c6, c4), c2), e0);
+                sd = del * fmaf(d2, fmaf(d2, s4, s2), e0);
+            }
+            float ec = cs, es = sn;
+            if (CPLX) {
+                ec = fmaf(e.x, cs, -e.y * sn);
+                es = fmaf(e.x, sn, e.y * cs);
+            }
+            pr[q] = fmaf(ec, cd, pr[q]);
+            pi[q] = fmaf(es, cd, pi[q]);
+            qr[q] = fmaf(-es, sd, qr[q]);
+            qi[q] = fmaf(ec, sd, qi[q]);
+        }
+    }
+}
+
+template <int NT, int PIX, bool FRESNEL, bool CPLX, bool PAIR>
 __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ MkSplitArgs A)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -219,7 +286,10 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
         float accr[PIX], acci[PIX], cmpr[PIX], cmpi[PIX];
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
-            pix[p] = pb * (NT * PIX) + p * NT + tid;
+            // PAIR: pixels 2j, 2j+1 of the thread are detector neighbours
+            // (consecutive indices; the host only pairs within rows)
+            pix[p] = PAIR ? pb * (NT * PIX) + 2 * ((p >> 1) * NT + tid) + (p & 1)
+                          : pb * (NT * PIX) + p * NT + tid;
             accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
         }
 
@@ -258,10 +328,54 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
             for (int p = 0; p < PIX; ++p) csr[p] = csi[p] = 0.f;
             // The |d|^2 term only for tiles wide enough to need it (uniform
             // across the block: no divergence).
-            if (FRESNEL && (float)o.w > A.fres_r)
-                mk_tile_terms<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
-            else
-                mk_tile_terms<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
+            const bool fr_tile = FRESNEL && (float)o.w > A.fres_r;
+            if constexpr (PAIR) {
+                constexpr int NP = PIX / 2;
+                float sx[NP], sy[NP], sz[NP], dx[NP], dy[NP], dz[NP], hp[NP];
+                float pr[NP], pi_[NP], qr[NP], qi[NP];
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                    const int a = 2 * q, b = 2 * q + 1;
+                    sx[q] = 0.5f * (wx[a] + wx[b]);
+                    sy[q] = 0.5f * (wy[a] + wy[b]);
+                    sz[q] = 0.5f * (wz[a] + wz[b]);
+                    dx[q] = 3.14159265358979f * (wx[a] - wx[b]);
+                    dy[q] = 3.14159265358979f * (wy[a] - wy[b]);
+                    dz[q] = 3.14159265358979f * (wz[a] - wz[b]);
+                    hp[q] = 0.5f * (hq[a] + hq[b]);
+                    pr[q] = pi_[q] = qr[q] = qi[q] = 0.f;
+                }
+                // the short delta polynomial for tiles small enough (uniform
+                // across the block, like fr_tile)
+                const bool short_tile = (float)o.w <= A.pair_short_r;
+                if (fr_tile) {
+                    if (short_tile)
+                        mk_tile_terms_pair<NP, true, CPLX, true>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
+                                                                 F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                    else
+                        mk_tile_terms_pair<NP, true, CPLX, false>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
+                                                                  F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                } else {
+                    if (short_tile)
+                        mk_tile_terms_pair<NP, false, CPLX, true>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
+                                                                  F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                    else
+                        mk_tile_terms_pair<NP, false, CPLX, false>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
+                                                                   F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                }
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                    csr[2 * q] = pr[q] + qr[q];
+                    csi[2 * q] = pi_[q] + qi[q];
+                    csr[2 * q + 1] = pr[q] - qr[q];
+                    csi[2 * q + 1] = pi_[q] - qi[q];
+                }
+            } else {
+                if (fr_tile)
+                    mk_tile_terms<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
+                else
+                    mk_tile_terms<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
+            }
             __syncthreads();   // every thread is done with buffer `buf`
             if (tid == 0 && t + 2 < t_hi) {
                 mk_fence_proxy_async();
@@ -415,21 +529,33 @@ int mk_launch_reduce(const double2 *partial, int slices, int n_pix, const double
 // ----------------------------------------------------------------- launch
 typedef void (*mk_split_fn)(const MkSplitArgs);
 
-template <int NT, int PIX>
-static mk_split_fn mk_pick3(bool fresnel, bool cplx)
+template <int NT, int PIX, bool PAIR>
+static mk_split_fn mk_pick4(bool fresnel, bool cplx)
 {
-    if (fresnel) return cplx ? mk_split_kernel<NT, PIX, true, true> : mk_split_kernel<NT, PIX, true, false>;
-    return cplx ? mk_split_kernel<NT, PIX, false, true> : mk_split_kernel<NT, PIX, false, false>;
+    if (fresnel)
+        return cplx ? mk_split_kernel<NT, PIX, true, true, PAIR> : mk_split_kernel<NT, PIX, true, false, PAIR>;
+    return cplx ? mk_split_kernel<NT, PIX, false, true, PAIR> : mk_split_kernel<NT, PIX, false, false, PAIR>;
 }
 
-static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx)
+template <int NT, int PIX>
+static mk_split_fn mk_pick3(bool fresnel, bool cplx, bool pair)
+{
+    if constexpr (PIX % 2 == 0) {
+        if (pair) return mk_pick4<NT, PIX, true>(fresnel, cplx);
+    } else {
+        if (pair) return nullptr;
+    }
+    return mk_pick4<NT, PIX, false>(fresnel, cplx);
+}
+
+static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, bool pair)
 {
 #define MK_PIX_CASES(NT_)                                                  \
     switch (pix) {                                                         \
-    case 1: return mk_pick3<NT_, 1>(fresnel, cplx);                        \
-    case 2: return mk_pick3<NT_, 2>(fresnel, cplx);                        \
-    case 4: return mk_pick3<NT_, 4>(fresnel, cplx);                        \
-    case 8: return mk_pick3<NT_, 8>(fresnel, cplx);                        \
+    case 1: return mk_pick3<NT_, 1>(fresnel, cplx, pair);                  \
+    case 2: return mk_pick3<NT_, 2>(fresnel, cplx, pair);                  \
+    case 4: return mk_pick3<NT_, 4>(fresnel, cplx, pair);                  \
+    case 8: return mk_pick3<NT_, 8>(fresnel, cplx, pair);                  \
     default: return nullptr;                                               \
     }
     switch (nt) {
@@ -451,7 +577,7 @@ struct MkLaunchShape {
 static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShape *out)
 {
     mk_split_fn fn = mk_pick(launch->threads, launch->pix_per_thread, launch->fresnel != 0,
-                             launch->amp_real == 0);
+                             launch->amp_real == 0, launch->pairs != 0);
     MK_REQUIRE(fn, "split kernel: unsupported launch shape threads=%d pix=%d", launch->threads,
                launch->pix_per_thread);
     const size_t smem = mk_split_smem(tile_atoms);
@@ -582,6 +708,7 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
     A.remove_forward = phys->remove_forward;
     A.pdeg = (float)phys->pol_deg;
     A.fres_r = launch->fresnel_radius_m > 0.0 ? (float)launch->fresnel_radius_m : 0.f;
+    A.pair_short_r = launch->pair_short_radius_m > 0.0 ? (float)launch->pair_short_radius_m : -1.f;
     MK_CHECK_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned long long), st));
     const long long grid = std::min<long long>(n_items, sh.resident);
     sh.fn<<<(unsigned)grid, launch->threads, mk_split_smem(T), st>>>(A);

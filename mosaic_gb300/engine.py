@@ -113,10 +113,12 @@ class Pixels:
         self.abi = MkPixels(self.ny, self.nz, self.xyz.data_ptr(), self.r0.data_ptr(),
                             self.q.data_ptr(), self.u.data_ptr(), self.phasor.data_ptr())
         sh = _stream_handle(stream)
+        self.spans = [(0, P)]
         if frames is None:
             check(L.mk_pixels_prepare(ctypes.byref(self.abi), ctypes.byref(phys), sh))
             return
         off = 0
+        self.spans = []
         for fny, fnz, bdir in frames:
             m = int(fny) * int(fnz)
             sub = MkPixels(int(fny), int(fnz), self.xyz[off:].data_ptr(), self.r0[off:].data_ptr(),
@@ -125,12 +127,29 @@ class Pixels:
             ph = MkPhysics.from_buffer_copy(phys)
             ph.beam_dir[:] = [float(v) for v in bdir]
             check(L.mk_pixels_prepare(ctypes.byref(sub), ctypes.byref(ph), sh))
+            self.spans.append((off, m))
             off += m
         if off != P:
             raise ValueError(f"frames cover {off} pixels, xyz has {P}")
 
     def r0_min(self):
         return float(self.r0.min())
+
+    def pair_step(self):
+        """Largest |u_2j - u_2j+1| over the pixel pairs (2j, 2j+1) of every
+        frame, u the unit vector to the pixel: the pairs mode shares one
+        sin/cos between the two pixels of a pair."""
+        u = self.u[:, :3].double()
+        if all(off % 2 == 0 for off, _ in self.spans):
+            h = self.n // 2
+            return float(torch.linalg.vector_norm(u[0:2 * h:2] - u[1:2 * h:2], dim=1).max()) if h else 0.0
+        worst = 0.0
+        for off, m in self.spans:
+            h = m // 2
+            if h:
+                d = u[off:off + 2 * h:2] - u[off + 1:off + 2 * h:2]
+                worst = max(worst, float(torch.linalg.vector_norm(d, dim=1).max()))
+        return worst
 
 
 @dataclass
@@ -221,19 +240,57 @@ class Tiles:
         return bool((self.amp[:, 1] == 0).all()) if self.n_tiles else True
 
 
-DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0)
+DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
+PAIR_DELTA_MAX = 0.5     # rad: the long pair polynomials are then exact to ~2e-6 per term
+PAIR_SHORT_DELTA = 0.07  # rad: the short ones to 1e-6 (the kernel's MK_PAIR_SHORT_DELTA)
+
+
+def _pair_rate(tiles, pix: Pixels, k):
+    """Half phase difference of a pixel pair per metre of tile radius [rad/m]:
+    (k/2) |u_a - u_b|, widened for the tile-origin term of w."""
+    grow = 1.0 + 2.0 * tiles.max_origin_norm() / max(pix.r0_min(), 1e-300)
+    return 0.5 * float(k) * pix.pair_step() * grow * 1.05
+
+
+def pair_delta(tiles, pix: Pixels, k):
+    """Bound on the half phase difference pi |D| |w_a - w_b| of a pixel pair
+    over all tiles [rad]."""
+    if not tiles.n_tiles:
+        return 0.0
+    return _pair_rate(tiles, pix, k) * tiles.max_radius()
+
+
+def pair_short_radius(tiles, pix: Pixels, k):
+    """Largest tile radius [m] whose pairs stay within PAIR_SHORT_DELTA."""
+    if not tiles.n_tiles:
+        return 0.0
+    rate = _pair_rate(tiles, pix, k)
+    return PAIR_SHORT_DELTA / rate if rate > 0 else 1.0
+
+
+def pairs_allowed(tiles, pix: Pixels, k):
+    return pair_delta(tiles, pix, k) <= PAIR_DELTA_MAX
 
 
 def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None, fresnel=-1,
               amp_real=None, out=None, accumulate=False, stream=None, fresnel_radius=0.0):
     """FP32 split-phase sum; returns float64 (P, 2) (a view of `out` if given).
     With ``fresnel`` set, only tiles wider than ``fresnel_radius`` [m] keep the
-    |d|^2 term (0: all tiles)."""
+    |d|^2 term (0: all tiles). ``launch["pairs"]`` = 1 shares one sin/cos
+    between pixels 2j and 2j+1; only legal where ``pairs_allowed`` holds;
+    ``launch["pair_short_radius_m"]`` (``pair_short_radius``) then selects
+    the short delta polynomial for the tiles up to that radius."""
     L = _require_cuda()
     cfg = dict(DEFAULT_LAUNCH, **(launch or {}))
+    pairs = bool(cfg.get("pairs", 0))
+    short_r = 0.0
+    if pairs:
+        short_r = cfg.get("pair_short_radius_m")
+        if short_r is None:
+            short_r = pair_short_radius(tiles, pix, phys.k)
     ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
                   int(tiles.amp_is_real() if amp_real is None else bool(amp_real)),
-                  float(fresnel_radius))
+                  float(fresnel_radius), int(pairs), short_r)
     wsb = ctypes.c_size_t(0)
     check(L.mk_split_plan(ctypes.byref(tiles.abi), ctypes.byref(pix.abi), ctypes.byref(ln),
                           ctypes.byref(wsb)))
@@ -290,3 +347,11 @@ class TilesView:
 
     def amp_is_real(self):
         return bool((self.amp[: self.n_tiles * self.tile_atoms, 1] == 0).all())
+
+    def max_radius(self):
+        return float(self.origin[: self.n_tiles, 3].max()) if self.n_tiles else 0.0
+
+    def max_origin_norm(self):
+        if not self.n_tiles:
+            return 0.0
+        return float(torch.linalg.vector_norm(self.origin[: self.n_tiles, :3], dim=1).max())

@@ -114,10 +114,19 @@ class BatchedScan:
                                     f"scan geometry outside the split-phase error budget "
                                     f"({third:.2e} rad > {tol:.0e})")
         self.diag = diag
-        cfg = dict(engine.DEFAULT_LAUNCH, **(launch or beam._kernel_launch or {}))
+        delta = engine.pair_delta(self.tiles, self.pix, beam.k)
+        self.diag["pair_delta_rad"] = delta
+        pairs_ok = delta <= engine.PAIR_DELTA_MAX
+        cfg = dict(engine.DEFAULT_LAUNCH, pairs=int(pairs_ok))
+        cfg.update(launch or beam._kernel_launch or {})
+        if not pairs_ok:
+            cfg["pairs"] = 0
+        short_r = engine.pair_short_radius(self.tiles, self.pix, beam.k) if cfg["pairs"] else 0.0
+        cfg["pair_short_radius_m"] = short_r
+        self.cfg = cfg
         self.launch = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]),
                                int(fresnel), int(self.tiles.amp_is_real()),
-                               float(diag["fresnel_radius_m"]))
+                               float(diag["fresnel_radius_m"]), int(bool(cfg["pairs"])), short_r)
         nf = len(self.frames)
         desc = (MkFrameDesc * nf)()
         n_items, n_part = ctypes.c_longlong(0), ctypes.c_longlong(0)

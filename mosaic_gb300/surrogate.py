@@ -2,17 +2,25 @@
 
 For a 2-D motor scan (theta x chi) the exact kinematic sum is computed on a
 sub-grid of training frames (every ``stride``-th point along each axis) in
-one batched launch; an MLP maps the two motor coordinates (with Fourier
-features) to the log-intensity of every ROI pixel and predicts the other
-frames. Every ``judge_every``-th predicted frame is recomputed exactly; if its
-relative error max|I_pred - I| / max I exceeds ``tol`` it falls back to the
-exact sum, together with the predicted frames it stands for.
+batched launches. Each frame is split into its peak M = max I and its
+normalised intensity I / M; the normalised training frames are expanded in
+their principal components (``FrameBasis``), and an MLP maps the two motor
+coordinates (with Fourier features) to the standardised component
+coefficients and log M. The loss weights each coefficient by its variance, so
+that it measures the error of the frame in intensity relative to its peak --
+the quantity the judge thresholds -- rather than in log intensity, which
+gives the dim pixels most of the weight. Every ``judge_every``-th predicted
+frame is recomputed exactly; if its relative error max|I_pred - I| / max I
+exceeds ``tol`` it falls back to the exact sum, together with the predicted
+frames it stands for.
 
 The network trains and predicts on the GPU with the library's own kernels
 (``mk_gemm_bf16``: BF16 operands, FP32 accumulation on the tensor cores;
-``mk_adam`` on FP32 master weights; ``mk_fourier_features``, ``mk_mse``,
-``mk_relu_backward``, ``mk_bias_grad``). No counterpart in the reference: the
-reference runs one full exposure per scan step (Experiment.py:285-336).
+``mk_adam`` on FP32 master weights; ``mk_fourier_features``,
+``mk_mse_weighted``, ``mk_relu_backward``, ``mk_bias_grad``); the frames are
+decoded from the coefficients on ``mk_gemm_bf16`` too. No counterpart in the
+reference: the reference runs one full exposure per scan step
+(Experiment.py:285-336).
 """
 from __future__ import annotations
 
@@ -103,13 +111,18 @@ class MLP:
                                           engine._stream_handle()))
         return dW, db
 
-    def mse(self, Y, T):
-        """(loss as a device scalar, dL/dY f32, bf16)."""
+    def mse(self, Y, T, col_w=None):
+        """(loss as a device scalar, dL/dY f32, bf16); ``col_w`` weights the
+        output columns (float32 device vector)."""
         n = Y.numel()
         G = torch.empty_like(Y)
         Gb = torch.empty(Y.shape, dtype=torch.bfloat16, device=self.dev)
         part = torch.empty((n + 255) // 256, dtype=torch.float64, device=self.dev)
-        check(self.L.mk_mse(n, _p(Y), _p(T), _p(G), _p(Gb), _p(part), engine._stream_handle()))
+        if col_w is None:
+            check(self.L.mk_mse(n, _p(Y), _p(T), _p(G), _p(Gb), _p(part), engine._stream_handle()))
+        else:
+            check(self.L.mk_mse_weighted(n, int(Y.shape[1]), _p(Y), _p(T), _p(col_w), _p(G),
+                                         _p(Gb), _p(part), engine._stream_handle()))
         return part.sum() / n, G, Gb
 
     def adam(self, dW, db, lr, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
@@ -122,8 +135,9 @@ class MLP:
             check(self.L.mk_adam(self.b[l].numel(), _p(self.b[l]), _p(db[l]), _p(self.mb[l]),
                                  _p(self.vb[l]), None, lr, beta1, beta2, eps, self.steps, 0.0, sh))
 
-    def fit(self, X, T, steps=1500, lr=2e-3, lr_final=1e-4, batch=None, seed=0):
-        """Adam on mean squared error; cosine learning-rate decay. Returns the loss history."""
+    def fit(self, X, T, steps=1500, lr=2e-3, lr_final=1e-4, batch=None, seed=0, col_w=None):
+        """Adam on (column-weighted) mean squared error; cosine learning-rate
+        decay. Returns the loss history."""
         gen = torch.Generator(device=self.dev)
         gen.manual_seed(seed)
         n = int(X.shape[0])
@@ -136,7 +150,7 @@ class MLP:
             else:
                 Xb, Tb = X, T
             acts, posts, Y = self.forward(Xb)
-            loss, G, Gb = self.mse(Y, Tb)
+            loss, G, Gb = self.mse(Y, Tb, col_w)
             dW, db = self.backward(acts, posts, G, Gb)
             self.adam(dW, db, float(a))
             losses.append(loss)
@@ -149,12 +163,13 @@ class MLP:
         return torch.cat(outs)
 
 
-def fourier_features(xy, n_freq=16, device="cuda", f_max=4.0, f_min=0.25):
+def fourier_features(xy, n_freq=16, device="cuda", f_max=0.5, f_min=0.25):
     """(n, 2) coordinates in [-1, 1] -> (n, width) bf16 network inputs with
     ``n_freq`` frequencies geometrically spaced from f_min to f_max cycles per
-    unit. f_max must stay below the Nyquist limit of the training grid
-    (n_train_per_axis / 4 cycles per unit): higher features only alias
-    between training frames."""
+    unit. Scan frames change smoothly with the motors: a low band keeps the
+    network's interpolation between training frames smooth (measured on the
+    4M-atom rocking scans: f_max = 0.5 generalises, a band reaching the
+    training grid's Nyquist limit only aliases between training frames)."""
     L = engine._require_cuda()
     xy = torch.as_tensor(np.ascontiguousarray(xy, dtype=np.float32)).to(device)
     width = 2 + 4 * int(n_freq)
@@ -172,6 +187,47 @@ def frame_rel_error(I_pred, I_exact):
     return num / I_exact.amax(dim=1).clamp_min(1e-300)
 
 
+def _split_bf16(x):
+    """x = hi + lo with both halves bf16 (16 mantissa bits together)."""
+    hi = x.to(torch.bfloat16)
+    lo = (x - hi.float()).to(torch.bfloat16)
+    return hi.contiguous(), lo.contiguous()
+
+
+class FrameBasis:
+    """Principal components of the training frames' normalised intensity
+    X = I / max I: the mean frame and ``rank`` orthonormal rows V (rank, P),
+    with the training frames' coefficients C = (X - mean) V^T. Built from the
+    Gram matrix of the centred frames (one FP32 product on the device; its
+    n x n eigendecomposition on the host in FP64)."""
+
+    def __init__(self, X, rank):
+        n = int(X.shape[0])
+        self.mu = X.mean(0).contiguous()
+        Xc = X - self.mu
+        lam, U = np.linalg.eigh((Xc @ Xc.T).double().cpu().numpy())
+        order = np.argsort(lam)[::-1][: min(int(rank), n)]
+        lam = np.clip(lam[order], 1e-30, None)
+        U = U[:, order]
+        dev = X.device
+        self.V = (torch.tensor(U / np.sqrt(lam), dtype=torch.float32, device=dev).T @ Xc).contiguous()
+        self.C = torch.tensor(U * np.sqrt(lam), dtype=torch.float32, device=dev)
+        self.rank = len(order)
+        self.V_hi, self.V_lo = _split_bf16(self.V)
+
+    def decode(self, net, coef):
+        """(m, rank) coefficients -> (m, P) frames coef V + mean, on the
+        library's BF16 GEMM with hi/lo operand splitting (three products,
+        FP32 accumulation: ~1e-5 relative)."""
+        m, P, r = int(coef.shape[0]), int(self.V.shape[1]), self.rank
+        ch, cl = _split_bf16(coef)
+        out = torch.empty((m, P), dtype=torch.float32, device=coef.device)
+        net._gemm(m, P, r, ch, r, 1, self.V_hi, P, 1, out, P, self.mu, GEMM_BIAS, None, 0)
+        net._gemm(m, P, r, ch, r, 1, self.V_lo, P, 1, out, P, None, GEMM_ACC, None, 0)
+        net._gemm(m, P, r, cl, r, 1, self.V_hi, P, 1, out, P, None, GEMM_ACC, None, 0)
+        return out
+
+
 class SurrogateScan:
     """Surrogate-assisted theta x chi scan (see the module docstring).
 
@@ -182,11 +238,15 @@ class SurrogateScan:
         stride: training frames every ``stride`` points along each axis
             (``raster=True``: every ``stride``-th frame in raster order).
         judge_every, tol: exact re-judging cadence and fallback threshold.
+        rank: principal components of the normalised frames the network
+            predicts; scale_weight: loss weight of the log peak output
+            against the (variance-weighted) components.
     """
 
     def __init__(self, beam, sample, detector, stage, theta, chi, roi=128, stride=4, raster=False,
-                 judge_every=8, tol=0.02, hidden=256, n_hidden=4, n_freq=16, fit_steps=1500,
-                 lr=2e-3, seed=0, sc_kwargs=None, device="cuda"):
+                 judge_every=8, tol=0.02, hidden=256, n_hidden=4, n_freq=16, fit_steps=2000,
+                 lr=3e-3, seed=0, sc_kwargs=None, device="cuda", rank=32, f_max=0.5, f_min=0.25,
+                 scale_weight=10.0, batch_frames=2048):
         self.beam, self.sample, self.detector, self.stage = beam, sample, detector, stage
         self.theta = np.asarray(theta, dtype=np.float64)
         self.chi = np.asarray(chi, dtype=np.float64)
@@ -194,6 +254,8 @@ class SurrogateScan:
         self.judge_every, self.tol = int(judge_every), float(tol)
         self.hidden, self.n_hidden, self.n_freq = hidden, n_hidden, n_freq
         self.fit_steps, self.lr, self.seed = fit_steps, lr, seed
+        self.rank, self.f_max, self.f_min = int(rank), float(f_max), float(f_min)
+        self.scale_weight, self.batch_frames = float(scale_weight), int(batch_frames)
         self.kw = dict(apply_polarization=False, spherical_decay=False, remove_forward=False)
         self.kw.update(sc_kwargs or {})
         self.dev = torch.device(device)
@@ -211,51 +273,75 @@ class SurrogateScan:
         self.steps = [dict(mu=mu0 + self.theta[i], chi=chi0 + self.chi[j]) for i, j in self.ij]
         self._staged = None
 
+    def stage(self):
+        """Stage the atoms and tiles once (setup shared by every exact call,
+        and by an exact-only scan alike)."""
+        if self._staged is None:
+            self.exact(np.zeros(1, np.int64))
+
     def exact(self, idx):
-        """Exact intensities (len(idx), roi*roi) of the given frames, one batched launch."""
+        """Exact intensities (len(idx), roi*roi) of the given frames, batched
+        launches of at most ``batch_frames`` frames."""
         idx = np.asarray(idx)
         if idx.size == 0:
             return torch.zeros((0, self.roi * self.roi), dtype=torch.float32, device=self.dev)
-        frames = frames_from_motors(self.stage, self.detector, [self.steps[i] for i in idx],
-                                    [self.roi] * len(idx))
-        if len(frames) == 1:               # a one-frame batch still goes through the scan path
-            frames = frames * 2
-        scan = BatchedScan(self.beam, self.sample, frames, staged=self._staged, **self.kw)
-        self._staged = self._staged or scan
-        out, _ = scan.run()
-        I = (out * out).sum(1).reshape(len(frames), -1)[: len(idx)].float()
-        return I
+        outs = []
+        for b in range(0, idx.size, self.batch_frames):
+            sub = idx[b: b + self.batch_frames]
+            frames = frames_from_motors(self.stage, self.detector, [self.steps[i] for i in sub],
+                                        [self.roi] * len(sub))
+            if len(frames) == 1:           # a one-frame batch still goes through the scan path
+                frames = frames * 2
+            scan = BatchedScan(self.beam, self.sample, frames, staged=self._staged, **self.kw)
+            self._staged = self._staged or scan
+            out, _ = scan.run()
+            outs.append((out * out).sum(1).reshape(len(frames), -1)[: len(sub)].float())
+        return torch.cat(outs)
 
-    def run(self, verify=0):
-        """Run the scan; ``verify`` > 0 also computes exact frames for that many
-        unjudged predicted frames (not timed) to measure the true error."""
+    def run(self, verify=0, exact_all=False):
+        """Run the scan. ``exact_all`` also computes every frame exactly (the
+        exact-only scan, timed) and the true error of every predicted frame;
+        otherwise the exact-only time is the training batch's per-frame time
+        times the frame count, and ``verify`` > 0 computes that many unjudged
+        predicted frames exactly (untimed) to measure their true error."""
         sync = torch.cuda.synchronize
         n = len(self.ij)
         t = {}
         sync()
         t0 = time.perf_counter()
+        self.stage()
+        sync()
+        setup_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
         tr = np.flatnonzero(self.train)
+        if tr.size < 2:
+            raise ValueError("the surrogate needs at least two training frames")
         I_train = self.exact(tr)
         sync()
         t["exact_train"] = time.perf_counter() - t0
-        # targets: per-pixel standardised log intensity
-        eps = 1e-6 * float(I_train.max())
-        logI = torch.log(I_train + eps)
-        mu, sd = logI.mean(0, keepdim=True), logI.std(0, keepdim=True).clamp_min(1e-3)
-        T = ((logI - mu) / sd).contiguous()
-        # highest feature frequency: half the Nyquist limit of the training grid
-        n_axis = min(len(np.unique(self.ij[tr, 0])), len(np.unique(self.ij[tr, 1])))
-        feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=max(0.5, n_axis / 8.0))
+        # targets: principal-component coefficients of the normalised frames
+        # (standardised) and the log of each frame's peak
         t0 = time.perf_counter()
-        self.net = MLP(feats.shape[1], T.shape[1], self.hidden, self.n_hidden, self.seed, self.dev)
+        M = I_train.amax(1, keepdim=True).clamp_min(1e-300)
+        basis = FrameBasis(I_train / M, self.rank)
+        cs = basis.C.std(0, keepdim=True).clamp_min(1e-12)
+        lm = torch.log(M)
+        lmu, lsd = lm.mean(), lm.std().clamp_min(1e-6)
+        T = torch.cat([basis.C / cs, (lm - lmu) / lsd], 1).contiguous()
+        w = cs[0] ** 2
+        col_w = torch.cat([w / w.sum() * basis.rank,
+                           torch.tensor([self.scale_weight], device=self.dev)]).float().contiguous()
+        feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=self.f_max, f_min=self.f_min)
+        self.net = MLP(feats.shape[1], basis.rank + 1, self.hidden, self.n_hidden, self.seed, self.dev)
         self.losses = self.net.fit(feats[torch.as_tensor(tr, device=self.dev)], T,
-                                   steps=self.fit_steps, lr=self.lr)
+                                   steps=self.fit_steps, lr=self.lr, col_w=col_w)
         sync()
         t["fit"] = time.perf_counter() - t0
         t0 = time.perf_counter()
         pred_idx = np.flatnonzero(~self.train)
         Yp = self.net.predict(feats[torch.as_tensor(pred_idx, device=self.dev)])
-        I_pred = (torch.exp(Yp * sd + mu) - eps).clamp_min(0.0)
+        shape = basis.decode(self.net, (Yp[:, : basis.rank] * cs).contiguous())
+        I_pred = shape.clamp_min_(0.0) * torch.exp(Yp[:, basis.rank:] * lsd + lmu)
         sync()
         t["predict"] = time.perf_counter() - t0
         # judge every judge_every-th predicted frame; a failed judge sends its
@@ -268,6 +354,7 @@ class SurrogateScan:
         err_j = frame_rel_error(I_pred[judged], I_j).cpu().numpy()
         sync()
         t["judge"] = time.perf_counter() - t0
+        I_model = I_pred.clone() if exact_all else None
         I_pred[torch.as_tensor(judged, device=self.dev)] = I_j
         failed = [blk for blk, e in zip(blocks, err_j) if e > self.tol]
         fb = np.concatenate([blk[1:] for blk in failed]) if failed else np.zeros(0, np.int64)
@@ -281,14 +368,26 @@ class SurrogateScan:
         frames[torch.as_tensor(pred_idx, device=self.dev)] = I_pred
         exact_frames = len(tr) + len(judged) + int(fb.size)
         total = sum(t.values())
-        per_exact = t["exact_train"] / max(len(tr), 1)
         res = dict(frames=frames, n_frames=n, n_train=len(tr), n_judged=len(judged),
                    n_fallback=int(fb.size), n_failed_judges=len(failed), exact_frames=exact_frames,
-                   judge_err=err_j, times=t, seconds=total, frames_per_s=n / total,
-                   exact_frames_per_s=1.0 / per_exact, exact_scan_seconds_est=n * per_exact,
-                   gain=(n * per_exact) / total, final_loss=float(self.losses[-1]),
-                   params=self.net.n_params)
-        if verify:
+                   judge_err=err_j, times=t, setup_seconds=setup_s, seconds=total,
+                   frames_per_s=n / total, final_loss=float(self.losses[-1]),
+                   params=self.net.n_params, rank=basis.rank)
+        if exact_all:
+            sync()
+            t0 = time.perf_counter()
+            I_all = self.exact(np.arange(n))
+            sync()
+            ex_s = time.perf_counter() - t0
+            res.update(exact_seconds=ex_s, exact_measured=True)
+            res["model_err"] = frame_rel_error(I_model, I_all[torch.as_tensor(pred_idx, device=self.dev)]
+                                               ).cpu().numpy()
+            res["final_err"] = frame_rel_error(frames, I_all).cpu().numpy()
+        else:
+            res.update(exact_seconds=n * t["exact_train"] / len(tr), exact_measured=False)
+        res["exact_frames_per_s"] = n / res["exact_seconds"]
+        res["gain"] = res["exact_seconds"] / total
+        if verify and not exact_all:
             rng = np.random.default_rng(self.seed + 1)
             unjudged = np.setdiff1d(np.arange(len(pred_idx)), np.concatenate([judged, fb]))
             pick = rng.choice(unjudged, size=min(int(verify), unjudged.size), replace=False) \

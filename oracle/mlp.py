@@ -35,11 +35,13 @@ def forward(H0, Ws, bs):
     return H, posts, Y.astype(np.float32).astype(np.float64)
 
 
-def backward(H, posts, Y, T, Ws):
-    """Gradients of mean((Y - T)^2) w.r.t. every W and b, with the GPU's
-    rounding points: bf16 gradient operands, float bias sums."""
+def backward(H, posts, Y, T, Ws, col_w=None):
+    """Gradients of mean(w (Y - T)^2) (w per output column, 1 without
+    ``col_w``) w.r.t. every W and b, with the GPU's rounding points: bf16
+    gradient operands, float bias sums."""
     n = Y.size
-    g = (2.0 * (Y - T) / n).astype(np.float32).astype(np.float64)
+    w = np.ones(Y.shape[1]) if col_w is None else np.asarray(col_w, np.float64)
+    g = (2.0 * w * (Y - T) / n).astype(np.float32).astype(np.float64)
     dWs, dbs = [None] * len(Ws), [None] * len(Ws)
     for l in range(len(Ws) - 1, -1, -1):
         gb = bf16(g)
@@ -49,5 +51,5 @@ def backward(H, posts, Y, T, Ws):
             break
         dH = (gb @ np.asarray(Ws[l], np.float64)).astype(np.float32).astype(np.float64)
         g = np.where(posts[l - 1] > 0.0, dH, 0.0)
-    loss = float(np.mean((Y - T) ** 2))
+    loss = float(np.mean(w * (Y - T) ** 2))
     return dWs, dbs, loss

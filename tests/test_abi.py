@@ -51,3 +51,32 @@ def test_version_and_host_side_validation():
         _lib.check(_lib.MK_ENOMEM)
     with pytest.raises(_lib.DeclineError):
         _lib.check(_lib.MK_EDECLINE)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the C structs have the header's size and field
+    offsets (compiled with the host C compiler)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    structs = {"mk_species": _lib.MkSpecies, "mk_physics": _lib.MkPhysics,
+               "mk_pixels": _lib.MkPixels, "mk_frame_desc": _lib.MkFrameDesc,
+               "mk_tiles": _lib.MkTiles, "mk_launch": _lib.MkLaunch}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mosaic_kin.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

@@ -75,6 +75,75 @@ def test_split_f32_matches_oracle(cuda, golden, tile_atoms):
         assert rel_max(got, ref) <= 1e-4, (i, rel_max(got, ref))
 
 
+@pytest.mark.parametrize("pix_pt", [2, 4, 8])
+def test_split_pairs_match_oracle(cuda, golden, pix_pt):
+    """Pixel-pair form (one sin/cos for two neighbouring pixels) on the
+    reference's kernel cases, wherever the pair bound admits it."""
+    d = golden("kernel_cases.npz")
+    used = 0
+    for i in range(int(d["n"])):
+        c = _kernel_case(d, i)
+        table, idx = table_from_rows(c["wk"], c["f0z"], c["anom"])
+        atoms = atoms_from_arrays(c["pos"], idx, c["amp"], table, cuda)
+        phys = engine.physics(c["k"], (1, 0, 0), c["ap"], c["pol"], c["dc"], c["rf"])
+        pix = engine.Pixels(c["cxyz"], c["ny"], c["nz"], phys, device=cuda)
+        tiles = engine.Tiles(atoms, c["k"], 128, device=cuda)
+        if not engine.pairs_allowed(tiles, pix, c["k"]):
+            continue
+        used += 1
+        base = dict(pix_per_thread=pix_pt, threads=128, slices=0)
+        got = field(engine.run_split(tiles, pix, phys, table, fresnel=1, launch=dict(base, pairs=1)))
+        one = field(engine.run_split(tiles, pix, phys, table, fresnel=1, launch=base))
+        ref = _oracle_case(c)
+        assert rel_intensity(got, ref) <= 1e-4, (i, rel_intensity(got, ref))
+        assert rel_max(got, ref) <= 1e-4, (i, rel_max(got, ref))
+        assert rel_max(got, one) <= 2e-5, (i, rel_max(got, one))
+    assert used >= 1
+
+
+@pytest.mark.parametrize("shape", [(24, 20), (13, 11), (25, 1)])
+def test_split_pairs_near_the_bound(cuda, shape):
+    """A (111)-oriented fcc Cu/Ni crystal seen by a detector whose pitch puts
+    the pair half-phase at about 0.35 rad (0.5 is the limit), odd pixel counts
+    and odd rows included (the pair then spans a row end, or the last pixel
+    pairs with itself): pair form against the oracle and against one sin/cos
+    per term."""
+    rng = np.random.default_rng(3)
+    w = workloads.fcc_cu_32k(cells=8, npix=20)
+    pos = w.sample.load_chunk_positions(1)
+    spc = rng.choice(np.array(["Cu", "Ni"]), size=pos.shape[0])
+    sample = ChunkedSample([(pos, spc)])
+    B = workloads._beam(10000.0, 200.0, pol_perp_rate=1.0)
+    B._kernel_tile_atoms = 256
+    stage = StaticStage(w.stage.rotation, w.stage.translation)
+
+    def det(pitch):
+        D = Detector()
+        D.create_detector(shape, (pitch, pitch))
+        D.position_detector_absolute(2.0e9, 2.0 * w.meta["theta_deg"], 0.0)
+        return D
+
+    kw = dict(apply_polarization=True, spherical_decay=True, remove_forward=False, return_double=True)
+    B._kernel_launch = dict(pix_per_thread=4, threads=128, slices=0, pairs=1)
+    B.atomic_scattering_kinematic(sample, det(5.5e5), stage, **kw)
+    d0 = B.last_run["pair_delta_rad"]
+    pitch = 5.5e5 * 0.35 / d0
+    D = det(pitch)
+    got = B.atomic_scattering_kinematic(sample, D, stage, **kw)
+    run = dict(B.last_run)
+    assert run["path"] == "split_f32" and run["launch"]["pairs"] == 1, run
+    assert 0.2 < run["pair_delta_rad"] <= engine.PAIR_DELTA_MAX, run["pair_delta_rad"]
+    B._kernel_launch = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
+    one = B.atomic_scattering_kinematic(sample, D, stage, **kw)
+    ref = oracle.interact_cpu([(pos, spc)], D.pixel_coordinates, D.shape, stage.rotation,
+                              stage.translation, B._energy, B.tables.f0,
+                              {e: B.tables.f0_zero(e) for e in ("Cu", "Ni")}, B.tables.f1f2,
+                              B._beam_E0_map, B._beam_grid(), B._polarization_state(),
+                              apply_polarization=True, spherical_decay=True)
+    assert rel_intensity(got, ref) <= 1e-4, rel_intensity(got, ref)
+    assert rel_max(got, one) <= 2e-5, rel_max(got, one)
+
+
 def _golden_beam(e):
     B = Beam()
     B.create_beam(float(e["energy"]), beam_size=(70.0, 60.0), beam_samples=(64, 48),

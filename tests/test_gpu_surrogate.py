@@ -44,18 +44,20 @@ def test_gemm_layouts_match_fp32_reference(cuda, M, N, K):
     assert torch.allclose(E.cpu().double(), G.double().T @ A.double(), rtol=1e-5, atol=1e-3)
 
 
-def test_mlp_gradients_match_oracle(cuda):
+@pytest.mark.parametrize("weighted", [False, True])
+def test_mlp_gradients_match_oracle(cuda, weighted):
     rng = np.random.default_rng(1)
     net = MLP(24, 96, hidden=64, n_hidden=3, seed=2, device=cuda)
     X = torch.tensor(omlp.bf16(rng.standard_normal((50, 24))), dtype=torch.bfloat16, device=cuda)
     T = torch.tensor(rng.standard_normal((50, 96)), dtype=torch.float32, device=cuda)
+    w = rng.uniform(0.1, 10.0, 96).astype(np.float32) if weighted else None
     acts, posts, Y = net.forward(X)
-    loss, G, Gb = net.mse(Y, T)
+    loss, G, Gb = net.mse(Y, T, torch.tensor(w, device=cuda) if weighted else None)
     dW, db = net.backward(acts, posts, G, Gb)
-    Ws = [w.float().cpu().numpy() for w in net.Wb]
+    Ws = [w_.float().cpu().numpy() for w_ in net.Wb]
     bs = [b.cpu().numpy() for b in net.b]
     H, oposts, oY = omlp.forward(X.float().cpu().numpy(), Ws, bs)
-    odW, odb, oloss = omlp.backward(H, oposts, oY, T.cpu().numpy(), Ws)
+    odW, odb, oloss = omlp.backward(H, oposts, oY, T.cpu().numpy(), Ws, col_w=w)
     assert abs(float(loss) - oloss) <= 1e-4 * oloss
     assert np.allclose(Y.cpu().numpy(), oY, rtol=1e-3, atol=1e-3 * np.abs(oY).max())
     for l in range(len(Ws)):
@@ -77,28 +79,43 @@ def test_mlp_fits_a_smooth_field(cuda):
     assert float(((net.predict(feats) - T) ** 2).mean()) < 2e-2
 
 
+def test_frame_basis_decode_on_the_gemm(cuda):
+    """Principal components of a set of frames and their decoding through
+    the BF16 GEMM with hi/lo splitting: full rank reproduces the frames."""
+    rng = np.random.default_rng(5)
+    X = torch.tensor(rng.random((40, 300)), dtype=torch.float32, device=cuda)
+    basis = surrogate.FrameBasis(X, 64)
+    assert basis.rank == 40
+    VV = (basis.V @ basis.V.T).cpu().numpy()
+    assert np.allclose(VV, np.eye(40), atol=1e-4)
+    net = MLP(4, 4, hidden=8, n_hidden=1, device=cuda)
+    Xr = basis.decode(net, basis.C.contiguous())
+    assert float((Xr - X).abs().max()) < 1e-4
+
+
 def test_surrogate_scan_gains_over_exact(cuda):
-    """A small strained crystal, 25 x 25 theta x chi grid: exact training
-    frames every 4th point per axis, the MLP for the rest, every 8th predicted
-    frame re-judged. The surrogate-assisted scan must beat the exact batched
-    scan in frames/s and keep judged frames within the 2% budget or send them
-    (and their blocks) to the exact sum."""
-    w = workloads.cu_bumps_scan_4m(cells=80, npix=128)      # 2.05M atoms
+    """A small strained crystal (2.05M atoms), 49 x 49 theta x chi grid over
+    +-0.2 deg, 64 x 64 ROI: exact training frames every 4th point per axis
+    (169), the MLP for the rest, every 8th predicted frame re-judged. Every
+    frame is also computed exactly (timed: the exact-only scan), so both the
+    network's own error on every predicted frame and the gain are measured."""
+    w = workloads.cu_bumps_scan_4m(cells=80, npix=128)
     th = np.radians(np.linspace(-0.2, 0.2, 49))
     ch = np.radians(np.linspace(-0.2, 0.2, 49))
     sc = SurrogateScan(w.beam, w.sample, w.detector, w.stage, th, ch, roi=64, stride=4,
-                       judge_every=8, tol=0.02, hidden=256, n_hidden=4, n_freq=16, fit_steps=1000,
-                       sc_kwargs=w.sc_kwargs)
-    res = sc.run(verify=16)
-    print({k: v for k, v in res.items() if k not in ("frames", "judge_err", "verify_err")},
-          "judge err median", float(np.median(res["judge_err"])),
-          "verify err median", float(np.median(res["verify_err"])) if len(res["verify_err"]) else None)
-    assert res["n_train"] == 169 and res["n_frames"] == 2401
-    assert res["final_loss"] < 0.2
-    assert np.isfinite(res["judge_err"]).all() and np.isfinite(res["verify_err"]).all()
-    # frames whose judge failed were replaced by the exact sum
+                       judge_every=8, tol=0.02, sc_kwargs=w.sc_kwargs)
+    res = sc.run(exact_all=True)
+    me, fe = res["model_err"], res["final_err"]
+    print({k: v for k, v in res.items() if k not in ("frames", "judge_err", "model_err", "final_err")},
+          "model err pct 50/90/100", np.percentile(me, [50, 90, 100]),
+          "final err pct 50/90/100", np.percentile(fe, [50, 90, 100]))
+    assert res["n_train"] == 169 and res["n_frames"] == 2401 and res["exact_measured"]
+    assert np.isfinite(me).all() and torch.isfinite(res["frames"]).all()
+    # the trained network alone, on every predicted frame
+    assert np.median(me) < 0.01
+    assert (me <= 0.02).mean() >= 0.9
+    # after judging and fallback
+    assert (fe <= 0.02).mean() >= 0.95
     assert res["n_fallback"] <= 7 * res["n_failed_judges"]
-    assert torch.isfinite(res["frames"]).all()
-    # what the trained network gains over computing every frame exactly
-    assert res["exact_frames"] < res["n_frames"]
-    assert res["gain"] > 1.0, res["gain"]
+    # frames/s over the exact-only scan, both timed here
+    assert res["gain"] > 1.5, res["gain"]
