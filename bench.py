@@ -4,7 +4,7 @@
                     [--config nacl_screw_8m]
 
 One step = one full kinematic exposure of the workload: stage transform and
-incident amplitudes, species/Morton tiling, per-pixel prologue, the FP32
+incident amplitudes, species + Hilbert tiling, per-pixel prologue, the FP32
 split-phase sum and the FP64 reduction. `value` is measured with the atom
 positions already resident in HBM; `e2e` goes through the public entry point
 ``beam.atomic_scattering_kinematic`` with host arrays (host->device copies and
@@ -16,6 +16,12 @@ The workload's data (positions + tiles, ~300 MB for 8.19M atoms) exceeds the
 N > 1 (torchrun): every rank runs its own replica of the workload (the path
 shards into independent exposures; there is no data-path collective) and
 `value` is the sum over ranks of terms / max-over-ranks time ("weak" scaling).
+
+Besides the timed steps, rank 0 reports (outside the timed region): the FP64
+plain kernel on a pixel subset (speed and error reference), the batched scan
+(48 frames of the 4M-atom rocking scan in one graph-captured launch), the
+surrogate-assisted 101 x 101 theta x chi scan (frames/s against the exact
+batched scan) and the CPU baseline.
 
 --impl reference times the reference algorithm's CPU implementation on the
 host cores (the C restatement in oracle/, all threads) on a bounded sample
@@ -213,6 +219,40 @@ def scan_leg(args, dev):
                     "frame index; atoms staged once, all frames one persistent launch"}
 
 
+def surrogate_leg(args, dev):
+    """Surrogate-assisted scan on the 101 x 101 theta x chi grid (+-0.3 deg)
+    of the 4M-atom crystal, 128^2 ROI: training frames every 4th point per
+    axis, every 8th predicted frame judged exactly, 2% fallback. The
+    exact-only scan's time is the training batch's per-frame time (same
+    batched kernel) times the 10,201 frames."""
+    import torch
+
+    from mosaic_gb300 import workloads
+    from mosaic_gb300.surrogate import SurrogateScan
+
+    w = workloads.cu_bumps_surrogate_4m()
+    m = w.meta
+    sc = SurrogateScan(w.beam, w.sample, w.detector, w.stage, m["theta_offsets"], m["chi_offsets"],
+                       roi=m["roi"], stride=4, judge_every=8, tol=0.02, sc_kwargs=w.sc_kwargs)
+    res = sc.run(verify=args.surrogate_verify)
+    torch.cuda.synchronize()
+    ve = res.get("verify_err", np.zeros(0))
+    pct = lambda x: [float(np.percentile(x, q)) for q in (50, 90, 100)] if len(x) else None
+    return {"workload": "cu_bumps_surrogate_4m", "grid": m["grid"], "roi": m["roi"],
+            "reading": "training frames every 4th point per axis (26 x 26)",
+            "frames": res["n_frames"], "frames_per_s": res["frames_per_s"],
+            "exact_frames_per_s": res["exact_frames_per_s"], "gain": res["gain"],
+            "exact_seconds_est": res["exact_seconds"], "seconds": res["seconds"],
+            "exact_frames": res["exact_frames"], "n_train": res["n_train"],
+            "n_judged": res["n_judged"], "n_failed_judges": res["n_failed_judges"],
+            "n_fallback": res["n_fallback"], "times": res["times"],
+            "judge_err_p50_p90_max": pct(res["judge_err"]),
+            "unjudged_err_p50_p90_max": pct(ve), "unjudged_checked": int(len(ve)),
+            "unjudged_frac_within_tol": float((ve <= 0.02).mean()) if len(ve) else None,
+            "mlp": {"params": res["params"], "components": res["rank"], "final_loss": res["final_loss"],
+                    "dtype": "bf16 weights/activations, fp32 accumulate (mma.sync)"}}
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -385,6 +425,7 @@ def run_ours(args):
     gpu_launches = args.steps * 8
 
     scan = scan_leg(args, dev) if (rank == 0 and args.scan_frames > 0) else None
+    surr = surrogate_leg(args, dev) if (rank == 0 and not args.no_surrogate) else None
     if rank == 0:
         cpu = cpu_baseline(w) if not args.no_cpu else None
         line = {
@@ -425,6 +466,7 @@ def run_ours(args):
             "clocks": clocks,
             "cpu_baseline": cpu,
             "scan": scan,
+            "surrogate_scan": surr,
         }
         print(json.dumps(line))
     if world > 1:
@@ -440,6 +482,10 @@ def main():
     ap.add_argument("--config", default="nacl_screw_8m")
     ap.add_argument("--fp64-subset", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="skip the surrogate-assisted scan leg (101 x 101 frames)")
+    ap.add_argument("--surrogate-verify", type=int, default=64,
+                    help="unjudged predicted frames checked against the exact sum (untimed)")
     ap.add_argument("--no-pairs", action="store_true",
                     help="one sin/cos per term (the pixel-pair form off)")
     ap.add_argument("--scan-frames", type=int, default=48,

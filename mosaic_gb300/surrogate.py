@@ -207,7 +207,11 @@ class FrameBasis:
         Xc = X - self.mu
         lam, U = np.linalg.eigh((Xc @ Xc.T).double().cpu().numpy())
         order = np.argsort(lam)[::-1][: min(int(rank), n)]
-        lam = np.clip(lam[order], 1e-30, None)
+        # drop components at the FP32 Gram product's round-off level (centring
+        # alone removes one dimension); 1e-6 of the top variance is 1e-3 of
+        # its amplitude
+        order = order[lam[order] > 1e-6 * max(float(lam.max()), 1e-300)]
+        lam = lam[order]
         U = U[:, order]
         dev = X.device
         self.V = (torch.tensor(U / np.sqrt(lam), dtype=torch.float32, device=dev).T @ Xc).contiguous()
@@ -273,11 +277,25 @@ class SurrogateScan:
         self.steps = [dict(mu=mu0 + self.theta[i], chi=chi0 + self.chi[j]) for i, j in self.ij]
         self._staged = None
 
-    def stage(self):
+    def prepare(self):
         """Stage the atoms and tiles once (setup shared by every exact call,
-        and by an exact-only scan alike)."""
+        and by an exact-only scan alike), and make the first call of every
+        kernel the surrogate uses (module loading, library handles) on a
+        throw-away problem, so that none of it lands in the timed phases."""
         if self._staged is None:
             self.exact(np.zeros(1, np.int64))
+            X = torch.rand((6, 64), device=self.dev)
+            b = FrameBasis(X, 3)
+            feats = fourier_features(self.xy[:6], self.n_freq, self.dev, f_max=self.f_max,
+                                     f_min=self.f_min)
+            net = MLP(feats.shape[1], b.rank + 1, hidden=32, n_hidden=2, seed=self.seed,
+                      device=self.dev)
+            T = torch.zeros((6, b.rank + 1), dtype=torch.float32, device=self.dev)
+            net.fit(feats, T, steps=2, col_w=torch.ones(b.rank + 1, device=self.dev))
+            Y = net.predict(feats)
+            sh = b.decode(net, Y[:, : b.rank].contiguous()).clamp_min_(0.0) * torch.exp(Y[:, b.rank:])
+            frame_rel_error(sh, sh + 1.0)
+            torch.cuda.synchronize()
 
     def exact(self, idx):
         """Exact intensities (len(idx), roi*roi) of the given frames, batched
@@ -309,7 +327,7 @@ class SurrogateScan:
         t = {}
         sync()
         t0 = time.perf_counter()
-        self.stage()
+        self.prepare()
         sync()
         setup_s = time.perf_counter() - t0
         t0 = time.perf_counter()

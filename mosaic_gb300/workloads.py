@@ -275,6 +275,18 @@ def cu_bumps_scan_4m(cells=100, npix=512, n_theta=181, chi_offsets_deg=(-0.3, -0
                          chi_offsets_deg=list(chi_offsets_deg), roi_sides=list(roi_sides), **meta))
 
 
+def cu_bumps_surrogate_4m(cells=100, npix=512, n_grid=101, half_range_deg=0.3, roi=128):
+    """Surrogate scan: the same 4M-atom bump-field crystal, a theta x chi grid
+    of n_grid x n_grid frames over +-half_range_deg on each motor (offsets
+    from the (111) Bragg setting), a roi x roi ROI at the detector centre."""
+    w = cu_bumps_scan_4m(cells=cells, npix=npix)
+    grid = np.radians(np.linspace(-half_range_deg, half_range_deg, n_grid))
+    w.name = "cu_bumps_surrogate_4m"
+    w.meta.update(theta_offsets=grid, chi_offsets=grid.copy(), roi=int(roi),
+                  grid=f"{n_grid}x{n_grid} over +-{half_range_deg} deg")
+    return w
+
+
 def nacl_screw_2m():
     """Quarter-size precision case (80 x 80 x 40 cells = 2,048,000 atoms, 256^2
     pixels) for kernel profiles: the same per-term work as nacl_screw_8m."""
@@ -284,7 +296,8 @@ def nacl_screw_2m():
 
 
 CONFIGS = {"fcc_cu_32k": fcc_cu_32k, "nacl_screw_8m": nacl_screw_8m, "nacl_screw_2m": nacl_screw_2m,
-           "cu_polycrystal_18m": cu_polycrystal_18m, "cu_bumps_scan_4m": cu_bumps_scan_4m}
+           "cu_polycrystal_18m": cu_polycrystal_18m, "cu_bumps_scan_4m": cu_bumps_scan_4m,
+           "cu_bumps_surrogate_4m": cu_bumps_surrogate_4m}
 
 
 def build(name, **kw):

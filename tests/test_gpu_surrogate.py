@@ -85,9 +85,9 @@ def test_frame_basis_decode_on_the_gemm(cuda):
     rng = np.random.default_rng(5)
     X = torch.tensor(rng.random((40, 300)), dtype=torch.float32, device=cuda)
     basis = surrogate.FrameBasis(X, 64)
-    assert basis.rank == 40
+    assert basis.rank == 39          # 40 centred frames span 39 dimensions
     VV = (basis.V @ basis.V.T).cpu().numpy()
-    assert np.allclose(VV, np.eye(40), atol=1e-4)
+    assert np.allclose(VV, np.eye(39), atol=1e-4)
     net = MLP(4, 4, hidden=8, n_hidden=1, device=cuda)
     Xr = basis.decode(net, basis.C.contiguous())
     assert float((Xr - X).abs().max()) < 1e-4
