@@ -69,6 +69,15 @@ typedef struct {
     double pol_e[3];      /* its unit vector (same frame) */
     int spherical_decay;  /* multiply by R0 / r */
     int remove_forward;   /* subtract f(0) where Q < Q_cut(pixel) */
+    /* Analyser acceptance of the general kernel (Beam.py:2350-2378): with
+     * theta the angle between the atom->pixel direction and the analyser
+     * axis, 1: top-hat, factor 1 for theta <= analyser_accept and 0 beyond;
+     * 2: Darwin roll-off 1 / (1 + (theta / analyser_halfwidth)^2) (factor 1
+     * when the half-width is <= 0); 0: no analyser. */
+    int analyser;
+    double analyser_dir[3];     /* unit analyser axis (frame of atoms and pixels) */
+    double analyser_accept;     /* top-hat acceptance half-angle [rad] */
+    double analyser_halfwidth;  /* Darwin half-width [rad] */
 } mk_physics;
 
 /* Per-pixel derived data, device arrays of length n_pix, filled by

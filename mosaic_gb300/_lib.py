@@ -118,7 +118,9 @@ class MkPhysics(ctypes.Structure):
     _fields_ = [("k", ctypes.c_double), ("beam_dir", ctypes.c_double * 3),
                 ("apply_pol", ctypes.c_int), ("pol_deg", ctypes.c_double),
                 ("pol_e", ctypes.c_double * 3), ("spherical_decay", ctypes.c_int),
-                ("remove_forward", ctypes.c_int)]
+                ("remove_forward", ctypes.c_int), ("analyser", ctypes.c_int),
+                ("analyser_dir", ctypes.c_double * 3), ("analyser_accept", ctypes.c_double),
+                ("analyser_halfwidth", ctypes.c_double)]
 
 
 class MkPixels(ctypes.Structure):

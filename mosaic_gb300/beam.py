@@ -232,10 +232,21 @@ class beam:
                                 e0=self._beam_E0_map, grid=self._beam_grid(), device=device)
 
     def physics(self, apply_polarization=False, spherical_decay=False, remove_forward=False,
-                beam_dir=(1.0, 0.0, 0.0), pol=None):
+                beam_dir=(1.0, 0.0, 0.0), pol=None, analyser=None):
         return engine.physics(self.k, beam_dir, apply_polarization,
                               self._polarization_state() if pol is None else pol,
-                              spherical_decay, remove_forward)
+                              spherical_decay, remove_forward, analyser)
+
+    @staticmethod
+    def analyser_budget(tiles, r0_min, phys):
+        """Largest relative error of the Darwin factor's first-order expansion
+        across a tile (the split kernel's per-atom form):
+        0.6 (rho / (R0 hw))^2 for tiles of radius rho; 0 otherwise (top-hat
+        tiles are classified exactly)."""
+        if phys.analyser == 2 and phys.analyser_halfwidth > 0.0:
+            rho = tiles.max_radius()
+            return 0.6 * (rho / (max(r0_min, 1e-30) * phys.analyser_halfwidth)) ** 2
+        return 0.0
 
     # ---------------------------------------------------------- the sum
     def split_budget(self, tiles, r0_min):
@@ -266,14 +277,22 @@ class beam:
             tiles = engine.Tiles(atoms, self.k, self._kernel_tile_atoms, device=atoms.pos.device)
             third, fresnel, tol, diag = self.split_budget(tiles, pix.r0_min())
             excursion = 2.0 * diag["tile_radius_m"] / max(pix.r0_min(), 1e-30)
+            ana_err = self.analyser_budget(tiles, pix.r0_min(), phys)
+            if ana_err > 1e-5:
+                self.last_run = dict(path="plain_f64", analyser_err=ana_err,
+                                     declined="Darwin analyser varies too fast across a tile", **diag)
+                return engine.run_plain(atoms, pix, phys, out=out, accumulate=accumulate)
             if third <= tol and excursion < 1e-6:
                 delta = engine.pair_delta(tiles, pix, self.k)
-                pairs_ok = delta <= engine.PAIR_DELTA_MAX
+                pairs_ok = delta <= engine.PAIR_DELTA_MAX and not phys.analyser
                 cfg = dict(launch or self._kernel_launch or tuned_launch(pix.n, tiles, pairs_ok))
                 if not pairs_ok:
                     cfg["pairs"] = 0
                 elif cfg.get("pairs"):
                     cfg["pair_short_radius_m"] = engine.pair_short_radius(tiles, pix, self.k)
+                if phys.analyser and (int(cfg.get("threads", 128)), int(cfg.get("pix_per_thread", 4))) \
+                        not in engine.ANALYSER_LAUNCHES:
+                    cfg.update(pix_per_thread=4, threads=128)
                 res = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg,
                                        fresnel=int(fresnel), out=out, accumulate=accumulate,
                                        fresnel_radius=diag["fresnel_radius_m"])
@@ -291,12 +310,12 @@ class beam:
                           apply_polarization: bool = False, spherical_decay: bool = True,
                           analyser_mode="off", analyser_acceptance_angle_rad: float = 0.0,
                           analyser_darwin_halfwidth_rad: float = 0.0, return_double=False):
-        """Kinematic scattering on the GPU (Beam.py:6028-6407); complex (Nz, Ny)."""
-        off = (analyser_mode is None
-               or (isinstance(analyser_mode, str) and analyser_mode.strip().lower() in ("off", "none", "disabled"))
-               or (not isinstance(analyser_mode, str) and analyser_mode == 0))
-        if not off:
-            raise NotImplementedError("analyser acceptance (top-hat/Darwin) is not provided")
+        """Kinematic scattering on the GPU (Beam.py:6028-6407); complex (Nz, Ny).
+
+        ``analyser_mode`` "top-hat" / "darwin" (or 1 / 2) applies the general
+        kernel's analyser factor (Beam.py:2350-2378) about the axis from the
+        origin to the detector's centre pixel (Beam.py:6127-6131)."""
+        kind = engine.analyser_kind(analyser_mode)
         if use_depth_ein:
             raise NotImplementedError("depth-dependent E_in (absorption maps) is not provided")
         if not torch.cuda.is_available():
@@ -308,7 +327,13 @@ class beam:
         coords = np.asarray(measurement_positions)
         if coords.shape != (3, Ny * Nz):
             raise ValueError(f"pixel coordinates {coords.shape} do not match shape ({Ny}, {Nz})")
-        phys = self.physics(apply_polarization, spherical_decay, remove_forward)
+        analyser = None
+        if kind:
+            cidx = (Nz // 2) * Ny + (Ny // 2)
+            centre = (coords[:, cidx].astype(np.float32) / np.float32(1e10)).astype(np.float64)
+            analyser = (kind, centre, float(analyser_acceptance_angle_rad),
+                        float(analyser_darwin_halfwidth_rad))
+        phys = self.physics(apply_polarization, spherical_decay, remove_forward, analyser=analyser)
         atoms = self.stage_atoms(sample, stage)
         pix = engine.Pixels(coords.astype(np.float64) / 1e10, Ny, Nz, phys)
         out = self.scatter_device(atoms, pix, phys)

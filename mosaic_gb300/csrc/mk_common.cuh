@@ -49,6 +49,43 @@ void mk_register_status_reader(mk_status_reader fn);
 #define MK_TWO_PI 6.283185307179586
 #define MK_PI 3.14159265358979323846
 
+// Analyser acceptance (Beam.py:2350-2378) from x = |r_hat - c|^2, the squared
+// chord between the unit atom->pixel direction and the analyser axis; the
+// angle is theta = 2 asin(sqrt(x) / 2), and x resolves small angles where
+// cos(theta) cannot. kind 1 top-hat: 1 for x <= x_accept (theta <= alpha,
+// x_accept = 4 sin^2(alpha / 2)), else 0; kind 2 Darwin:
+// 1 / (1 + (theta / hw)^2), 1 when hw <= 0.
+__host__ __device__ __forceinline__ double mk_analyser_factor(int kind, double x, double x_accept,
+                                                            double hw)
+{
+    if (kind == 1) return x <= x_accept ? 1.0 : 0.0;
+    if (kind == 2 && hw > 0.0) {
+        const double h = 0.5 * sqrt(x > 0.0 ? x : 0.0);
+        const double th = 2.0 * asin(h < 1.0 ? h : 1.0) / hw;
+        return 1.0 / (1.0 + th * th);
+    }
+    return 1.0;
+}
+
+// Checks and unpacks the analyser fields of mk_physics.
+static inline int mk_analyser_pack(const mk_physics *phys, int *kind, double *ax, double *ay,
+                                   double *az, double *x_accept, double *hw)
+{
+    *kind = phys->analyser;
+    *ax = *ay = *az = *x_accept = *hw = 0.0;
+    if (!phys->analyser) return MK_OK;
+    MK_REQUIRE(phys->analyser == 1 || phys->analyser == 2, "analyser kind must be 0, 1 or 2");
+    const double *c = phys->analyser_dir;
+    const double n = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    MK_REQUIRE(n > 0.0 && fabs(n - 1.0) < 1e-6, "analyser_dir must be a unit vector");
+    MK_REQUIRE(phys->analyser_accept >= 0.0, "analyser acceptance must be >= 0");
+    *ax = c[0] / n; *ay = c[1] / n; *az = c[2] / n;
+    const double h = sin(0.5 * (phys->analyser_accept < MK_PI ? phys->analyser_accept : MK_PI));
+    *x_accept = 4.0 * h * h;
+    *hw = phys->analyser_halfwidth;
+    return MK_OK;
+}
+
 // Per-species table passed by value to kernels.
 struct MkSpecies {
     int n;

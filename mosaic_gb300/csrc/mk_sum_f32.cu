@@ -77,6 +77,11 @@ struct MkSplitArgs {
     float pdeg;
     float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
     float pair_short_r; // PAIR kernels: tiles up to this radius [m] use the short polynomial
+    // analyser (ANA kernels, single exposures): kind 1 top-hat / 2 Darwin,
+    // beam direction and analyser axis in FP64, 4 sin^2(alpha/2), half-width
+    int analyser;
+    double an_b[3], an_c[3];
+    double an_xacc, an_hw, inv_kappa;
 };
 
 #define TWO_PI_F 6.28318530717958647692f
@@ -168,6 +173,51 @@ __device__ __forceinline__ void mk_tile_terms(const float4 *__restrict__ P,
     }
 }
 
+// The terms of one tile with a per-atom analyser multiplier
+//   m = (t <= th) ? g0 + g1 t : 0,   t = D.g (the change of the squared chord
+// |r_hat - c|^2 across the tile, linear in the offset D). Top-hat pixels that
+// straddle the acceptance edge in this tile use (th = x_accept - x0, g0 = 1,
+// g1 = 0); Darwin pixels the first-order expansion of the roll-off
+// (th = inf); pixels with one factor for the whole tile (g0, g1 = 0, inf).
+template <int PIX, bool FR, bool CPLX>
+__device__ __forceinline__ void mk_tile_terms_ana(
+    const float4 *__restrict__ P, const float2 *__restrict__ E, int T, const float (&wx)[PIX],
+    const float (&wy)[PIX], const float (&wz)[PIX], const float (&hq)[PIX], float bx, float by,
+    float bz, const float (&gx)[PIX], const float (&gy)[PIX], const float (&gz)[PIX],
+    const float (&th)[PIX], const float (&g0)[PIX], const float (&g1)[PIX], float (&csr)[PIX],
+    float (&csi)[PIX])
+{
+#pragma unroll 2
+    for (int j = 0; j < T; ++j) {
+        const float4 a = P[j];
+        const float2 e = E[j];
+        float db = 0.f;
+        if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
+#pragma unroll
+        for (int p = 0; p < PIX; ++p) {
+            float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
+            if (FR) {
+                const float sp = db - lin;
+                lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
+            }
+            const float t = fmaf(a.z, gz[p], fmaf(a.y, gy[p], a.x * gx[p]));
+            const float m = t <= th[p] ? fmaf(g1[p], t, g0[p]) : 0.f;
+            const float r = mk_frac_nearest(lin);
+            float sn, cs;
+            __sincosf(r * TWO_PI_F, &sn, &cs);
+            const float er = e.x * m;
+            if (CPLX) {
+                const float ei = e.y * m;
+                csr[p] = fmaf(er, cs, fmaf(-ei, sn, csr[p]));
+                csi[p] = fmaf(er, sn, fmaf(ei, cs, csi[p]));
+            } else {
+                csr[p] = fmaf(er, cs, csr[p]);
+                csi[p] = fmaf(er, sn, csi[p]);
+            }
+        }
+    }
+}
+
 // Pixel pairs (a, b) that are neighbours on the detector: with
 // sigma = D.(w_a + w_b)/2 (cycles) and delta = pi D.(w_a - w_b) (radians),
 //   exp(2 pi i D.w_a) = exp(2 pi i sigma) exp(+i delta),
@@ -234,7 +284,7 @@ __device__ __forceinline__ void mk_tile_terms_pair(
     }
 }
 
-template <int NT, int PIX, bool FRESNEL, bool CPLX, bool PAIR>
+template <int NT, int PIX, bool FRESNEL, bool CPLX, bool PAIR, bool ANA>
 __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ MkSplitArgs A)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -311,6 +361,70 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                 // 1 / (2 kappa |P - o|) for the |d|^2 term (D is in cycles).
                 hq[p] = FRESNEL ? 0.5f * uu.w / (A.kappa * fmaf(-uo, uu.w, 1.f)) : 0.f;
             }
+            // Analyser per (tile, pixel), in FP64: x0 = |u' - c|^2 at the tile
+            // origin and its gradient in the offset D; a top-hat factor is one
+            // number for the whole tile unless the tile's spread of x crosses
+            // the acceptance edge.
+            float agx[PIX], agy[PIX], agz[PIX], ath[PIX], ag0[PIX], ag1[PIX];
+            bool warp_atom = false, warp_zero = false;
+            if constexpr (ANA) {
+                bool need_atom = false, all_zero = true;
+#pragma unroll
+                for (int p = 0; p < PIX; ++p) {
+                    const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
+                    const double4 qq = A.q[g];
+                    const double ip = (double)A.u[g].w;
+                    const double ux = A.an_b[0] - qq.x * A.inv_kappa;
+                    const double uy = A.an_b[1] - qq.y * A.inv_kappa;
+                    const double uz = A.an_b[2] - qq.z * A.inv_kappa;
+                    const double uo = ux * o.x + uy * o.y + uz * o.z;
+                    const double px_ = ux - (o.x - uo * ux) * ip;
+                    const double py_ = uy - (o.y - uo * uy) * ip;
+                    const double pz_ = uz - (o.z - uo * uz) * ip;
+                    const double vx = px_ - A.an_c[0], vy = py_ - A.an_c[1], vz = pz_ - A.an_c[2];
+                    const double x0 = vx * vx + vy * vy + vz * vz;
+                    const double ro = ip / (1.0 - uo * ip);          // 1 / |P - o|
+                    const double vu = vx * px_ + vy * py_ + vz * pz_;
+                    const double gs = -2.0 * ro * A.inv_kappa;       // per cycle of D
+                    const double gxd = gs * (vx - vu * px_), gyd = gs * (vy - vu * py_),
+                                 gzd = gs * (vz - vu * pz_);
+                    agx[p] = (float)gxd; agy[p] = (float)gyd; agz[p] = (float)gzd;
+                    const double rho = o.w;
+                    const double spread = sqrt(gxd * gxd + gyd * gyd + gzd * gzd) * rho / A.inv_kappa +
+                                          4.0 * rho * rho * ro * ro;
+                    ath[p] = INFINITY;
+                    ag1[p] = 0.f;
+                    if (A.analyser == 1) {
+                        if (x0 + spread <= A.an_xacc) {
+                            ag0[p] = 1.f;
+                        } else if (x0 - spread > A.an_xacc) {
+                            ag0[p] = 0.f;
+                        } else {
+                            ag0[p] = 1.f;
+                            ath[p] = (float)(A.an_xacc - x0);
+                            need_atom = true;
+                        }
+                    } else if (A.analyser == 2 && A.an_hw > 0.0) {
+                        // G(x) = 1 / (1 + theta^2 / hw^2), theta = 2 asin(sqrt(x)/2);
+                        // dtheta^2/dx = (theta / sqrt x) / sqrt(1 - x/4)
+                        const double sx = sqrt(x0);
+                        const double thv = 2.0 * asin(fmin(0.5 * sx, 1.0));
+                        const double ts = sx > 1e-6 ? thv / sx : 1.0 + x0 / 24.0;
+                        const double r = thv / A.an_hw;
+                        const double G0 = 1.0 / (1.0 + r * r);
+                        const double G1 = -G0 * G0 * ts / sqrt(fmax(1.0 - 0.25 * x0, 1e-30)) /
+                                          (A.an_hw * A.an_hw);
+                        ag0[p] = (float)G0;
+                        ag1[p] = (float)G1;
+                        need_atom = true;
+                    } else {
+                        ag0[p] = 1.f;
+                    }
+                    if (pix[p] < F.n_pix && ag0[p] != 0.f) all_zero = false;
+                }
+                warp_atom = __any_sync(0xffffffffu, need_atom);
+                warp_zero = __all_sync(0xffffffffu, all_zero && !need_atom);
+            }
             const bool ok = mk_mbar_wait_bounded(&bar[buf], parity, MK_WAIT_LIMIT_NS);
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
@@ -370,11 +484,27 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                     csr[2 * q + 1] = pr[q] - qr[q];
                     csi[2 * q + 1] = pi_[q] - qi[q];
                 }
+            } else if (ANA && warp_zero) {
+                // every pixel of the warp is outside the acceptance for this tile
+            } else if (ANA && warp_atom) {
+                if (fr_tile)
+                    mk_tile_terms_ana<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
+                                                       agx, agy, agz, ath, ag0, ag1, csr, csi);
+                else
+                    mk_tile_terms_ana<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
+                                                        agx, agy, agz, ath, ag0, ag1, csr, csi);
             } else {
                 if (fr_tile)
                     mk_tile_terms<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
                 else
                     mk_tile_terms<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
+                if constexpr (ANA) {
+#pragma unroll
+                    for (int p = 0; p < PIX; ++p) {   // one analyser factor per (tile, pixel)
+                        csr[p] *= ag0[p];
+                        csi[p] *= ag0[p];
+                    }
+                }
             }
             __syncthreads();   // every thread is done with buffer `buf`
             if (tid == 0 && t + 2 < t_hi) {
@@ -529,33 +659,42 @@ int mk_launch_reduce(const double2 *partial, int slices, int n_pix, const double
 // ----------------------------------------------------------------- launch
 typedef void (*mk_split_fn)(const MkSplitArgs);
 
-template <int NT, int PIX, bool PAIR>
+template <int NT, int PIX, bool PAIR, bool ANA>
 static mk_split_fn mk_pick4(bool fresnel, bool cplx)
 {
     if (fresnel)
-        return cplx ? mk_split_kernel<NT, PIX, true, true, PAIR> : mk_split_kernel<NT, PIX, true, false, PAIR>;
-    return cplx ? mk_split_kernel<NT, PIX, false, true, PAIR> : mk_split_kernel<NT, PIX, false, false, PAIR>;
+        return cplx ? mk_split_kernel<NT, PIX, true, true, PAIR, ANA>
+                    : mk_split_kernel<NT, PIX, true, false, PAIR, ANA>;
+    return cplx ? mk_split_kernel<NT, PIX, false, true, PAIR, ANA>
+                : mk_split_kernel<NT, PIX, false, false, PAIR, ANA>;
 }
 
+// Pairs need an even PIX; the analyser kernels (no pairs) exist for
+// 128/256 threads and 2 or 4 pixels per thread.
 template <int NT, int PIX>
-static mk_split_fn mk_pick3(bool fresnel, bool cplx, bool pair)
+static mk_split_fn mk_pick3(bool fresnel, bool cplx, bool pair, bool ana)
 {
+    if (ana) {
+        if constexpr ((NT == 128 || NT == 256) && (PIX == 2 || PIX == 4))
+            return pair ? nullptr : mk_pick4<NT, PIX, false, true>(fresnel, cplx);
+        return nullptr;
+    }
     if constexpr (PIX % 2 == 0) {
-        if (pair) return mk_pick4<NT, PIX, true>(fresnel, cplx);
+        if (pair) return mk_pick4<NT, PIX, true, false>(fresnel, cplx);
     } else {
         if (pair) return nullptr;
     }
-    return mk_pick4<NT, PIX, false>(fresnel, cplx);
+    return mk_pick4<NT, PIX, false, false>(fresnel, cplx);
 }
 
-static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, bool pair)
+static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, bool pair, bool ana)
 {
 #define MK_PIX_CASES(NT_)                                                  \
     switch (pix) {                                                         \
-    case 1: return mk_pick3<NT_, 1>(fresnel, cplx, pair);                  \
-    case 2: return mk_pick3<NT_, 2>(fresnel, cplx, pair);                  \
-    case 4: return mk_pick3<NT_, 4>(fresnel, cplx, pair);                  \
-    case 8: return mk_pick3<NT_, 8>(fresnel, cplx, pair);                  \
+    case 1: return mk_pick3<NT_, 1>(fresnel, cplx, pair, ana);             \
+    case 2: return mk_pick3<NT_, 2>(fresnel, cplx, pair, ana);             \
+    case 4: return mk_pick3<NT_, 4>(fresnel, cplx, pair, ana);             \
+    case 8: return mk_pick3<NT_, 8>(fresnel, cplx, pair, ana);             \
     default: return nullptr;                                               \
     }
     switch (nt) {
@@ -574,12 +713,14 @@ struct MkLaunchShape {
     int resident;      // blocks that fit the GPU at once
 };
 
-static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShape *out)
+static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShape *out,
+                           bool ana = false)
 {
     mk_split_fn fn = mk_pick(launch->threads, launch->pix_per_thread, launch->fresnel != 0,
-                             launch->amp_real == 0, launch->pairs != 0);
-    MK_REQUIRE(fn, "split kernel: unsupported launch shape threads=%d pix=%d", launch->threads,
-               launch->pix_per_thread);
+                             launch->amp_real == 0, launch->pairs != 0, ana);
+    MK_REQUIRE(fn, "split kernel: unsupported launch shape threads=%d pix=%d pairs=%d%s",
+               launch->threads, launch->pix_per_thread, launch->pairs,
+               ana ? " with the analyser (128/256 threads, 2/4 pixels, no pairs)" : "");
     const size_t smem = mk_split_smem(tile_atoms);
     MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
@@ -677,8 +818,10 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
     memset(&A, 0, sizeof(A));
     int rc = mk_species_pack(spc, &A.sp);
     if (rc != MK_OK) return rc;
+    const bool ana = phys->analyser != 0;
+    MK_REQUIRE(!ana || n_frames == 1, "split kernel: the analyser is for single exposures");
     MkLaunchShape sh;
-    rc = mk_launch_shape(T, launch, &sh);
+    rc = mk_launch_shape(T, launch, &sh, ana);
     if (rc != MK_OK) return rc;
     mk_register_status_reader(mk_split_read_status);
     int *status = nullptr;
@@ -709,6 +852,14 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
     A.pdeg = (float)phys->pol_deg;
     A.fres_r = launch->fresnel_radius_m > 0.0 ? (float)launch->fresnel_radius_m : 0.f;
     A.pair_short_r = launch->pair_short_radius_m > 0.0 ? (float)launch->pair_short_radius_m : -1.f;
+    if (ana) {
+        double cx, cy, cz;
+        rc = mk_analyser_pack(phys, &A.analyser, &cx, &cy, &cz, &A.an_xacc, &A.an_hw);
+        if (rc != MK_OK) return rc;
+        A.an_c[0] = cx; A.an_c[1] = cy; A.an_c[2] = cz;
+        for (int c = 0; c < 3; ++c) A.an_b[c] = phys->beam_dir[c];
+        A.inv_kappa = MK_TWO_PI / phys->k;
+    }
     MK_CHECK_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned long long), st));
     const long long grid = std::min<long long>(n_items, sh.resident);
     sh.fn<<<(unsigned)grid, launch->threads, mk_split_smem(T), st>>>(A);

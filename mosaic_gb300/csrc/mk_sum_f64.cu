@@ -33,6 +33,8 @@ struct MkPlainArgs {
     double k;
     int apply_pol, decay, remove_forward;
     double pdeg, ex, ey, ez;
+    int analyser;                      // 0 off, 1 top-hat, 2 Darwin
+    double ax, ay, az, x_accept, hw;   // axis, 4 sin^2(alpha/2), half-width
 };
 
 __global__ void __launch_bounds__(F64_NT) mk_plain_f64_kernel(
@@ -110,6 +112,11 @@ __global__ void __launch_bounds__(F64_NT) mk_plain_f64_kernel(
                 P = P < 0.0 ? 0.0 : (P > 1.0 ? 1.0 : P);
                 scale *= sqrt(P);
             }
+            if (A.analyser) {
+                const double vx = dx / r - A.ax, vy = dy / r - A.ay, vz = dz / r - A.az;
+                scale *= mk_analyser_factor(A.analyser, vx * vx + vy * vy + vz * vz, A.x_accept,
+                                            A.hw);
+            }
             acc_r += (tr * c - ti * sn) * scale;
             acc_i += (tr * sn + ti * c) * scale;
         }
@@ -159,6 +166,8 @@ extern "C" int mk_kin_plain_f64(int64_t n, const double *pos, const int *species
     A.ex = phys->pol_e[0];
     A.ey = phys->pol_e[1];
     A.ez = phys->pol_e[2];
+    rc = mk_analyser_pack(phys, &A.analyser, &A.ax, &A.ay, &A.az, &A.x_accept, &A.hw);
+    if (rc != MK_OK) return rc;
     cudaStream_t st = mk_stream(stream);
     if (n == 0) {
         if (!accumulate) MK_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)n_pix, st));

@@ -76,8 +76,29 @@ class SpeciesTable:
                          ai.ctypes.data, None if b is None else b.ctypes.data)
 
 
+ANALYSER_KINDS = {"off": 0, "none": 0, "disabled": 0, "top_hat": 1, "tophat": 1, "top-hat": 1,
+                  "top": 1, "darwin": 2, "rolloff": 2, "roll-off": 2}
+
+
+# (threads, pixels per thread) the split kernel's analyser variant is built for
+ANALYSER_LAUNCHES = ((128, 2), (128, 4), (256, 2), (256, 4))
+
+
+def analyser_kind(mode):
+    """Analyser mode (name or 0/1/2) -> 0 off, 1 top-hat, 2 Darwin; unknown
+    names and codes mean off, as in the reference (Beam.py:6134-6143)."""
+    if mode is None:
+        return 0
+    if isinstance(mode, str):
+        return ANALYSER_KINDS.get(mode.strip().lower(), 0)
+    k = int(mode)
+    return k if k in (1, 2) else 0
+
+
 def physics(k, beam_dir=(1.0, 0.0, 0.0), apply_pol=False, pol=(0.0, 0.0, 1.0, 0.0),
-            spherical_decay=False, remove_forward=False):
+            spherical_decay=False, remove_forward=False, analyser=None):
+    """mk_physics. ``analyser`` = (kind, axis (3,), acceptance [rad],
+    Darwin half-width [rad]) or None."""
     ph = MkPhysics()
     ph.k = float(k)
     ph.beam_dir[:] = [float(v) for v in beam_dir]
@@ -86,6 +107,15 @@ def physics(k, beam_dir=(1.0, 0.0, 0.0), apply_pol=False, pol=(0.0, 0.0, 1.0, 0.
     ph.pol_e[:] = [float(v) for v in pol[1:4]]
     ph.spherical_decay = int(bool(spherical_decay))
     ph.remove_forward = int(bool(remove_forward))
+    if analyser is not None and analyser_kind(analyser[0]):
+        axis = np.asarray(analyser[1], dtype=np.float64).reshape(3)
+        nrm = float(np.linalg.norm(axis))
+        if not nrm > 0.0:
+            raise ValueError("analyser axis must be a non-zero vector")
+        ph.analyser = analyser_kind(analyser[0])
+        ph.analyser_dir[:] = [float(v) for v in axis / nrm]
+        ph.analyser_accept = float(analyser[2])
+        ph.analyser_halfwidth = float(analyser[3])
     return ph
 
 

@@ -295,7 +295,17 @@ def nacl_screw_2m():
     return w
 
 
+def nacl_screw_8m_px128():
+    """The headline crystal (8,192,000 atoms) on a 128 x 128 detector: a
+    profile case whose tiles (~200 MB) exceed L2 like the full run's, so its
+    DRAM traffic per pixel block is the full run's."""
+    w = nacl_screw_8m(npix=128)
+    w.name = "nacl_screw_8m_px128"
+    return w
+
+
 CONFIGS = {"fcc_cu_32k": fcc_cu_32k, "nacl_screw_8m": nacl_screw_8m, "nacl_screw_2m": nacl_screw_2m,
+           "nacl_screw_8m_px128": nacl_screw_8m_px128,
            "cu_polycrystal_18m": cu_polycrystal_18m, "cu_bumps_scan_4m": cu_bumps_scan_4m,
            "cu_bumps_surrogate_4m": cu_bumps_surrogate_4m}
 

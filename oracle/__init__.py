@@ -70,7 +70,7 @@ def lib():
             ctypes.c_int64, dp, fp, fp, ctypes.c_int, fp, fp, fp, fp, fp,
             ctypes.c_int, ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int,
             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-            ctypes.c_int, dp, dp, ctypes.c_int]
+            ctypes.c_int, ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, dp, dp, ctypes.c_int]
         L.mko_prop_mul_f64.restype = None
         L.mko_prop_mul_f64.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -85,12 +85,15 @@ def _p(a, ct):
 
 def scatter_f64(pos_m, wk, f0z, anom_re, anom_im, amp_re, amp_im, cx, cy, cz, k,
                 ny, nz, remove_forward=False, apply_pol=False,
-                pol=(0.0, 0.0, 1.0, 0.0), decay=False, dw_b=None, n_threads=None):
+                pol=(0.0, 0.0, 1.0, 0.0), decay=False, dw_b=None, n_threads=None,
+                analyser=None):
     """FP64 kinematic sum (compute_scattering_cffi semantics, double output).
 
     Args mirror ``Beam.py:631-651``: positions (N,3) metres, per-atom WK rows
     (N,11), f0(0), f'/f'' and incident amplitude; pixel coordinates in metres.
-    ``pol`` = (p, ex, ey, ez). Returns complex128 (ny*nz,).
+    ``pol`` = (p, ex, ey, ez). ``analyser`` = (kind 1 top-hat / 2 Darwin,
+    axis (3,), acceptance [rad], half-width [rad]), the general GPU kernel's
+    factor (Beam.py:2350-2378). Returns complex128 (ny*nz,).
     """
     L = lib()
     n = int(np.asarray(pos_m).shape[0])
@@ -105,6 +108,12 @@ def scatter_f64(pos_m, wk, f0z, anom_re, anom_im, amp_re, amp_im, cx, cy, cz, k,
     out_r = np.zeros(P)
     out_i = np.zeros(P)
     nt = int(n_threads or os.cpu_count() or 1)
+    an_kind, an_axis, an_acc, an_hw = 0, np.zeros(3), 0.0, 0.0
+    if analyser is not None and int(analyser[0]):
+        an_kind = int(analyser[0])
+        an_axis = f64(analyser[1]).reshape(3)
+        an_acc, an_hw = float(analyser[2]), float(analyser[3])
+    an_axis = f64(an_axis)
     rc = L.mko_scatter_f64(
         n, _p(pos, ctypes.c_double), _p(wk, ctypes.c_float), _p(f0z, ctypes.c_float),
         int(bool(remove_forward)), _p(ar, ctypes.c_float), _p(ai, ctypes.c_float),
@@ -113,6 +122,7 @@ def scatter_f64(pos_m, wk, f0z, anom_re, anom_im, amp_re, amp_im, cx, cy, cz, k,
         int(ny), int(nz), _p(cx, ctypes.c_double), _p(cy, ctypes.c_double),
         _p(cz, ctypes.c_double), float(k), int(bool(apply_pol)),
         float(pol[0]), float(pol[1]), float(pol[2]), float(pol[3]), int(bool(decay)),
+        an_kind, _p(an_axis, ctypes.c_double), an_acc, an_hw,
         _p(out_r, ctypes.c_double), _p(out_i, ctypes.c_double), nt)
     if rc != 0:
         raise MemoryError("oracle scatter could not allocate its work buffers")
@@ -201,9 +211,11 @@ def ein_bilinear(pos, E0, du, dv, uc, vc, e1=(0, 1, 0), e2=(0, 0, 1)):
 def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV,
                  f0_rows, f0_zero, f1f2_tables, E0, beam_grid, pol_state,
                  remove_forward=False, apply_polarization=False,
-                 spherical_decay=False, dw_b=None, n_threads=None):
+                 spherical_decay=False, dw_b=None, n_threads=None, analyser=None):
     """Restatement of ``interact_beam_cpu`` (Beam.py:5773-5956) for E0-only
-    incident fields, returning complex128 (Nz, Ny).
+    incident fields, returning complex128 (Nz, Ny). ``analyser`` (see
+    ``scatter_f64``) adds the GPU general kernel's analyser factor, which the
+    reference's CPU path does not apply.
 
     chunks: iterable of (positions (N,3) float32 A, species labels (N,)).
     beam_grid: (du, dv, uc, vc). f0_rows: element -> (11,) float32;
@@ -247,5 +259,6 @@ def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV
                            amp.real, amp.imag, cx, cy, cz, k, Ny, Nz,
                            remove_forward=remove_forward, apply_pol=apply_polarization,
                            pol=pol_state, decay=spherical_decay,
-                           dw_b=None if dw_b is None else b, n_threads=n_threads)
+                           dw_b=None if dw_b is None else b, n_threads=n_threads,
+                           analyser=analyser)
     return out.reshape(Nz, Ny)

@@ -23,6 +23,11 @@
  * with Q_cut(P) from the right/up pixel neighbours (Beam.py:716-746) and the
  * polarization factor P_pol = (1-p)(1+dotv^2)/2 + p(1-(e.r_hat)^2) clamped to
  * [0,1] (Beam.py:793-801).
+ *
+ * Optional analyser (the reference's GPU general kernel only, Beam.py:2350-2378;
+ * its CPU path ignores it): theta = angle between r_hat and the analyser axis
+ * c, evaluated as theta = 2 asin(|r_hat - c| / 2); top-hat: term x 0 when
+ * theta > alpha; Darwin: term x 1 / (1 + (theta / hw)^2) (x 1 when hw <= 0).
  */
 #include <math.h>
 #include <pthread.h>
@@ -82,6 +87,8 @@ typedef struct {
     int npix;
     const double *cx, *cy, *cz, *qcut, *r0;
     double k, pdeg, ex, ey, ez;
+    int analyser;
+    double anx, any, anz, accept, hw;
     double *acc_r, *acc_i; /* this slice's own accumulators */
 } mko_slice;
 
@@ -124,6 +131,16 @@ static void *mko_run_slice(void *arg)
                 if (P > 1.0) P = 1.0;
                 scale *= sqrt(P);
             }
+            if (S->analyser) {
+                const double vx = dx / r - S->anx, vy = dy / r - S->any, vz = dz / r - S->anz;
+                const double th = 2.0 * asin(0.5 * sqrt(vx * vx + vy * vy + vz * vz));
+                if (S->analyser == 1) {
+                    if (th > S->accept) scale = 0.0;
+                } else if (S->analyser == 2 && S->hw > 0.0) {
+                    const double t = th / S->hw;
+                    scale *= 1.0 / (1.0 + t * t);
+                }
+            }
             S->acc_r[p] += (tr * c - ti * sn) * scale;
             S->acc_i[p] += (tr * sn + ti * c) * scale;
         }
@@ -145,7 +162,8 @@ int mko_scatter_f64(int64_t n_atoms, const double *pos, const float *wk,
                     const float *dw_b, int ny, int nz, const double *cx,
                     const double *cy, const double *cz, double k, int apply_pol,
                     double pol_deg, double pol_ex, double pol_ey, double pol_ez,
-                    int decay, double *out_re, double *out_im, int n_threads)
+                    int decay, int analyser, const double *an_axis, double an_accept,
+                    double an_halfwidth, double *out_re, double *out_im, int n_threads)
 {
     const int npix = ny * nz;
     if (n_atoms <= 0 || npix <= 0) return 0;
@@ -173,6 +191,13 @@ int mko_scatter_f64(int64_t n_atoms, const double *pos, const float *wk,
         S->remove_forward = remove_forward; S->apply_pol = apply_pol; S->decay = decay;
         S->npix = npix; S->cx = cx; S->cy = cy; S->cz = cz; S->qcut = qcut; S->r0 = r0;
         S->k = k; S->pdeg = pol_deg; S->ex = pol_ex; S->ey = pol_ey; S->ez = pol_ez;
+        S->analyser = analyser;
+        if (analyser) {
+            const double n = sqrt(an_axis[0] * an_axis[0] + an_axis[1] * an_axis[1] +
+                                  an_axis[2] * an_axis[2]);
+            S->anx = an_axis[0] / n; S->any = an_axis[1] / n; S->anz = an_axis[2] / n;
+        }
+        S->accept = an_accept; S->hw = an_halfwidth;
         S->acc_r = acc + (size_t)2 * npix * t;
         S->acc_i = S->acc_r + npix;
     }
