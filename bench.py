@@ -296,6 +296,8 @@ def run_ours(args):
 
     w = workloads.build(args.config)
     B = w.beam
+    if args.tile_atoms:
+        B._kernel_tile_atoms = int(args.tile_atoms)
     kw = w.sc_kwargs
     phys = B.physics(kw["apply_polarization"], kw["spherical_decay"], kw["remove_forward"])
     pos_h, idx_h, labels = B.collect_atoms(w.sample)
@@ -444,6 +446,14 @@ def run_ours(args):
             "gpu_launches": gpu_launches,
             "roofline": {"bound": bound, "achieved": achieved / 1e9, "peak": peak_terms / 1e9,
                          "unit": "Gterm/s", "frac": achieved / peak_terms, "traffic": None,
+                         "traffic_profile": {"workload": "nacl_screw_8m_px128 (same 8.19M atoms, 128^2 "
+                                             "pixels; tiles exceed L2 as here)",
+                                             "dram_bytes_per_launch": 294395136,
+                                             "terms_per_launch": 8192000 * 16384,
+                                             "note": "ncu dram__bytes_read+write of one launch; reads "
+                                                     "~ the tile data once (concurrent items share "
+                                                     "slices in L2), writes the partial fields; "
+                                                     "not proportional to terms, so not scaled"},
                          "peak_source": f"canonical term: min(MUFU sin/cos {mufu:.2f}/clk/SM / "
                                         f"{MUFU_PER_TERM} per term, FP32 {fma:.1f}/clk/SM / "
                                         f"{FP32_PER_TERM} per term), both pipes measured on this "
@@ -480,6 +490,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="nacl_screw_8m")
+    ap.add_argument("--tile-atoms", type=int, default=0,
+                    help="atoms per tile (power of two, 128-4096; 0: the beam's default 1024)")
     ap.add_argument("--fp64-subset", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true",

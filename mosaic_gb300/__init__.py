@@ -7,9 +7,9 @@ sum in hand-written sm_103a CUDA kernels behind the C ABI of
 """
 from .beam import beam
 from .geometry import Detector, Stage, StaticStage, polarization_from_rate, polarization_state
-from .sample import ChunkedSample, thermal_displacement
+from .sample import ChunkedSample, DiskSample, thermal_displacement, write_sample
 from .tables import ScatteringTables
 
-__all__ = ["beam", "Detector", "Stage", "StaticStage", "ChunkedSample", "ScatteringTables",
+__all__ = ["beam", "Detector", "Stage", "StaticStage", "ChunkedSample", "DiskSample", "write_sample", "ScatteringTables",
            "polarization_from_rate", "polarization_state", "thermal_displacement"]
 __version__ = "1.0.0"

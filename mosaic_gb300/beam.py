@@ -192,19 +192,9 @@ class beam:
         pos_list, idx_list, labels = [], [], []
         lab_index = {}
         for cid in range(1, n_chunks + 1):
-            try:
-                codes, lab = sample.load_chunk_species(cid, use_gpu=False, codes=True)
-                codes = np.asarray(codes)
-                lab = np.asarray(lab).astype(str)
-            except TypeError:
-                spc = np.asarray(sample.load_chunk_species(cid, use_gpu=False)).astype(str)
-                lab, codes = np.unique(spc, return_inverse=True)
-                codes = codes.reshape(-1)
+            codes, lab, pos = self._load_chunk(sample, cid)
             if codes.size == 0:
                 continue
-            pos = np.asarray(sample.load_chunk_positions(cid, use_gpu=False), dtype=np.float32)
-            if pos.shape[0] != codes.shape[0]:
-                raise ValueError(f"positions/species size mismatch for chunk {cid}")
             remap = np.full(len(lab), -1, dtype=np.int32)
             for i, el in enumerate(lab):
                 if not self.tables.has(el):
@@ -223,13 +213,102 @@ class beam:
             return np.zeros((0, 3), np.float32), np.zeros(0, np.int32), labels
         return np.concatenate(pos_list), np.concatenate(idx_list), labels
 
+    def _load_chunk(self, sample, cid):
+        """(codes, labels, positions float32) of one chunk, host side."""
+        try:
+            codes, lab = sample.load_chunk_species(cid, use_gpu=False, codes=True)
+            codes = np.asarray(codes)
+            lab = np.asarray(lab).astype(str)
+        except TypeError:
+            spc = np.asarray(sample.load_chunk_species(cid, use_gpu=False)).astype(str)
+            lab, codes = np.unique(spc, return_inverse=True)
+            codes = codes.reshape(-1)
+        pos = np.asarray(sample.load_chunk_positions(cid, use_gpu=False), dtype=np.float32) \
+            if codes.size else np.zeros((0, 3), np.float32)
+        if pos.shape[0] != codes.shape[0]:
+            raise ValueError(f"positions/species size mismatch for chunk {cid}")
+        return codes, lab, pos
+
+    def stream_atoms(self, sample, device="cuda"):
+        """Chunks straight into device arrays, without a host-side copy of the
+        whole sample: one worker thread reads chunk i+1 (file read, thermal
+        draw) while chunk i goes host -> device from one of two pinned staging
+        buffers on a side stream. Returns device positions (N, 3) float32 A,
+        species indices (N,) int32, the labels and the atoms per label."""
+        from concurrent.futures import ThreadPoolExecutor
+        n_chunks = int(sample.chunk_total or 0)
+        sizes = [int(sample.chunk_atom_count(c)) for c in range(1, n_chunks + 1)]
+        n_max = sum(sizes)
+        dev = torch.device(device)
+        pos_d = torch.empty((max(n_max, 1), 3), dtype=torch.float32, device=dev)
+        idx_d = torch.empty(max(n_max, 1), dtype=torch.int32, device=dev)
+        big = max(sizes) if sizes else 1
+        cache = getattr(self, "_staging", None)
+        if cache is None or cache[0][0].shape[0] < big:
+            cache = ([torch.empty((big, 3), dtype=torch.float32).pin_memory() for _ in range(2)],
+                     [torch.empty(big, dtype=torch.int32).pin_memory() for _ in range(2)])
+            self._staging = cache                # pinned once, reused by later calls
+        st_pos, st_idx = cache
+        done = [None, None]
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        labels, lab_index, counts = [], {}, []
+        off = 0
+        with ThreadPoolExecutor(max_workers=1) as ex:
+            nxt = ex.submit(self._load_chunk, sample, 1) if n_chunks else None
+            for cid in range(1, n_chunks + 1):
+                codes, lab, pos = nxt.result()
+                nxt = ex.submit(self._load_chunk, sample, cid + 1) if cid < n_chunks else None
+                if codes.size == 0:
+                    continue
+                remap = np.full(len(lab), -1, dtype=np.int32)
+                for i, el in enumerate(lab):
+                    if not self.tables.has(el):
+                        continue
+                    if el not in lab_index:
+                        lab_index[el] = len(labels)
+                        labels.append(el)
+                        counts.append(0)
+                    remap[i] = lab_index[el]
+                g = remap[codes]
+                keep = g >= 0
+                if not keep.all():
+                    pos, g = pos[keep], g[keep]
+                n = int(pos.shape[0])
+                if n == 0:
+                    continue
+                for j, c in enumerate(np.bincount(g, minlength=len(labels))):
+                    counts[j] += int(c)
+                b = cid & 1
+                if done[b] is not None:
+                    done[b].synchronize()        # staging buffer b is free again
+                st_pos[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(pos)))
+                st_idx[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(g, dtype=np.int32)))
+                with torch.cuda.stream(side):
+                    pos_d[off:off + n].copy_(st_pos[b][:n], non_blocking=True)
+                    idx_d[off:off + n].copy_(st_idx[b][:n], non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(side)
+                    done[b] = ev
+                off += n
+        torch.cuda.current_stream(dev).wait_stream(side)
+        # the staging buffers must outlive the copies: wait before they go
+        for ev in done:
+            if ev is not None:
+                ev.synchronize()
+        return pos_d[:off], idx_d[:off], labels, np.asarray(counts, dtype=np.int64)
+
     def stage_atoms(self, sample, stage, device="cuda"):
-        """All atoms on the device, lab frame, with their incident amplitudes."""
-        pos, idx, labels = self.collect_atoms(sample)
+        """All atoms on the device, lab frame, with their incident amplitudes
+        (chunks streamed to the device by ``stream_atoms``)."""
+        pos, idx, labels, counts = self.stream_atoms(sample, device)
         table = engine.SpeciesTable.build(labels or ["H"], self.tables, self._energy,
                                           self._debye_waller)
+        if not labels:
+            counts = np.zeros(1, dtype=np.int64)
         return engine.atoms_lab(pos, idx, stage.rotation, stage.translation, table,
-                                e0=self._beam_E0_map, grid=self._beam_grid(), device=device)
+                                e0=self._beam_E0_map, grid=self._beam_grid(), device=device,
+                                counts=counts)
 
     def physics(self, apply_polarization=False, spherical_decay=False, remove_forward=False,
                 beam_dir=(1.0, 0.0, 0.0), pol=None, analyser=None):

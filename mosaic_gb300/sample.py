@@ -1,4 +1,5 @@
-"""In-memory chunked sample with the reference's chunk API.
+"""Chunked samples with the reference's chunk API: in memory
+(``ChunkedSample``) and in the reference's on-disk format (``DiskSample``).
 
 The scattering entry point reads a sample only through this duck type
 (MOSAIC Sample.py:715-872): ``chunk_total``, ``chunk_atom_count(cid)``,
@@ -87,3 +88,92 @@ class ChunkedSample:
     @property
     def n_atoms(self):
         return sum(c[0].shape[0] for c in self._chunks)
+
+
+class DiskSample:
+    """A sample directory in the reference's on-disk format, read directly.
+
+    Layout (Sample.py:543-676, 735-872): ``sample_metadata.json`` (with
+    ``chunk_total`` and ``species_labels``), per chunk i (1-based)
+    ``atomic_positions_{i}.npy`` (N, 3) Angstrom and ``atomic_species_{i}.npy``
+    -- integer codes into ``species_labels``, or the labels themselves (files
+    written outside the sample's own directory). Position files are opened
+    memory-mapped; the atom count comes from the .npy header. The thermal
+    displacement, when given (dict(sigma=, max_displacement=, seed=), the
+    reference's ``temp_params`` for the Gaussian rule), is applied on every
+    load, as the reference does, with the same per-chunk generator.
+    """
+
+    def __init__(self, directory, thermal=None):
+        import json
+        import os
+        self.directory = str(directory)
+        path = os.path.join(self.directory, "sample_metadata.json")
+        with open(path) as fh:
+            meta = json.load(fh)
+        self.metadata = meta
+        self._chunk_total = int(meta.get("chunk_total") or 0)
+        self._labels = np.asarray(meta.get("species_labels") or [], dtype=str)
+        self.thermal = thermal
+        dims = meta.get("dimensions")
+        self.dimensions = tuple(dims) if dims is not None else None
+
+    def _path(self, stem, chunk_number):
+        import os
+        return os.path.join(self.directory, f"{stem}_{int(chunk_number)}.npy")
+
+    @property
+    def chunk_total(self):
+        return self._chunk_total
+
+    def chunk_atom_count(self, chunk_number):
+        return int(np.load(self._path("atomic_positions", chunk_number), mmap_mode="r").shape[0])
+
+    def load_chunk_positions(self, chunk_number, use_gpu=False, raw=False):
+        pos = np.load(self._path("atomic_positions", chunk_number))
+        if self.thermal and not raw:
+            t = self.thermal
+            return thermal_displacement(pos, t.get("sigma", 0.25), t.get("max_displacement", 1.0),
+                                        t.get("seed", 40), chunk_number)
+        return pos
+
+    def load_chunk_species(self, chunk_number, use_gpu=False, codes=False):
+        arr = np.load(self._path("atomic_species", chunk_number))
+        if arr.dtype.kind in "iu":
+            if arr.size and int(arr.max()) >= self._labels.size:
+                raise ValueError(f"species codes in chunk {chunk_number} exceed the label table "
+                                 f"({self._labels.size} labels) of sample_metadata.json")
+            return (arr, self._labels) if codes else self._labels[arr]
+        if codes:
+            labels, inv = np.unique(arr.astype(str), return_inverse=True)
+            return inv.reshape(-1).astype(np.uint8 if labels.size <= 256 else np.uint16), labels
+        return arr.astype(str)
+
+    @property
+    def n_atoms(self):
+        return sum(self.chunk_atom_count(c) for c in range(1, self._chunk_total + 1))
+
+
+def write_sample(directory, chunks, labels=None, dimensions=None):
+    """Write chunks in the on-disk format ``DiskSample`` reads: positions
+    float32 and species codes (uint8, or uint16 above 256 labels) with the
+    label table in ``sample_metadata.json``."""
+    import json
+    import os
+    os.makedirs(directory, exist_ok=True)
+    table = list(labels) if labels is not None else []
+    for i, (pos, spc) in enumerate(chunks, start=1):
+        labs, inv = np.unique(np.asarray(spc).astype(str), return_inverse=True)
+        for lab in labs:
+            if str(lab) not in table:
+                table.append(str(lab))
+        m = np.array([table.index(str(lab)) for lab in labs], dtype=np.int64)
+        codes = m[inv.reshape(-1)].astype(np.uint8 if len(table) <= 256 else np.uint16)
+        np.save(os.path.join(directory, f"atomic_positions_{i}.npy"),
+                np.ascontiguousarray(pos, dtype=np.float32))
+        np.save(os.path.join(directory, f"atomic_species_{i}.npy"), codes)
+    meta = {"dimensions": None if dimensions is None else [float(v) for v in dimensions],
+            "offset": None, "rotation": None, "chunk_total": len(chunks), "sample_type": None,
+            "species_labels": table}
+    with open(os.path.join(directory, "sample_metadata.json"), "w") as fh:
+        json.dump(meta, fh, indent=4)

@@ -71,20 +71,38 @@ def test_analyser_entry_point_matches_oracle(cuda, mode, accept, hw):
 
 
 def test_top_hat_edge_inside_tiles(cuda):
-    """A coarse detector whose acceptance edge crosses many pixels, large
-    tiles (1024 atoms): the split kernel's per-atom edge test in the tiles the
-    edge cuts, against the oracle."""
-    B, sample, D, stage, pos, spc = _setup(shape=(33, 31), pitch=2.0e5)
-    B._kernel_tile_atoms = 1024
-    acc = 2.2e-3
+    """The acceptance edge put through one pixel: the half-angle is that
+    pixel's angle from the axis as seen from the crystal's centre, so the edge
+    cuts its atoms (and the tiles they sit in) about in half. The split
+    kernel's per-atom edge test must match the oracle there, and that pixel
+    must keep a fraction of its intensity strictly between 0 and 1."""
+    B, sample, D, stage, pos, spc = _setup(shape=(33, 31))
+    B._kernel_tile_atoms = 256
+    ny, nz = D.shape
+    coords = np.asarray(D.pixel_coordinates, np.float64) / 1e10
+    p = (nz // 2 + 2) * ny + (ny // 2 + 3)
+    lab = (np.asarray(pos, np.float32) @ np.asarray(stage.rotation, np.float32).T +
+           np.asarray(stage.translation, np.float32)).astype(np.float64) / 1e10
+    centre = lab.mean(0)
+    axis = _axis(D)
+    axis = axis / np.linalg.norm(axis)
+    d = coords[:, p] - centre
+    d /= np.linalg.norm(d)
+    acc = 2.0 * np.arcsin(0.5 * np.linalg.norm(d - axis))
     kw = dict(apply_polarization=True, spherical_decay=True, return_double=True,
               analyser_mode="top-hat", analyser_acceptance_angle_rad=acc)
     ref = _oracle(B, D, stage, pos, spc, (1, _axis(D), acc, 0.0))
+    plain = _oracle(B, D, stage, pos, spc, None)
+    frac = abs(ref[p]) ** 2 / abs(plain[p]) ** 2
+    assert 0.02 < frac < 0.98, frac
     B._use_fast_kernel = True
     got = B.atomic_scattering_kinematic(sample, D, stage, **kw).reshape(-1)
     assert B.last_run["path"] == "split_f32"
     assert rel_intensity(got, ref) <= 1e-4, rel_intensity(got, ref)
-    assert np.count_nonzero(np.abs(ref) == 0) > 0
+    assert abs(abs(got[p]) ** 2 - abs(ref[p]) ** 2) <= 1e-4 * abs(plain[p]) ** 2
+    B._use_fast_kernel = False
+    got64 = B.atomic_scattering_kinematic(sample, D, stage, **kw).reshape(-1)
+    assert rel_max(got64, ref) <= 1e-6
 
 
 def test_darwin_declines_when_too_narrow(cuda):
@@ -98,9 +116,10 @@ def test_darwin_declines_when_too_narrow(cuda):
     assert B.last_run["path"] == "plain_f64" and "analyser_err" in B.last_run
 
 
-def test_analyser_rejected_by_the_scan_kernel(cuda):
-    """The batched scan kernel has no analyser: a request is an argument error,
-    not a silent drop."""
+def test_analyser_launch_shapes(cuda):
+    """The analyser kernels exist for 128/256 threads x 2/4 pixels: another
+    shape is an argument error (never a silent drop of the analyser); the
+    default shape runs."""
     from mosaic_gb300 import _lib
     B, sample, D, stage, pos, spc = _setup()
     atoms = B.stage_atoms(sample, stage)

@@ -1,0 +1,46 @@
+"""Streamed staging (chunks straight into device arrays through pinned
+buffers) and the on-disk sample format, on the GPU."""
+import numpy as np
+import pytest
+import torch
+
+from mosaic_gb300 import ChunkedSample, DiskSample, Detector, StaticStage, workloads, write_sample
+
+pytestmark = pytest.mark.gpu
+
+
+def _crystal():
+    rng = np.random.default_rng(5)
+    w = workloads.fcc_cu_32k(cells=8, npix=20)
+    pos = w.sample.load_chunk_positions(1)
+    spc = rng.choice(np.array(["Cu", "Ni", "Xx"]), size=pos.shape[0])   # Xx: no table, dropped
+    cut = [0, 700, 700, 1500, pos.shape[0]]                             # one empty chunk
+    return w, [(pos[a:b], spc[a:b]) for a, b in zip(cut[:-1], cut[1:])]
+
+
+def test_streamed_staging_equals_host_collection(cuda):
+    w, chunks = _crystal()
+    B = workloads._beam(10000.0, 200.0)
+    s = ChunkedSample(chunks, thermal=dict(sigma=0.08, max_displacement=1.0, seed=40))
+    pos_h, idx_h, labels_h = B.collect_atoms(s)
+    pos_d, idx_d, labels_d, counts = B.stream_atoms(s, cuda)
+    assert labels_d == labels_h
+    assert torch.equal(pos_d.cpu(), torch.as_tensor(pos_h))
+    assert torch.equal(idx_d.cpu(), torch.as_tensor(idx_h.astype(np.int32)))
+    assert np.array_equal(counts, np.bincount(idx_h, minlength=len(labels_h)))
+
+
+def test_disk_sample_through_the_entry_point(cuda, tmp_path):
+    w, chunks = _crystal()
+    write_sample(tmp_path, chunks)
+    th = dict(sigma=0.08, max_displacement=1.0, seed=40)
+    B = workloads._beam(10000.0, 200.0, pol_perp_rate=1.0)
+    D = Detector()
+    D.create_detector((24, 20), (5.5e5, 5.5e5))
+    D.position_detector_absolute(2.0e9, 2.0 * w.meta["theta_deg"], 0.0)
+    st = StaticStage(w.stage.rotation, w.stage.translation)
+    kw = dict(apply_polarization=True, return_double=True)
+    a = B.atomic_scattering_kinematic(DiskSample(tmp_path, thermal=th), D, st, **kw)
+    b = B.atomic_scattering_kinematic(ChunkedSample(chunks, thermal=th), D, st, **kw)
+    assert np.array_equal(a, b)
+    assert np.abs(a).max() > 0
