@@ -167,6 +167,34 @@ int mk_atoms_lab(int64_t n, const float *pos_in, const float *rot, const float *
                  const float *e0, int grid_ny, int grid_nz, const double *grid,
                  double *pos_lab, float *amp, void *stream);
 
+/* --- depth-dependent incident field (Beam.py:956-1045, 4963-5140,
+ * 5583-5618, 7118-7283) ---------------------------------------------------
+ * Column sums of the forward scattering factors on the beam grid (the
+ * transmission map's input, _compute_beam_column_A_map_*): every atom inside
+ * the grid deposits fwd[species] = (f0(0) + f', f'') with 3 x 3
+ * triangular-shaped-cloud weights around its grid position (+x beam:
+ * u = y, v = z). pos_lab: device (n, 3) float64 [m] from mk_atoms_lab;
+ * fwd: device (n_species, 2) float32; grid: host du, dv, uc, vc [A];
+ * sum_re, sum_im: device (grid_ny, grid_nz) float32, overwritten. */
+int mk_beam_column_sums(int64_t n, const double *pos_lab, const int *species, const float *fwd,
+                        int n_species, int grid_ny, int grid_nz, const double *grid,
+                        float *sum_re, float *sum_im, void *stream);
+/* Column sums -> tau = max(k beta, 0), phi = -k delta with
+ * delta, beta = r_e lambda^2 / (2 pi du dv) x sums (float32 maps). */
+int mk_beam_column_maps(int grid_ny, int grid_nz, const float *sum_re, const float *sum_im,
+                        double wavelength_A, double du_A, double dv_A, float *tau, float *phi,
+                        void *stream);
+/* tau, phi in place through A = exp(-tau + i phi): tau = -log(|A| + 1e-20),
+ * phi = arg A (the reference reads its maps back from the complex map). */
+int mk_beam_column_wrap(int grid_ny, int grid_nz, float *tau, float *phi, void *stream);
+/* Per-atom amplitude E0 exp(-f tau) exp(i f phi), E0, tau, phi sampled
+ * bilinearly at the atom's grid position, f = clip((x - s_min) /
+ * (s_max - s_min), 0, 1) its depth fraction along the +x beam; zero outside
+ * the grid. Overwrites amp (n, 2) float32. */
+int mk_atoms_ein_depth(int64_t n, const double *pos_lab, const float *e0, const float *tau,
+                       const float *phi, int grid_ny, int grid_nz, const double *grid,
+                       double s_min, double s_max, float *amp, void *stream);
+
 /* Bytes of workspace mk_tiles_build needs for n atoms. */
 size_t mk_tiles_workspace_size(int64_t n);
 /* Species-partitioned space-filling order and tile build. Replaces

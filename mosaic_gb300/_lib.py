@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas"
               "--expt-relaxed-constexpr"]
 # Per-source extra flags. The FP64 plain sum must not contract a*b+c into FMA:
 # it restates the uncontracted CPU arithmetic term for term.
-EXTRA = {"mk_sum_f64.cu": ["--fmad=false"]}
+EXTRA = {"mk_sum_f64.cu": ["--fmad=false"], "mk_depth.cu": ["--fmad=false"]}
 
 MK_OK, MK_EINVAL, MK_ENOMEM, MK_ETIMEOUT, MK_EDECLINE, MK_ECUDA = 0, -1, -2, -3, -4, -5
 MAX_SPECIES = 16
@@ -175,6 +175,14 @@ SIGNATURES = {
                                            ctypes.c_float, ctypes.c_int, _vp, _vp]),
     "mk_relu_backward": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp]),
     "mk_bias_grad": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    "mk_beam_column_sums": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, _vp, _vp, _vp, _vp]),
+    "mk_beam_column_maps": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, _vp, _vp, _vp]),
+    "mk_beam_column_wrap": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    "mk_atoms_ein_depth": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int,
+                                          ctypes.c_int, _vp, ctypes.c_double, ctypes.c_double, _vp,
+                                          _vp]),
     "mk_mse": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp]),
     "mk_mse_weighted": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _vp, _vp, _vp, _vp, _vp,
                                        _vp, _vp]),

@@ -310,6 +310,28 @@ class beam:
                                 e0=self._beam_E0_map, grid=self._beam_grid(), device=device,
                                 counts=counts)
 
+    def apply_depth_ein(self, atoms, kernel_radius=0):
+        """Depth-dependent incident field (Beam.py:4963-5140): the transmission
+        maps of the staged sample itself, its depth window, and the per-atom
+        amplitudes E0 exp(-f tau) exp(i f phi), in place on ``atoms``.
+        Returns (tau, phi, (s_min, s_max))."""
+        self._require_forward_beam()
+        tau, phi = engine.depth_maps(atoms, self._beam_E0_map.shape, self._beam_grid(),
+                                     self._wavelength * 1e10, kernel_radius)
+        s_min, s_max = engine.depth_bounds(atoms)
+        engine.ein_depth(atoms, self._beam_E0_map, self._beam_grid(), tau, phi, s_min, s_max)
+        return tau, phi, (s_min, s_max)
+
+    def depth_ein_maps(self, sample, stage, kernel_radius=0):
+        """The transmission map A(u, v) = exp(-tau + i phi) (complex64 host,
+        _compute_beam_column_A_map_*, Beam.py:7118-7283) and the depth window
+        (_compute_global_depth_bounds, Beam.py:5583-5618) of a sample."""
+        atoms = self.stage_atoms(sample, stage)
+        tau, phi = engine.depth_maps(atoms, self._beam_E0_map.shape, self._beam_grid(),
+                                     self._wavelength * 1e10, kernel_radius, wrap=False)
+        A = torch.polar(torch.exp(-tau.double()), phi.double()).to(torch.complex64)
+        return A.cpu().numpy(), engine.depth_bounds(atoms)
+
     def physics(self, apply_polarization=False, spherical_decay=False, remove_forward=False,
                 beam_dir=(1.0, 0.0, 0.0), pol=None, analyser=None):
         return engine.physics(self.k, beam_dir, apply_polarization,
@@ -395,8 +417,6 @@ class beam:
         kernel's analyser factor (Beam.py:2350-2378) about the axis from the
         origin to the detector's centre pixel (Beam.py:6127-6131)."""
         kind = engine.analyser_kind(analyser_mode)
-        if use_depth_ein:
-            raise NotImplementedError("depth-dependent E_in (absorption maps) is not provided")
         if not torch.cuda.is_available():
             raise RuntimeError("interact_beam_gpu: no CUDA GPU (this library has no CPU path)")
         self._require_forward_beam()
@@ -414,6 +434,10 @@ class beam:
                         float(analyser_darwin_halfwidth_rad))
         phys = self.physics(apply_polarization, spherical_decay, remove_forward, analyser=analyser)
         atoms = self.stage_atoms(sample, stage)
+        if use_depth_ein:
+            # computed on the device for every call; the reference's on-disk
+            # cache (ein_cache_dir, recompute_cache) has nothing to save here
+            self.apply_depth_ein(atoms)
         pix = engine.Pixels(coords.astype(np.float64) / 1e10, Ny, Nz, phys)
         out = self.scatter_device(atoms, pix, phys)
         engine.sync()

@@ -232,6 +232,83 @@ def atoms_lab(pos_A, species_idx, rot, trans, table, e0=None, grid=None, device=
     return Atoms(pos, sp, amp, np.asarray(counts, dtype=np.int64), table)
 
 
+def depth_forward_factors(table):
+    """(S, 2) float32 per species: f0(0) + f' and f'' (the forward factors of
+    the transmission map, summed in float32 as Beam.py:7190-7197 does)."""
+    re = table.f0z.astype(np.float32) + table.anom.real.astype(np.float32)
+    return np.stack([re, table.anom.imag.astype(np.float32)], 1).astype(np.float32)
+
+
+def _gauss_blur(m, rad):
+    """Circular convolution with the reference's (2 rad + 1)^2 Gaussian placed
+    at the map's corner (np.fft.fft2(k, s=shape), Beam.py:7268-7277)."""
+    sig = rad / 2.0
+    y, x = np.ogrid[-rad:rad + 1, -rad:rad + 1]
+    k = np.exp(-(x * x + y * y) / (2.0 * sig * sig)).astype(np.float32)
+    k /= k.sum()
+    K = torch.zeros(m.shape, dtype=torch.float64, device=m.device)
+    K[: 2 * rad + 1, : 2 * rad + 1] = torch.as_tensor(k.astype(np.float64))
+    out = torch.fft.ifft2(torch.fft.fft2(m.double()) * torch.fft.fft2(K)).real
+    return out.float().contiguous()
+
+
+def depth_maps(atoms, grid_shape, grid, wavelength_A, kernel_radius=0, wrap=True, stream=None):
+    """Attenuation and phase maps (tau, phi) of the whole sample on the beam
+    grid, float32 device (NyB, NzB): column sums of the atoms' forward
+    factors (mk_beam_column_sums), tau/phi (mk_beam_column_maps), the
+    optional Gaussian blur of radius ``kernel_radius`` pixels, and with
+    ``wrap`` the round trip through A = exp(-tau + i phi) the per-atom field
+    reads (mk_beam_column_wrap)."""
+    L = _require_cuda()
+    ny, nz = int(grid_shape[0]), int(grid_shape[1])
+    dev = atoms.pos.device
+    f32 = dict(dtype=torch.float32, device=dev)
+    sr, si = torch.empty((ny, nz), **f32), torch.empty((ny, nz), **f32)
+    fwd = torch.as_tensor(depth_forward_factors(atoms.table)).to(dev)
+    g = np.ascontiguousarray(grid, dtype=np.float64)
+    gp = g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    sh = _stream_handle(stream)
+    check(L.mk_beam_column_sums(atoms.n, _ptr(atoms.pos), _ptr(atoms.species), _ptr(fwd),
+                                int(fwd.shape[0]), ny, nz, gp, _ptr(sr), _ptr(si), sh))
+    tau, phi = torch.empty((ny, nz), **f32), torch.empty((ny, nz), **f32)
+    check(L.mk_beam_column_maps(ny, nz, _ptr(sr), _ptr(si), float(wavelength_A), float(g[0]),
+                                float(g[1]), _ptr(tau), _ptr(phi), sh))
+    if int(kernel_radius) > 0:
+        rad = int(kernel_radius)
+        if 2 * rad + 1 > min(ny, nz):
+            raise ValueError(f"blur radius {rad} does not fit the {ny} x {nz} beam grid")
+        phi = _gauss_blur(phi, rad)
+        tau = torch.clamp_min(_gauss_blur(tau, rad), 0.0).contiguous()
+    if wrap:
+        check(L.mk_beam_column_wrap(ny, nz, _ptr(tau), _ptr(phi), sh))
+    return tau, phi
+
+
+def depth_bounds(atoms):
+    """Front and back of the sample along the +x beam [A] as the float32 lab
+    x the stage transform produced (Beam.py:5583-5618); (0, 1) when flat."""
+    if atoms.n == 0:
+        return 0.0, 1.0
+    x = atoms.pos[:, 0]
+    lo = float(np.float32(float(x.min()) * 1e10))
+    hi = float(np.float32(float(x.max()) * 1e10))
+    return (lo, hi) if hi > lo else (0.0, 1.0)
+
+
+def ein_depth(atoms, e0, grid, tau, phi, s_min, s_max, stream=None):
+    """Overwrite the atoms' amplitudes with the depth-dependent incident field
+    (mk_atoms_ein_depth)."""
+    L = _require_cuda()
+    e0_t = torch.view_as_real(torch.as_tensor(np.ascontiguousarray(e0, dtype=np.complex64))).to(
+        atoms.pos.device)
+    g = np.ascontiguousarray(grid, dtype=np.float64)
+    check(L.mk_atoms_ein_depth(atoms.n, _ptr(atoms.pos), _ptr(e0_t), _ptr(tau), _ptr(phi),
+                               int(tau.shape[0]), int(tau.shape[1]),
+                               g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), float(s_min),
+                               float(s_max), _ptr(atoms.amp), _stream_handle(stream)))
+    return atoms
+
+
 class Tiles:
     """Species-partitioned, Morton-ordered atom tiles (mk_tiles_build)."""
 

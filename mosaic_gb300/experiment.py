@@ -18,6 +18,8 @@ import copy
 
 import numpy as np
 
+from . import engine
+from .geometry import StaticStage
 from .scan import BatchedScan, Frame, roi_indices
 
 DET_AXES = {"two_theta": "two_theta", "2theta": "two_theta", "tth": "two_theta", "eta": "eta",
@@ -137,12 +139,29 @@ def scan_nD(sample, beam, detector, stage, ranges, stepsizes, motors, degrees=Tr
     if optics is not None:
         raise NotImplementedError("optics stacks per scan step are not provided")
     kw = dict(apply_polarization=False, spherical_decay=False, remove_forward=False)
-    kw.update({k: v for k, v in (adi_kwargs or {}).get("sc_kwargs", {}).items() if k in kw})
+    sc = dict((adi_kwargs or {}).get("sc_kwargs", {}))
+    kw.update({k: v for k, v in sc.items() if k in kw})
     axes, shape, frames = scan_frames(detector, stage, ranges, stepsizes, motors, degrees,
                                       scan_mode, couplings, rois)
-    scan = BatchedScan(beam, sample, frames, **kw)
-    scan.run()
-    sums = scan.sum_intensity().reshape(shape)
+    per_frame = bool(sc.get("use_depth_ein")) or engine.analyser_kind(sc.get("analyser_mode"))
+    scan = None
+    if per_frame:
+        # The analyser and the depth-dependent field change with every pose:
+        # one exposure per step through the single-exposure kernels, as the
+        # reference's own scan loop does (Experiment.py:285-336).
+        one = {k: sc[k] for k in ("analyser_mode", "analyser_acceptance_angle_rad",
+                                  "analyser_darwin_halfwidth_rad", "use_depth_ein") if k in sc}
+        sums = np.empty(len(frames))
+        for i, f in enumerate(frames):
+            st = StaticStage(f.rotation, f.translation)
+            A = beam.interact_beam_gpu(sample, np.asarray(f.pixels), f.shape, st,
+                                       return_double=True, **kw, **one)
+            sums[i] = float((np.abs(A) ** 2).sum())
+        sums = sums.reshape(shape)
+    else:
+        scan = BatchedScan(beam, sample, frames, **kw)
+        scan.run()
+        sums = scan.sum_intensity().reshape(shape)
     if step_callback is not None:
         for k, idx in enumerate(np.ndindex(*shape)):
             step_callback({"step": k + 1, "total": len(frames), "index": tuple(int(i) for i in idx),

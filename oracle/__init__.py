@@ -208,14 +208,118 @@ def ein_bilinear(pos, E0, du, dv, uc, vc, e1=(0, 1, 0), e2=(0, 0, 1)):
     return out
 
 
+def ein_depth(pos, E0, tau, phi, du, dv, uc, vc, s_min, s_max, e1=(0, 1, 0), e2=(0, 0, 1),
+              khat=(1, 0, 0)):
+    """Per-atom incident amplitude with the depth-dependent transmission
+    (Beam.py:956-1045): E0, tau and phi sampled bilinearly at the atom's
+    beam-grid position, Ein = E0 exp(-f tau) exp(i f phi) with
+    f = clip((khat.pos - s_min) / (s_max - s_min), 0, 1); zero outside the
+    grid. float32 arithmetic in the reference's order."""
+    pos = np.asarray(pos, dtype=np.float32)
+    e1, e2, khat = (np.asarray(v, dtype=np.float32) for v in (e1, e2, khat))
+    N = pos.shape[0]
+    out = np.zeros(N, dtype=np.complex64)
+    NyB, NzB = E0.shape
+    au = pos[:, 0] * e1[0] + pos[:, 1] * e1[1] + pos[:, 2] * e1[2]
+    av = pos[:, 0] * e2[0] + pos[:, 1] * e2[1] + pos[:, 2] * e2[2]
+    iu = au / float(du) + float(uc)
+    iv = av / float(dv) + float(vc)
+    inb = (iu >= 0.0) & (iu <= NyB - 1) & (iv >= 0.0) & (iv <= NzB - 1)
+    if not np.any(inb):
+        return out
+    iu, iv = iu[inb], iv[inb]
+    i0 = np.floor(iu).astype(np.int64)
+    j0 = np.floor(iv).astype(np.int64)
+    i1 = np.clip(i0 + 1, 0, NyB - 1)
+    j1 = np.clip(j0 + 1, 0, NzB - 1)
+    fu = (iu - i0).astype(np.float32)
+    fv = (iv - j0).astype(np.float32)
+    w00, w01, w10, w11 = (1 - fu) * (1 - fv), (1 - fu) * fv, fu * (1 - fv), fu * fv
+    r00, r01, r10, r11 = i0 * NzB + j0, i0 * NzB + j1, i1 * NzB + j0, i1 * NzB + j1
+    tf = np.asarray(tau, np.float32).ravel()
+    pf = np.asarray(phi, np.float32).ravel()
+    Ef = np.asarray(E0, dtype=np.complex64).ravel()
+    tau_s = tf[r00] * w00 + tf[r01] * w01 + tf[r10] * w10 + tf[r11] * w11
+    phi_s = pf[r00] * w00 + pf[r01] * w01 + pf[r10] * w10 + pf[r11] * w11
+    E0_s = Ef[r00] * w00 + Ef[r01] * w01 + Ef[r10] * w10 + Ef[r11] * w11
+    s_vals = pos[inb, 0] * khat[0] + pos[inb, 1] * khat[1] + pos[inb, 2] * khat[2]
+    denom = float(s_max) - float(s_min)
+    if not denom > 0.0:
+        denom = 1.0
+    f = np.clip((s_vals - float(s_min)) / denom, 0.0, 1.0).astype(np.float32)
+    amp = np.exp(-f * tau_s).astype(np.float32)
+    ph = f * phi_s
+    c, sn = np.cos(ph), np.sin(ph)
+    re = (E0_s.real * c - E0_s.imag * sn) * amp
+    im = (E0_s.real * sn + E0_s.imag * c) * amp
+    out[inb] = (re + 1j * im).astype(np.complex64)
+    return out
+
+
+def column_map(lab_A, fwd_re, fwd_im, grid_shape, du, dv, uc, vc, wavelength_A,
+               e1=(0, 1, 0), e2=(0, 0, 1)):
+    """Transmission map A(u, v) = exp(-tau + i phi) of the sample on the beam
+    grid (Beam.py:7118-7283): each atom's forward factors f0(0) + f' and f''
+    deposited with 3 x 3 triangular-shaped-cloud weights around its grid
+    position, column sums -> phi = -k delta, tau = max(k beta, 0) with
+    delta, beta = r_e lambda^2 / (2 pi du dv) x sums. lab_A (N, 3) float32
+    Angstrom (after the stage transform); returns complex64 (NyB, NzB)."""
+    NyB, NzB = grid_shape
+    pos = np.asarray(lab_A, dtype=np.float32)
+    e1 = np.asarray(e1, dtype=np.float64)
+    e2 = np.asarray(e2, dtype=np.float64)
+    sr = np.zeros((NyB, NzB), np.float32)
+    si = np.zeros((NyB, NzB), np.float32)
+
+    def tsc(d):
+        w = np.zeros_like(d, dtype=np.float32)
+        m0 = d <= 0.5
+        w[m0] = 0.75 - d[m0] * d[m0]
+        m1 = (~m0) & (d <= 1.5)
+        t = 1.5 - d[m1]
+        w[m1] = 0.5 * t * t
+        return w
+
+    au = pos[:, 0] * e1[0] + pos[:, 1] * e1[1] + pos[:, 2] * e1[2]
+    av = pos[:, 0] * e2[0] + pos[:, 1] * e2[1] + pos[:, 2] * e2[2]
+    iu = au / du + uc
+    iv = av / dv + vc
+    inb = (iu >= 0.0) & (iu <= NyB - 1) & (iv >= 0.0) & (iv <= NzB - 1)
+    if np.any(inb):
+        iu, iv = iu[inb], iv[inb]
+        fr = np.asarray(fwd_re, np.float32)[inb]
+        fi = np.asarray(fwd_im, np.float32)[inb]
+        ic = np.floor(iu + 0.5).astype(np.int64)
+        jc = np.floor(iv + 0.5).astype(np.int64)
+        for dx in (-1, 0, 1):
+            wx = tsc(np.abs(iu - (ic + dx)))
+            for dy in (-1, 0, 1):
+                wy = tsc(np.abs(iv - (jc + dy)))
+                fac = wx * wy
+                ii, jj = ic + dx, jc + dy
+                m = (ii >= 0) & (ii < NyB) & (jj >= 0) & (jj < NzB) & (fac > 0.0)
+                idx = ii[m] * NzB + jj[m]
+                np.add.at(sr.ravel(), idx, (fr[m] * fac[m]).astype(np.float32))
+                np.add.at(si.ravel(), idx, (fi[m] * fac[m]).astype(np.float32))
+    r_e_A = 2.81794092e-5
+    C = (r_e_A * wavelength_A * wavelength_A) / (2.0 * np.pi * du * dv)
+    kA = 2.0 * np.pi / wavelength_A
+    phi = (-kA * (C * sr)).astype(np.float32)
+    tau = np.maximum((kA * (C * si)).astype(np.float32), np.float32(0.0))
+    return np.exp(-tau + 1j * phi).astype(np.complex64)
+
+
 def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV,
                  f0_rows, f0_zero, f1f2_tables, E0, beam_grid, pol_state,
                  remove_forward=False, apply_polarization=False,
-                 spherical_decay=False, dw_b=None, n_threads=None, analyser=None):
-    """Restatement of ``interact_beam_cpu`` (Beam.py:5773-5956) for E0-only
-    incident fields, returning complex128 (Nz, Ny). ``analyser`` (see
-    ``scatter_f64``) adds the GPU general kernel's analyser factor, which the
-    reference's CPU path does not apply.
+                 spherical_decay=False, dw_b=None, n_threads=None, analyser=None,
+                 depth=False):
+    """Restatement of ``interact_beam_cpu`` (Beam.py:5773-5956), returning
+    complex128 (Nz, Ny). ``analyser`` (see ``scatter_f64``) adds the GPU
+    general kernel's analyser factor, which the reference's CPU path does not
+    apply. ``depth`` uses the depth-dependent incident field
+    (Beam.py:4963-5140: transmission map of the whole sample, global depth
+    window, ``ein_depth``) instead of E0 alone.
 
     chunks: iterable of (positions (N,3) float32 A, species labels (N,)).
     beam_grid: (du, dv, uc, vc). f0_rows: element -> (11,) float32;
@@ -230,6 +334,33 @@ def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV
     R = np.asarray(rotation, dtype=np.float32)
     T = np.asarray(translation, dtype=np.float32)
     du, dv, uc, vc = beam_grid
+    tau_d = phi_d = None
+    if depth:
+        labs, fr_all, fi_all = [], [], []
+        for pos, spc in chunks:
+            pos = np.asarray(pos, dtype=np.float32)
+            if pos.shape[0] == 0:
+                continue
+            spc = np.asarray(spc).astype(str)
+            lab = (pos @ R.T + T).astype(np.float32)
+            fr = np.zeros(pos.shape[0], np.float32)
+            fi = np.zeros(pos.shape[0], np.float32)
+            for el in np.unique(spc):
+                m = spc == el
+                c = anomalous(energy_eV, f1f2_tables[el]) if el in f1f2_tables else 0j
+                fr[m] = np.float32(f0_zero.get(el, 0.0)) + np.float32(c.real)
+                fi[m] = np.float32(c.imag)
+            labs.append(lab)
+            fr_all.append(fr)
+            fi_all.append(fi)
+        lab_all = np.concatenate(labs)
+        A = column_map(lab_all, np.concatenate(fr_all), np.concatenate(fi_all), E0.shape,
+                       du, dv, uc, vc, lam * 1e10)
+        tau_d = (-np.log(np.abs(A) + np.float32(1e-20))).astype(np.float32)
+        phi_d = np.angle(A).astype(np.float32)
+        s_min, s_max = float(lab_all[:, 0].min()), float(lab_all[:, 0].max())
+        if not s_max > s_min:
+            s_min, s_max = 0.0, 1.0
     for pos, spc in chunks:
         pos = np.asarray(pos, dtype=np.float32)
         spc = np.asarray(spc).astype(str)
@@ -237,7 +368,8 @@ def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV
         if n == 0:
             continue
         lab = (pos @ R.T + T).astype(np.float32)
-        amp = ein_bilinear(lab, E0, du, dv, uc, vc)
+        amp = (ein_depth(lab, E0, tau_d, phi_d, du, dv, uc, vc, s_min, s_max) if depth
+               else ein_bilinear(lab, E0, du, dv, uc, vc))
         wk = np.zeros((n, 11), np.float32)
         f0z = np.zeros(n, np.float32)
         ar = np.zeros(n, np.float32)

@@ -2,7 +2,7 @@
 
 Run in a container where the reference MOSAIC checkout is importable:
 
-    python tests/golden/make_golden.py /path/to/MOSAIC
+    python tests/golden/make_golden.py /path/to/MOSAIC [--only-depth]
 
 The reference imports pandas for two helpers only; pandas is not installed
 here, so ``_shim/pandas.py`` supplies ``unique``/``factorize``/``DataFrame``
@@ -13,7 +13,8 @@ reference's own code: its cffi C kernel ``compute_scattering_cffi``
 (Beam.py:503-615), ``_ein_bilinear_cpu`` (Beam.py:956-1045), the polarization
 state (Beam.py:31-47, 117-149), detector placement (Detector.py:73-741), stage
 rotations (Stage.py:252-382), the Gaussian thermal draw (Sample.py:2084-2156,
-2321-2334) and the free-space propagator (Beam.py:4622-4900, 7945-8022).
+2321-2334), the free-space propagator (Beam.py:4622-4900, 7945-8022) and the
+depth-dependent incident field (Beam.py:956-1045, 5583-5618, 7118-7283).
 
 The fixtures are small .npz files; the GPU machine never needs the reference.
 """
@@ -248,8 +249,69 @@ def main(ref_dir: str) -> None:
         prop[f"asp{i}"] = B._angular_spectrum_propagate_cpu(field, dy, dy, zz, plib, pffi)
         prop[f"aspcase{i}"] = np.array([dy, zz])
     np.savez_compressed(os.path.join(HERE, "propagation.npz"), **prop)
+    depth_ein(B)
     print("golden fixtures written to", HERE)
 
 
+class _Sample:
+    """Minimal chunk duck type for the reference's depth-Ein helpers."""
+
+    def __init__(self, chunks):
+        self.chunks = chunks
+        self.chunk_total = len(chunks)
+
+    def load_chunk_positions(self, cid, use_gpu=False, raw=False):
+        return self.chunks[cid - 1][0].copy()
+
+    def load_chunk_species(self, cid, use_gpu=False, codes=False):
+        return self.chunks[cid - 1][1].copy()
+
+
+class _Stage:
+    def __init__(self, R, T):
+        self.rotation = R
+        self.translation = T
+
+
+def depth_ein(B):
+    """Depth-dependent incident field: the reference's transmission map
+    (_compute_beam_column_A_map_cpu, Beam.py:7118-7283), depth window
+    (_compute_global_depth_bounds, Beam.py:5583-5618) and per-atom Ein
+    (_ein_bilinear_cpu, Beam.py:956-1045) on a small gold/iron slab."""
+    rng = np.random.default_rng(4963)
+    a = 4.078
+    cells = np.stack(np.meshgrid(np.arange(30), np.arange(10), np.arange(10), indexing="ij"), -1)
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    pos = ((cells.reshape(-1, 1, 3) + basis[None]) * a).reshape(-1, 3)
+    pos = (pos - pos.mean(0)).astype(np.float32)
+    spc = np.where(rng.random(pos.shape[0]) < 0.8, "Au", "Fe")
+    half = pos.shape[0] // 2
+    sample = _Sample([(pos[:half], spc[:half]), (pos[half:], spc[half:])])
+    c, s_ = np.cos(np.radians(3.0)), np.sin(np.radians(3.0))
+    R = np.array([[c, -s_, 0], [s_, c, 0], [0, 0, 1]], np.float32)
+    T = np.array([1.5, -2.0, 0.5], np.float32)
+    stage = _Stage(R, T)
+    B.create_beam(10000.0, beam_size=(60.0, 60.0), beam_samples=(61, 61))
+    A = B._compute_beam_column_A_map_cpu(sample, stage)
+    s_min, s_max = B._compute_global_depth_bounds(sample, stage)
+    tau = (-np.log(np.abs(A) + np.float32(1e-20))).astype(np.float32)
+    phi = np.angle(A).astype(np.float32)
+    lab = (pos @ R.T + T).astype(np.float32)
+    ein = B._ein_bilinear_cpu(lab, tau, phi, B._beam_E0_map.astype(np.complex64),
+                              B._beam_e1.astype(np.float32), B._beam_e2.astype(np.float32),
+                              np.array([1, 0, 0], np.float32), B._beam_du, B._beam_dv,
+                              B._beam_uc, B._beam_vc, s_min, s_max)
+    np.savez_compressed(os.path.join(HERE, "depth_ein.npz"), pos=pos, spc=spc, R=R, T=T,
+                        grid=np.array([B._beam_du, B._beam_dv, B._beam_uc, B._beam_vc]),
+                        E0=B._beam_E0_map, A=A, s=np.array([s_min, s_max]), ein=ein,
+                        wavelength=np.array(B._wavelength), energy=np.array(B._energy))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 2 and sys.argv[2] == "--only-depth":
+        sys.path[:0] = [os.path.join(HERE, "_shim"), ref]
+        import Beam  # noqa: E402
+        depth_ein(Beam.beam(directory=tempfile.mkdtemp(prefix="mosaic_golden_")))
+    else:
+        main(ref)

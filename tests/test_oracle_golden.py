@@ -88,3 +88,31 @@ def test_oracle_prop_mul_matches_reference(golden):
         # the reference evaluates the phase in float32 (cosf/sinf)
         scale = np.abs(d["Fs"]).max()
         assert np.abs(got - ref).max() / scale <= 5e-5, i
+
+
+def test_depth_ein_oracle_matches_reference(golden):
+    """Transmission map, depth window and depth-dependent Ein of a gold/iron
+    slab, against the reference's own outputs (Beam.py:956-1045, 5583-5618,
+    7118-7283)."""
+    d = golden("depth_ein.npz")
+    t = golden("tables.npz")
+    els = list(t["tab_elements"])
+    e_idx = list(t["tab_energies"]).index(float(d["energy"]))
+    spc = d["spc"].astype(str)
+    fr = np.zeros(spc.size, np.float32)
+    fi = np.zeros(spc.size, np.float32)
+    for el in ("Au", "Fe"):
+        m = spc == el
+        c = t["tab_anom"][els.index(el), e_idx]
+        fr[m] = np.float32(t["tab_f0z"][els.index(el)]) + np.float32(c.real)
+        fi[m] = np.float32(c.imag)
+    lab = (d["pos"] @ d["R"].T + d["T"]).astype(np.float32)
+    du, dv, uc, vc = d["grid"]
+    A = oracle.column_map(lab, fr, fi, d["A"].shape, du, dv, uc, vc, float(d["wavelength"]) * 1e10)
+    ref = d["A"]
+    assert np.allclose(A, ref, rtol=0, atol=2e-6), np.abs(A - ref).max()
+    assert np.allclose([lab[:, 0].min(), lab[:, 0].max()], d["s"], rtol=0, atol=1e-5)
+    tau = (-np.log(np.abs(ref) + np.float32(1e-20))).astype(np.float32)
+    phi = np.angle(ref).astype(np.float32)
+    ein = oracle.ein_depth(lab, d["E0"], tau, phi, du, dv, uc, vc, d["s"][0], d["s"][1])
+    assert np.allclose(ein, d["ein"], rtol=0, atol=1e-6 * np.abs(d["ein"]).max())
