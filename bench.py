@@ -45,6 +45,7 @@ sys.path.insert(0, HERE)
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 MUFU_PER_CLK_SM = 16        # sin/cos results per clock per SM (MUFU)
 FP32_PER_CLK_SM = 128
+METRIC = "Gatom*pixel/s (kinematic sum, FP32 split-phase) vs FP64 plain on 1 GB300"
 MUFU_PER_TERM, FP32_PER_TERM = 2, 12   # canonical split-phase term
 # pixel-pair form: one sin/cos per two terms; per pair 22 FP32-pipe ops (two
 # 3-term dot products, rounding 2, scale 1, delta^2 1, cos/sin polynomials 6,
@@ -266,10 +267,14 @@ def run_reference(args):
         if i >= args.warmup:
             steps.append(r)
     val = float(np.median([s["value"] for s in steps]))
-    line = {"impl": "reference", "metric": "Gatom*pixel/s (kinematic sum)", "value": val,
+    line = {"impl": "reference", "metric": METRIC, "value": val,
             "unit": "Gatom*pixel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.config, "host_cores": threads},
+            "config": {"workload": args.config, "atoms": int(sum(w.sample.chunk_atom_count(c)
+                                                                  for c in range(1, w.sample.chunk_total + 1))),
+                       "pixels": int(np.prod(w.detector.shape)), "host_cores": threads,
+                       "sample": "one chunk x central 16x16 pixels per step (terms/s is linear in atoms "
+                                 "and pixels)"},
             "cpu_baseline": {"value": val, "unit": "Gatom*pixel/s", "cores": threads,
                              "kind": "port", "sample": steps[-1]["sample"]},
             "e2e": {"value": val, "unit": "Gatom*pixel/s", "h2d_bytes_per_step": 0,
@@ -431,7 +436,7 @@ def run_ours(args):
     if rank == 0:
         cpu = cpu_baseline(w) if not args.no_cpu else None
         line = {
-            "metric": "Gatom*pixel/s (kinematic sum, FP32 split-phase) vs FP64 plain on 1 GB300",
+            "metric": METRIC,
             "value": value, "unit": "Gatom*pixel/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 origins and reduction)",

@@ -256,8 +256,20 @@ def ein_depth(pos, E0, tau, phi, du, dv, uc, vc, s_min, s_max, e1=(0, 1, 0), e2=
     return out
 
 
+def blur_map(m, rad):
+    """The reference's optional Gaussian blur of tau and phi (Beam.py:7268-7277):
+    a (2 rad + 1)^2 Gaussian of sigma rad / 2, zero-padded at the map's corner,
+    applied by FFT (circular)."""
+    sig = rad / 2.0
+    y, x = np.ogrid[-rad:rad + 1, -rad:rad + 1]
+    k = np.exp(-(x * x + y * y) / (2.0 * sig * sig)).astype(np.float32)
+    k /= k.sum()
+    Fk = np.fft.fft2(k, s=m.shape)
+    return np.fft.ifft2(np.fft.fft2(m) * Fk).real.astype(np.float32)
+
+
 def column_map(lab_A, fwd_re, fwd_im, grid_shape, du, dv, uc, vc, wavelength_A,
-               e1=(0, 1, 0), e2=(0, 0, 1)):
+               e1=(0, 1, 0), e2=(0, 0, 1), kernel_radius=0):
     """Transmission map A(u, v) = exp(-tau + i phi) of the sample on the beam
     grid (Beam.py:7118-7283): each atom's forward factors f0(0) + f' and f''
     deposited with 3 x 3 triangular-shaped-cloud weights around its grid
@@ -306,6 +318,9 @@ def column_map(lab_A, fwd_re, fwd_im, grid_shape, du, dv, uc, vc, wavelength_A,
     kA = 2.0 * np.pi / wavelength_A
     phi = (-kA * (C * sr)).astype(np.float32)
     tau = np.maximum((kA * (C * si)).astype(np.float32), np.float32(0.0))
+    if kernel_radius > 0:
+        phi = blur_map(phi, int(kernel_radius))
+        tau = np.maximum(blur_map(tau, int(kernel_radius)), np.float32(0.0))
     return np.exp(-tau + 1j * phi).astype(np.complex64)
 
 

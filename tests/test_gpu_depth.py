@@ -46,13 +46,19 @@ def test_depth_maps_and_field_match_reference(cuda, golden):
 
 @pytest.mark.parametrize("fast", [False, True])
 def test_depth_entry_point_matches_oracle(cuda, fast):
+    """An 80 x 6 x 6-cell Cu/Au slab (~290 A long) at the (111) Bragg setting:
+    its own transmission moves the incident phase by a few 1e-2 rad."""
     rng = np.random.default_rng(7)
     w = workloads.fcc_cu_32k(cells=8, npix=20)
-    pos = w.sample.load_chunk_positions(1)
+    a = w.meta["a"]
+    cells = np.stack(np.meshgrid(np.arange(80), np.arange(6), np.arange(6), indexing="ij"), -1)
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    pos = ((cells.reshape(-1, 1, 3) + basis[None]) * a).reshape(-1, 3)
+    pos = (pos - pos.mean(0)).astype(np.float32)
     spc = rng.choice(np.array(["Cu", "Au"]), size=pos.shape[0])
     half = pos.shape[0] // 2
     sample = ChunkedSample([(pos[:half], spc[:half]), (pos[half:], spc[half:])])
-    B = workloads._beam(10000.0, 200.0, pol_perp_rate=1.0)
+    B = workloads._beam(10000.0, 600.0, pol_perp_rate=1.0)
     D = Detector()
     D.create_detector((24, 20), (5.5e5, 5.5e5))
     D.position_detector_absolute(2.0e9, 2.0 * w.meta["theta_deg"], 0.0)
@@ -67,7 +73,7 @@ def test_depth_entry_point_matches_oracle(cuda, fast):
             B._beam_grid(), B._polarization_state())
     ref = oracle.interact_cpu(*args, apply_polarization=True, depth=True).reshape(-1)
     flat = oracle.interact_cpu(*args, apply_polarization=True).reshape(-1)
-    assert rel_intensity(flat, ref) > 1e-3          # the depth field changes the pattern
+    assert rel_intensity(flat, ref) > 1.5e-3        # the depth field changes the pattern
     if fast:
         assert rel_intensity(got, ref) <= 1e-4, rel_intensity(got, ref)
     else:

@@ -52,3 +52,23 @@ def test_scan_graph_replay_is_bitwise(cuda):
     import torch
     torch.cuda.synchronize()
     assert torch.equal(scan.out, first)
+
+
+def test_scan_nd_batched_and_per_step_paths_agree(cuda):
+    """scan_nD runs in one batched launch; with an analyser it runs one
+    exposure per step instead (the analyser follows the pose). An analyser
+    that accepts every direction (half-angle pi) must then give the batched
+    sums; a narrow one must take intensity away."""
+    from mosaic_gb300 import experiment
+    w = workloads.fcc_cu_32k(cells=8, npix=32)
+    th = w.meta["theta_deg"]
+    args = (w.sample, w.beam, w.detector, w.stage, [(th - 0.4, th + 0.4)], [0.2], ["mu"])
+    kw = dict(apply_polarization=True, spherical_decay=False, remove_forward=False)
+    base = experiment.scan_nD(*args, adi_kwargs=dict(sc_kwargs=kw))["sum_intensity"]
+    wide = experiment.scan_nD(*args, adi_kwargs=dict(sc_kwargs=dict(
+        kw, analyser_mode="top-hat", analyser_acceptance_angle_rad=np.pi)))["sum_intensity"]
+    assert base.shape == wide.shape == (5,)
+    assert np.allclose(wide, base, rtol=1e-4, atol=0), (wide, base)
+    narrow = experiment.scan_nD(*args, adi_kwargs=dict(sc_kwargs=dict(
+        kw, analyser_mode="top-hat", analyser_acceptance_angle_rad=2e-4)))["sum_intensity"]
+    assert np.all(narrow < 0.9 * base) and np.all(narrow > 0)

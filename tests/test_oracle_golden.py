@@ -116,3 +116,15 @@ def test_depth_ein_oracle_matches_reference(golden):
     phi = np.angle(ref).astype(np.float32)
     ein = oracle.ein_depth(lab, d["E0"], tau, phi, du, dv, uc, vc, d["s"][0], d["s"][1])
     assert np.allclose(ein, d["ein"], rtol=0, atol=1e-6 * np.abs(d["ein"]).max())
+
+
+def test_depth_blur_matches_oracle():
+    """The host-side Gaussian blur of the depth maps (torch FFT, the map's
+    device) against the reference's NumPy form."""
+    import torch
+    from mosaic_gb300 import engine
+    rng = np.random.default_rng(3)
+    m = rng.standard_normal((40, 33)).astype(np.float32)
+    for rad in (1, 3, 6):
+        got = engine._gauss_blur(torch.tensor(m), rad).numpy()
+        assert np.allclose(got, oracle.blur_map(m, rad), rtol=0, atol=1e-6), rad
