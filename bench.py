@@ -246,6 +246,7 @@ def surrogate_leg(args, dev):
             "exact_seconds_est": res["exact_seconds"], "seconds": res["seconds"],
             "exact_frames": res["exact_frames"], "n_train": res["n_train"],
             "n_judged": res["n_judged"], "n_failed_judges": res["n_failed_judges"],
+            "n_rejudged": res["n_rejudged"], "n_failed_rejudges": res["n_failed_rejudges"],
             "n_fallback": res["n_fallback"], "times": res["times"],
             "judge_err_p50_p90_max": pct(res["judge_err"]),
             "unjudged_err_p50_p90_max": pct(ve), "unjudged_checked": int(len(ve)),

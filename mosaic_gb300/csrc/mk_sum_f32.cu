@@ -232,6 +232,10 @@ __device__ __forceinline__ void mk_tile_terms_ana(
 // P = sum e e^{i sigma} cos(delta) and Q = i sum e e^{i sigma} sin(delta);
 // pixel a = P + Q, pixel b = P - Q.
 #define MK_PAIR_SHORT_DELTA 0.07f
+#ifndef MK_PAIR_UNROLL
+#define MK_PAIR_UNROLL 8
+#endif
+constexpr int kPairUnroll = MK_PAIR_UNROLL;   // atoms per unrolled step of the pair loop
 template <int NPAIR, bool FR, bool CPLX, bool SHORT>
 __device__ __forceinline__ void mk_tile_terms_pair(
     const float4 *__restrict__ P, const float2 *__restrict__ E, int T, const float (&sx)[NPAIR],
@@ -240,7 +244,7 @@ __device__ __forceinline__ void mk_tile_terms_pair(
     float by, float bz, float (&pr)[NPAIR], float (&pi)[NPAIR], float (&qr)[NPAIR],
     float (&qi)[NPAIR])
 {
-#pragma unroll 4
+#pragma unroll (kPairUnroll)
     for (int j = 0; j < T; ++j) {
         const float4 a = P[j];
         const float2 e = E[j];

@@ -11,8 +11,9 @@ that it measures the error of the frame in intensity relative to its peak --
 the quantity the judge thresholds -- rather than in log intensity, which
 gives the dim pixels most of the weight. Every ``judge_every``-th predicted
 frame is recomputed exactly; if its relative error max|I_pred - I| / max I
-exceeds ``tol`` it falls back to the exact sum, together with the predicted
-frames it stands for.
+exceeds ``tol``, the network trains further on every exact frame so far
+(training and judged), predicts that block again and one more of its frames
+is judged; a block failing that too falls back to the exact sum.
 
 The network trains and predicts on the GPU with the library's own kernels
 (``mk_gemm_bf16``: BF16 operands, FP32 accumulation on the tensor cores;
@@ -245,12 +246,16 @@ class SurrogateScan:
         rank: principal components of the normalised frames the network
             predicts; scale_weight: loss weight of the log peak output
             against the (variance-weighted) components.
+        refine_steps: when judges fail, further training steps on all exact
+            frames (training + judged) before the failed blocks are predicted
+            again and re-judged once (0: failed blocks go straight to the
+            exact sum).
     """
 
     def __init__(self, beam, sample, detector, stage, theta, chi, roi=128, stride=4, raster=False,
                  judge_every=8, tol=0.02, hidden=256, n_hidden=4, n_freq=16, fit_steps=2000,
                  lr=3e-3, seed=0, sc_kwargs=None, device="cuda", rank=32, f_max=0.5, f_min=0.25,
-                 scale_weight=10.0, batch_frames=2048):
+                 scale_weight=10.0, batch_frames=2048, refine_steps=600):
         self.beam, self.sample, self.detector, self.stage = beam, sample, detector, stage
         self.theta = np.asarray(theta, dtype=np.float64)
         self.chi = np.asarray(chi, dtype=np.float64)
@@ -260,6 +265,7 @@ class SurrogateScan:
         self.fit_steps, self.lr, self.seed = fit_steps, lr, seed
         self.rank, self.f_max, self.f_min = int(rank), float(f_max), float(f_min)
         self.scale_weight, self.batch_frames = float(scale_weight), int(batch_frames)
+        self.refine_steps = int(refine_steps)
         self.kw = dict(apply_polarization=False, spherical_decay=False, remove_forward=False)
         self.kw.update(sc_kwargs or {})
         self.dev = torch.device(device)
@@ -375,7 +381,42 @@ class SurrogateScan:
         I_model = I_pred.clone() if exact_all else None
         I_pred[torch.as_tensor(judged, device=self.dev)] = I_j
         failed = [blk for blk, e in zip(blocks, err_j) if e > self.tol]
-        fb = np.concatenate([blk[1:] for blk in failed]) if failed else np.zeros(0, np.int64)
+        probes = np.zeros(0, np.int64)
+        err_p = np.zeros(0)
+        t0 = time.perf_counter()
+        if failed and self.refine_steps > 0:
+            # Every exact frame so far (training and judged) trains the network
+            # further; the failed blocks are predicted again and one more frame
+            # of each is judged; only blocks failing that too go to the exact sum.
+            Mj = I_j.amax(1, keepdim=True).clamp_min(1e-300)
+            Cj = (I_j / Mj - basis.mu) @ basis.V.T
+            Tj = torch.cat([Cj / cs, (torch.log(Mj) - lmu) / lsd], 1)
+            sel = torch.as_tensor(np.concatenate([tr, pred_idx[judged]]), device=self.dev)
+            self.losses = np.concatenate([self.losses, self.net.fit(
+                feats[sel], torch.cat([T, Tj]).contiguous(), steps=self.refine_steps,
+                lr=0.3 * self.lr, col_w=col_w)])
+            redo = np.concatenate([blk[1:] for blk in failed])
+            if redo.size:
+                Yr = self.net.predict(feats[torch.as_tensor(pred_idx[redo], device=self.dev)])
+                sh = basis.decode(self.net, (Yr[:, : basis.rank] * cs).contiguous())
+                I_pred[torch.as_tensor(redo, device=self.dev)] = \
+                    sh.clamp_min_(0.0) * torch.exp(Yr[:, basis.rank:] * lsd + lmu)
+            with_rest = [blk for blk in failed if len(blk) > 1]
+            probes = np.array([blk[len(blk) // 2] for blk in with_rest], dtype=np.int64)
+            if probes.size:
+                I_p = self.exact(pred_idx[probes])
+                err_p = frame_rel_error(I_pred[probes], I_p).cpu().numpy()
+                if exact_all:
+                    I_model[torch.as_tensor(redo, device=self.dev)] = \
+                        I_pred[torch.as_tensor(redo, device=self.dev)]
+                I_pred[torch.as_tensor(probes, device=self.dev)] = I_p
+            still = [(blk, p) for blk, p, e in zip(with_rest, probes, err_p) if e > self.tol]
+            fb = (np.concatenate([blk[(blk != blk[0]) & (blk != p)] for blk, p in still])
+                  if still else np.zeros(0, np.int64))
+        else:
+            fb = np.concatenate([blk[1:] for blk in failed]) if failed else np.zeros(0, np.int64)
+        sync()
+        t["refine"] = time.perf_counter() - t0
         t0 = time.perf_counter()
         if fb.size:
             I_pred[torch.as_tensor(fb, device=self.dev)] = self.exact(pred_idx[fb])
@@ -384,10 +425,11 @@ class SurrogateScan:
         frames = torch.empty((n, self.roi * self.roi), dtype=torch.float32, device=self.dev)
         frames[torch.as_tensor(tr, device=self.dev)] = I_train
         frames[torch.as_tensor(pred_idx, device=self.dev)] = I_pred
-        exact_frames = len(tr) + len(judged) + int(fb.size)
+        exact_frames = len(tr) + len(judged) + int(probes.size) + int(fb.size)
         total = sum(t.values())
         res = dict(frames=frames, n_frames=n, n_train=len(tr), n_judged=len(judged),
                    n_fallback=int(fb.size), n_failed_judges=len(failed), exact_frames=exact_frames,
+                   n_rejudged=int(probes.size), n_failed_rejudges=int((err_p > self.tol).sum()),
                    judge_err=err_j, times=t, setup_seconds=setup_s, seconds=total,
                    frames_per_s=n / total, final_loss=float(self.losses[-1]),
                    params=self.net.n_params, rank=basis.rank)
@@ -407,7 +449,7 @@ class SurrogateScan:
         res["gain"] = res["exact_seconds"] / total
         if verify and not exact_all:
             rng = np.random.default_rng(self.seed + 1)
-            unjudged = np.setdiff1d(np.arange(len(pred_idx)), np.concatenate([judged, fb]))
+            unjudged = np.setdiff1d(np.arange(len(pred_idx)), np.concatenate([judged, probes, fb]))
             pick = rng.choice(unjudged, size=min(int(verify), unjudged.size), replace=False) \
                 if unjudged.size else np.zeros(0, np.int64)
             I_true = self.exact(pred_idx[pick])

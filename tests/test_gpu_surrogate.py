@@ -116,6 +116,6 @@ def test_surrogate_scan_gains_over_exact(cuda):
     assert (me <= 0.02).mean() >= 0.9
     # after judging and fallback
     assert (fe <= 0.02).mean() >= 0.95
-    assert res["n_fallback"] <= 7 * res["n_failed_judges"]
+    assert res["n_fallback"] <= 6 * res["n_failed_rejudges"] and res["n_rejudged"] <= res["n_failed_judges"]
     # frames/s over the exact-only scan, both timed here
     assert res["gain"] > 1.5, res["gain"]
