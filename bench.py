@@ -80,6 +80,11 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            # the first sample takes nvidia-smi's start-up: wait for it (at most
+            # 3 s) so that a short timed region still has samples around it
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -90,6 +95,9 @@ class ClockSampler:
 
     def __exit__(self, *exc):
         if self.proc is not None:
+            n0, t0 = len(self.lines), time.time()
+            while len(self.lines) == n0 and time.time() - t0 < 0.5 and self.proc.poll() is None:
+                time.sleep(0.01)             # one sample at the region's end
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)

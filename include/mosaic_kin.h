@@ -333,7 +333,8 @@ int mk_adam(long long n, float *w, const float *g, float *m, float *v, void *w_b
 /* --- diagnostics ------------------------------------------------------ */
 /* Pipe-throughput microbenchmark (no counterpart in the reference): results
  * per clock per SM of kind 0 MUFU sine, 1 MUFU sine+cosine (two results per
- * call), 2 FRND (rintf), 3 FFMA, over one wave of blocks; `iters` loop trips
+ * call), 2 FRND (rintf), 3 FFMA, 4 packed FFMA2 (counted in FMAs), over
+ * one wave of blocks; `iters` loop trips
  * of eight chains per thread. Synchronises `stream`. Workspace of
  * mk_probe_workspace_size() bytes (device). Gives the split kernel's roofline
  * denominator on the GPU at hand. */
