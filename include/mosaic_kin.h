@@ -117,8 +117,10 @@ typedef struct {
     int tile_atoms;       /* power of two, 128..4096 */
     double *origin;       /* device (n_tiles, 4): origin x, y, z [m], radius [m] */
     int *species;         /* device (n_tiles) species index */
-    float *pos;           /* device (n_tiles*tile_atoms, 4): k/2pi (a - o) [cycles], |.|^2 */
-    float *amp;           /* device (n_tiles*tile_atoms, 2): incident amplitude */
+    float *pos;           /* device (n_tiles*tile_atoms, 4): k/2pi (a - o) [cycles], |.|^2,
+                             atom pairs interleaved: x0 x1 y0 y1 z0 z1 w0 w1 */
+    float *amp;           /* device (n_tiles*tile_atoms, 2): incident amplitude,
+                             atom pairs interleaved: re0 re1 im0 im1 */
 } mk_tiles;
 
 /* Launch shape of the split-phase kernel (autotuned by the host). */

@@ -355,8 +355,18 @@ __global__ void __launch_bounds__(NT) mk_tile_kernel(MkTileMap M, double kappa,
                             (float)(kappa * kappa * d2));
             E = amp[a];
         }
-        tpos[base + j] = P;
-        tamp[base + j] = E;
+        // atom pairs interleaved: per pair (2q, 2q+1) the floats
+        // x0 x1 y0 y1 z0 z1 w0 w1 and er0 er1 ei0 ei1, so that the sum
+        // kernels load two atoms' coordinates as packed f32x2 operands
+        float *pf = reinterpret_cast<float *>(tpos) + 4 * (base + (j & ~1));
+        float *af = reinterpret_cast<float *>(tamp) + 2 * (base + (j & ~1));
+        const int h = j & 1;
+        pf[h] = P.x;
+        pf[2 + h] = P.y;
+        pf[4 + h] = P.z;
+        pf[6 + h] = P.w;
+        af[h] = E.x;
+        af[2 + h] = E.y;
     }
     for (int off = 16; off > 0; off >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, off));
     if ((threadIdx.x & 31) == 0) rad2[threadIdx.x >> 5] = r2max;

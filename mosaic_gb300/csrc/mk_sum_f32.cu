@@ -136,40 +136,70 @@ __device__ __forceinline__ void mk_issue_tile(const MkSplitArgs &A, float4 *s_po
     mk_tma_load_1d(s_amp + buf * T, A.tamp + (size_t)tile * T, T * sizeof(float2), &bar[buf]);
 }
 
+// Tile atoms in shared memory come in interleaved pairs (see mk_tiles_build):
+// float4 P[2q] = (x0, x1, y0, y1), P[2q+1] = (z0, z1, w0, w1) and
+// float4 E[q] = (re0, re1, im0, im1) for atoms 2q, 2q+1.
+struct MkAtom {
+    float4 a;   // x, y, z (cycles), |D|^2
+    float2 e;   // amplitude
+};
+__device__ __forceinline__ void mk_atom_pair(const float4 *__restrict__ P,
+                                             const float4 *__restrict__ E, int q, MkAtom &u,
+                                             MkAtom &v)
+{
+    const float4 A = P[2 * q], B = P[2 * q + 1], M = E[q];
+    u.a = make_float4(A.x, A.z, B.x, B.z);
+    v.a = make_float4(A.y, A.w, B.y, B.w);
+    u.e = make_float2(M.x, M.z);
+    v.e = make_float2(M.y, M.w);
+}
+
 // The terms of one tile against PIX pixels: csr/csi += E_j exp(2 pi i phase).
 // FR adds the |d|^2 term of the in-tile distance (db = D.b per atom).
 template <int PIX, bool FR, bool CPLX>
+__device__ __forceinline__ void mk_atom_terms(const MkAtom &at, const float (&wx)[PIX],
+                                              const float (&wy)[PIX], const float (&wz)[PIX],
+                                              const float (&hq)[PIX], float bx, float by,
+                                              float bz, float (&csr)[PIX], float (&csi)[PIX])
+{
+    const float4 a = at.a;
+    const float2 e = at.e;
+    float db = 0.f;
+    if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
+#pragma unroll
+    for (int p = 0; p < PIX; ++p) {
+        float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
+        if (FR) {
+            const float sp = db - lin;
+            lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
+        }
+        const float r = mk_frac_nearest(lin);
+        float sn, cs;
+        __sincosf(r * TWO_PI_F, &sn, &cs);
+        if (CPLX) {
+            csr[p] = fmaf(e.x, cs, fmaf(-e.y, sn, csr[p]));
+            csi[p] = fmaf(e.x, sn, fmaf(e.y, cs, csi[p]));
+        } else {
+            csr[p] = fmaf(e.x, cs, csr[p]);
+            csi[p] = fmaf(e.x, sn, csi[p]);
+        }
+    }
+}
+
+template <int PIX, bool FR, bool CPLX>
 __device__ __forceinline__ void mk_tile_terms(const float4 *__restrict__ P,
-                                              const float2 *__restrict__ E, int T,
+                                              const float4 *__restrict__ E, int T,
                                               const float (&wx)[PIX], const float (&wy)[PIX],
                                               const float (&wz)[PIX], const float (&hq)[PIX],
                                               float bx, float by, float bz, float (&csr)[PIX],
                                               float (&csi)[PIX])
 {
-#pragma unroll 4
-    for (int j = 0; j < T; ++j) {
-        const float4 a = P[j];
-        const float2 e = E[j];
-        float db = 0.f;
-        if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
-#pragma unroll
-        for (int p = 0; p < PIX; ++p) {
-            float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
-            if (FR) {
-                const float sp = db - lin;
-                lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
-            }
-            const float r = mk_frac_nearest(lin);
-            float sn, cs;
-            __sincosf(r * TWO_PI_F, &sn, &cs);
-            if (CPLX) {
-                csr[p] = fmaf(e.x, cs, fmaf(-e.y, sn, csr[p]));
-                csi[p] = fmaf(e.x, sn, fmaf(e.y, cs, csi[p]));
-            } else {
-                csr[p] = fmaf(e.x, cs, csr[p]);
-                csi[p] = fmaf(e.x, sn, csi[p]);
-            }
-        }
+#pragma unroll 2
+    for (int q = 0; q < T / 2; ++q) {
+        MkAtom u, v;
+        mk_atom_pair(P, E, q, u, v);
+        mk_atom_terms<PIX, FR, CPLX>(u, wx, wy, wz, hq, bx, by, bz, csr, csi);
+        mk_atom_terms<PIX, FR, CPLX>(v, wx, wy, wz, hq, bx, by, bz, csr, csi);
     }
 }
 
@@ -180,43 +210,98 @@ __device__ __forceinline__ void mk_tile_terms(const float4 *__restrict__ P,
 // g1 = 0); Darwin pixels the first-order expansion of the roll-off
 // (th = inf); pixels with one factor for the whole tile (g0, g1 = 0, inf).
 template <int PIX, bool FR, bool CPLX>
+__device__ __forceinline__ void mk_atom_terms_ana(
+    const MkAtom &at, const float (&wx)[PIX], const float (&wy)[PIX], const float (&wz)[PIX],
+    const float (&hq)[PIX], float bx, float by, float bz, const float (&gx)[PIX],
+    const float (&gy)[PIX], const float (&gz)[PIX], const float (&th)[PIX],
+    const float (&g0)[PIX], const float (&g1)[PIX], float (&csr)[PIX], float (&csi)[PIX])
+{
+    const float4 a = at.a;
+    const float2 e = at.e;
+    float db = 0.f;
+    if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
+#pragma unroll
+    for (int p = 0; p < PIX; ++p) {
+        float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
+        if (FR) {
+            const float sp = db - lin;
+            lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
+        }
+        const float t = fmaf(a.z, gz[p], fmaf(a.y, gy[p], a.x * gx[p]));
+        const float m = t <= th[p] ? fmaf(g1[p], t, g0[p]) : 0.f;
+        const float r = mk_frac_nearest(lin);
+        float sn, cs;
+        __sincosf(r * TWO_PI_F, &sn, &cs);
+        const float er = e.x * m;
+        if (CPLX) {
+            const float ei = e.y * m;
+            csr[p] = fmaf(er, cs, fmaf(-ei, sn, csr[p]));
+            csi[p] = fmaf(er, sn, fmaf(ei, cs, csi[p]));
+        } else {
+            csr[p] = fmaf(er, cs, csr[p]);
+            csi[p] = fmaf(er, sn, csi[p]);
+        }
+    }
+}
+
+template <int PIX, bool FR, bool CPLX>
 __device__ __forceinline__ void mk_tile_terms_ana(
-    const float4 *__restrict__ P, const float2 *__restrict__ E, int T, const float (&wx)[PIX],
+    const float4 *__restrict__ P, const float4 *__restrict__ E, int T, const float (&wx)[PIX],
     const float (&wy)[PIX], const float (&wz)[PIX], const float (&hq)[PIX], float bx, float by,
     float bz, const float (&gx)[PIX], const float (&gy)[PIX], const float (&gz)[PIX],
     const float (&th)[PIX], const float (&g0)[PIX], const float (&g1)[PIX], float (&csr)[PIX],
     float (&csi)[PIX])
 {
-#pragma unroll 2
-    for (int j = 0; j < T; ++j) {
-        const float4 a = P[j];
-        const float2 e = E[j];
-        float db = 0.f;
-        if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
-#pragma unroll
-        for (int p = 0; p < PIX; ++p) {
-            float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
-            if (FR) {
-                const float sp = db - lin;
-                lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
-            }
-            const float t = fmaf(a.z, gz[p], fmaf(a.y, gy[p], a.x * gx[p]));
-            const float m = t <= th[p] ? fmaf(g1[p], t, g0[p]) : 0.f;
-            const float r = mk_frac_nearest(lin);
-            float sn, cs;
-            __sincosf(r * TWO_PI_F, &sn, &cs);
-            const float er = e.x * m;
-            if (CPLX) {
-                const float ei = e.y * m;
-                csr[p] = fmaf(er, cs, fmaf(-ei, sn, csr[p]));
-                csi[p] = fmaf(er, sn, fmaf(ei, cs, csi[p]));
-            } else {
-                csr[p] = fmaf(er, cs, csr[p]);
-                csi[p] = fmaf(er, sn, csi[p]);
-            }
-        }
+    for (int q = 0; q < T / 2; ++q) {
+        MkAtom u, v;
+        mk_atom_pair(P, E, q, u, v);
+        mk_atom_terms_ana<PIX, FR, CPLX>(u, wx, wy, wz, hq, bx, by, bz, gx, gy, gz, th, g0, g1, csr, csi);
+        mk_atom_terms_ana<PIX, FR, CPLX>(v, wx, wy, wz, hq, bx, by, bz, gx, gy, gz, th, g0, g1, csr, csi);
     }
 }
+
+// Packed FP32 pairs: f32x2 instructions (sm_100 and later) apply one IEEE
+// fp32 operation to both halves of a 64-bit register pair. The pair loop
+// below keeps two atoms in the two halves, so one instruction does the work
+// of two (the FMA pipe's float rate is unchanged; issue slots halve).
+typedef unsigned long long mk_f2;
+__device__ __forceinline__ mk_f2 f2_pack(float lo, float hi)
+{
+    mk_f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(mk_f2 v)
+{
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ mk_f2 f2_fma(mk_f2 a, mk_f2 b, mk_f2 c)
+{
+    mk_f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ mk_f2 f2_mul(mk_f2 a, mk_f2 b)
+{
+    mk_f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ mk_f2 f2_add(mk_f2 a, mk_f2 b)
+{
+    mk_f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ mk_f2 f2_sub(mk_f2 a, mk_f2 b)
+{
+    mk_f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ mk_f2 f2_splat(float x) { return f2_pack(x, x); }
 
 // Pixel pairs (a, b) that are neighbours on the detector: with
 // sigma = D.(w_a + w_b)/2 (cycles) and delta = pi D.(w_a - w_b) (radians),
@@ -229,61 +314,78 @@ __device__ __forceinline__ void mk_tile_terms_ana(
 //         e sin = delta (e - (e/6) d^2); truncation below delta^4/24 = 1e-6;
 //   long  (|delta| <= 0.5): through d^6 and d^5; below delta^7/7! = 1.6e-6.
 // One MUFU sin/cos for two terms instead of two. Sums kept as
-// P = sum e e^{i sigma} cos(delta) and Q = i sum e e^{i sigma} sin(delta);
-// pixel a = P + Q, pixel b = P - Q.
+// P = sum e e^{i sigma} cos(delta) and S = sum e e^{i sigma} sin(delta)
+// (Q = i S); pixel a = P + i S, pixel b = P - i S. Every quantity of the
+// loop is an f32x2 pair over the tile's atoms 2q and 2q+1 (interleaved in
+// shared memory); the two halves of the accumulators are added at the end.
 #define MK_PAIR_SHORT_DELTA 0.07f
 #ifndef MK_PAIR_UNROLL
 #define MK_PAIR_UNROLL 8
 #endif
-constexpr int kPairUnroll = MK_PAIR_UNROLL;   // atoms per unrolled step of the pair loop
+constexpr int kPairUnroll = MK_PAIR_UNROLL / 2;   // atom pairs per unrolled step
 template <int NPAIR, bool FR, bool CPLX, bool SHORT>
 __device__ __forceinline__ void mk_tile_terms_pair(
-    const float4 *__restrict__ P, const float2 *__restrict__ E, int T, const float (&sx)[NPAIR],
-    const float (&sy)[NPAIR], const float (&sz)[NPAIR], const float (&dx)[NPAIR],
-    const float (&dy)[NPAIR], const float (&dz)[NPAIR], const float (&hq)[NPAIR], float bx,
-    float by, float bz, float (&pr)[NPAIR], float (&pi)[NPAIR], float (&qr)[NPAIR],
-    float (&qi)[NPAIR])
+    const float4 *__restrict__ P, const float4 *__restrict__ E, int T, const mk_f2 (&sx)[NPAIR],
+    const mk_f2 (&sy)[NPAIR], const mk_f2 (&sz)[NPAIR], const mk_f2 (&dx)[NPAIR],
+    const mk_f2 (&dy)[NPAIR], const mk_f2 (&dz)[NPAIR], const mk_f2 (&hq)[NPAIR], mk_f2 bx,
+    mk_f2 by, mk_f2 bz, mk_f2 (&pr)[NPAIR], mk_f2 (&pi)[NPAIR], mk_f2 (&sr)[NPAIR],
+    mk_f2 (&si)[NPAIR])
 {
+    const mk_f2 magic = f2_splat(MK_ROUND_MAGIC), two_pi = f2_splat(TWO_PI_F);
+    const mk_f2 one = f2_splat(1.f), m_one = f2_splat(-1.f);
+    const mk_f2 k2 = f2_splat(-0.5f), k3 = f2_splat(-1.f / 6.f);
+    const mk_f2 k4 = f2_splat(1.f / 24.f), k5 = f2_splat(1.f / 120.f), k6 = f2_splat(-1.f / 720.f);
+    const ulonglong2 *P2 = reinterpret_cast<const ulonglong2 *>(P);
+    const ulonglong2 *E2 = reinterpret_cast<const ulonglong2 *>(E);
 #pragma unroll (kPairUnroll)
-    for (int j = 0; j < T; ++j) {
-        const float4 a = P[j];
-        const float2 e = E[j];
-        float db = 0.f;
-        if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
+    for (int q = 0; q < T / 2; ++q) {
+        const ulonglong2 A = P2[2 * q], B = P2[2 * q + 1], M = E2[q];
+        const mk_f2 X = A.x, Y = A.y, Z = B.x, W = B.y, ER = M.x, EI = M.y;
+        mk_f2 db = 0ull;
+        if (FR) db = f2_fma(Z, bz, f2_fma(Y, by, f2_mul(X, bx)));
         // per-atom polynomial coefficients (amplitude folded in when real)
-        const float e0 = CPLX ? 1.f : e.x;
-        const float c2 = -0.5f * e0, s2 = (-1.f / 6.f) * e0;
-        const float c4 = SHORT ? 0.f : (1.f / 24.f) * e0, s4 = SHORT ? 0.f : (1.f / 120.f) * e0;
-        const float c6 = SHORT ? 0.f : (-1.f / 720.f) * e0;
+        const mk_f2 e0 = CPLX ? one : ER;
+        const mk_f2 c2 = f2_mul(e0, k2), s2 = f2_mul(e0, k3);
+        mk_f2 c4 = 0ull, s4 = 0ull, c6 = 0ull;
+        if (!SHORT) {
+            c4 = f2_mul(e0, k4);
+            s4 = f2_mul(e0, k5);
+            c6 = f2_mul(e0, k6);
+        }
+        mk_f2 EIn = 0ull;
+        if (CPLX) EIn = f2_mul(EI, m_one);
 #pragma unroll
-        for (int q = 0; q < NPAIR; ++q) {
-            float sig = fmaf(a.z, sz[q], fmaf(a.y, sy[q], a.x * sx[q]));
+        for (int p = 0; p < NPAIR; ++p) {
+            mk_f2 sig = f2_fma(Z, sz[p], f2_fma(Y, sy[p], f2_mul(X, sx[p])));
             if (FR) {
-                const float sp = db - sig;
-                sig = fmaf(fmaf(-sp, sp, a.w), hq[q], sig);
+                const mk_f2 sp = f2_sub(db, sig);
+                sig = f2_fma(f2_fma(f2_mul(sp, m_one), sp, W), hq[p], sig);
             }
-            const float del = fmaf(a.z, dz[q], fmaf(a.y, dy[q], a.x * dx[q]));
-            const float r = mk_frac_nearest(sig);
-            float sn, cs;
-            __sincosf(r * TWO_PI_F, &sn, &cs);
-            const float d2 = del * del;
-            float cd, sd;
+            const mk_f2 del = f2_fma(Z, dz[p], f2_fma(Y, dy[p], f2_mul(X, dx[p])));
+            const mk_f2 rr = f2_mul(f2_sub(sig, f2_sub(f2_add(sig, magic), magic)), two_pi);
+            const float2 r = f2_unpack(rr);
+            float s0, c0, s1, c1;
+            __sincosf(r.x, &s0, &c0);
+            __sincosf(r.y, &s1, &c1);
+            mk_f2 ec = f2_pack(c0, c1), es = f2_pack(s0, s1);
+            const mk_f2 d2 = f2_mul(del, del);
+            mk_f2 cd, sd;
             if (SHORT) {
-                cd = fmaf(d2, c2, e0);
-                sd = del * fmaf(d2, s2, e0);
+                cd = f2_fma(d2, c2, e0);
+                sd = f2_mul(del, f2_fma(d2, s2, e0));
             } else {
-                cd = fmaf(d2, fmaf(d2, fmaf(d2, c6, c4), c2), e0);
-                sd = del * fmaf(d2, fmaf(d2, s4, s2), e0);
+                cd = f2_fma(d2, f2_fma(d2, f2_fma(d2, c6, c4), c2), e0);
+                sd = f2_mul(del, f2_fma(d2, f2_fma(d2, s4, s2), e0));
             }
-            float ec = cs, es = sn;
             if (CPLX) {
-                ec = fmaf(e.x, cs, -e.y * sn);
-                es = fmaf(e.x, sn, e.y * cs);
+                const mk_f2 c = ec;
+                ec = f2_fma(ER, c, f2_mul(EIn, es));
+                es = f2_fma(ER, es, f2_mul(EI, c));
             }
-            pr[q] = fmaf(ec, cd, pr[q]);
-            pi[q] = fmaf(es, cd, pi[q]);
-            qr[q] = fmaf(-es, sd, qr[q]);
-            qi[q] = fmaf(ec, sd, qi[q]);
+            pr[p] = f2_fma(ec, cd, pr[p]);
+            pi[p] = f2_fma(es, cd, pi[p]);
+            sr[p] = f2_fma(es, sd, sr[p]);
+            si[p] = f2_fma(ec, sd, si[p]);
         }
     }
 }
@@ -440,7 +542,8 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                 return;
             }
             const float4 *P = s_pos + buf * T;
-            const float2 *E = s_amp + buf * T;
+            // T float2 amplitudes = T/2 float4 (interleaved atom pairs)
+            const float4 *E = reinterpret_cast<const float4 *>(s_amp + buf * T);
             float csr[PIX], csi[PIX];
 #pragma unroll
             for (int p = 0; p < PIX; ++p) csr[p] = csi[p] = 0.f;
@@ -449,44 +552,50 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
             const bool fr_tile = FRESNEL && (float)o.w > A.fres_r;
             if constexpr (PAIR) {
                 constexpr int NP = PIX / 2;
-                float sx[NP], sy[NP], sz[NP], dx[NP], dy[NP], dz[NP], hp[NP];
-                float pr[NP], pi_[NP], qr[NP], qi[NP];
+                mk_f2 sx[NP], sy[NP], sz[NP], dx[NP], dy[NP], dz[NP], hp[NP];
+                mk_f2 pr[NP], pi_[NP], sr[NP], si[NP];
 #pragma unroll
                 for (int q = 0; q < NP; ++q) {
                     const int a = 2 * q, b = 2 * q + 1;
-                    sx[q] = 0.5f * (wx[a] + wx[b]);
-                    sy[q] = 0.5f * (wy[a] + wy[b]);
-                    sz[q] = 0.5f * (wz[a] + wz[b]);
-                    dx[q] = 3.14159265358979f * (wx[a] - wx[b]);
-                    dy[q] = 3.14159265358979f * (wy[a] - wy[b]);
-                    dz[q] = 3.14159265358979f * (wz[a] - wz[b]);
-                    hp[q] = 0.5f * (hq[a] + hq[b]);
-                    pr[q] = pi_[q] = qr[q] = qi[q] = 0.f;
+                    sx[q] = f2_splat(0.5f * (wx[a] + wx[b]));
+                    sy[q] = f2_splat(0.5f * (wy[a] + wy[b]));
+                    sz[q] = f2_splat(0.5f * (wz[a] + wz[b]));
+                    dx[q] = f2_splat(3.14159265358979f * (wx[a] - wx[b]));
+                    dy[q] = f2_splat(3.14159265358979f * (wy[a] - wy[b]));
+                    dz[q] = f2_splat(3.14159265358979f * (wz[a] - wz[b]));
+                    hp[q] = f2_splat(0.5f * (hq[a] + hq[b]));
+                    pr[q] = pi_[q] = sr[q] = si[q] = 0ull;    // +0.0f in both halves
                 }
+                const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
                 // the short delta polynomial for tiles small enough (uniform
                 // across the block, like fr_tile)
                 const bool short_tile = (float)o.w <= A.pair_short_r;
                 if (fr_tile) {
                     if (short_tile)
                         mk_tile_terms_pair<NP, true, CPLX, true>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                 F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                                                                 bx, by, bz, pr, pi_, sr, si);
                     else
                         mk_tile_terms_pair<NP, true, CPLX, false>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                  F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                                                                  bx, by, bz, pr, pi_, sr, si);
                 } else {
                     if (short_tile)
                         mk_tile_terms_pair<NP, false, CPLX, true>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                  F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                                                                  bx, by, bz, pr, pi_, sr, si);
                     else
                         mk_tile_terms_pair<NP, false, CPLX, false>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                   F.b[0], F.b[1], F.b[2], pr, pi_, qr, qi);
+                                                                   bx, by, bz, pr, pi_, sr, si);
                 }
 #pragma unroll
                 for (int q = 0; q < NP; ++q) {
-                    csr[2 * q] = pr[q] + qr[q];
-                    csi[2 * q] = pi_[q] + qi[q];
-                    csr[2 * q + 1] = pr[q] - qr[q];
-                    csi[2 * q + 1] = pi_[q] - qi[q];
+                    // halves = even and odd atoms of the tile
+                    const float2 a = f2_unpack(pr[q]), b = f2_unpack(pi_[q]);
+                    const float2 c = f2_unpack(sr[q]), d = f2_unpack(si[q]);
+                    const float P_re = a.x + a.y, P_im = b.x + b.y;
+                    const float S_im = c.x + c.y, S_re = d.x + d.y;   // Q = i S
+                    csr[2 * q] = P_re - S_im;
+                    csi[2 * q] = P_im + S_re;
+                    csr[2 * q + 1] = P_re + S_im;
+                    csi[2 * q + 1] = P_im - S_re;
                 }
             } else if (ANA && warp_zero) {
                 // every pixel of the warp is outside the acceptance for this tile

@@ -344,7 +344,8 @@ class Tiles:
         return float(torch.linalg.vector_norm(self.origin[: self.n_tiles, :3], dim=1).max())
 
     def amp_is_real(self):
-        return bool((self.amp[:, 1] == 0).all()) if self.n_tiles else True
+        # atom pairs interleaved as re0 re1 im0 im1
+        return bool((self.amp.view(-1, 4)[:, 2:] == 0).all()) if self.n_tiles else True
 
 
 DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
@@ -453,7 +454,7 @@ class TilesView:
                            self.species.data_ptr(), self.pos.data_ptr(), self.amp.data_ptr())
 
     def amp_is_real(self):
-        return bool((self.amp[: self.n_tiles * self.tile_atoms, 1] == 0).all())
+        return bool((self.amp[: self.n_tiles * self.tile_atoms].reshape(-1, 4)[:, 2:] == 0).all())
 
     def max_radius(self):
         return float(self.origin[: self.n_tiles, 3].max()) if self.n_tiles else 0.0
