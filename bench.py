@@ -47,10 +47,11 @@ MUFU_PER_CLK_SM = 16        # sin/cos results per clock per SM (MUFU)
 FP32_PER_CLK_SM = 128
 METRIC = "Gatom*pixel/s (kinematic sum, FP32 split-phase) vs FP64 plain on 1 GB300"
 MUFU_PER_TERM, FP32_PER_TERM = 2, 12   # canonical split-phase term
-# pixel-pair form: one sin/cos per two terms; per pair 22 FP32-pipe ops (two
-# 3-term dot products, rounding 2, scale 1, delta^2 1, cos/sin polynomials 6,
-# amplitude 2, four accumulators 4)
-MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR = 1, 11
+# pixel-pair form: one sin/cos per two terms; per pixel pair and atom 20 FP32
+# lane operations (two 3-term dot products 6, rounding 3, scale 1, delta^2 1,
+# short cos/sin polynomials 3, four accumulators 4, sin/cos argument scaling
+# 1, per-atom coefficients 1), run as packed f32x2 over atom pairs
+MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR = 1, 10
 
 
 def _dist():

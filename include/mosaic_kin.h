@@ -331,6 +331,13 @@ int mk_mse_weighted(long long n, int n_col, const float *y, const float *t, cons
  * the bf16 copy w_bf16 (or NULL). */
 int mk_adam(long long n, float *w, const float *g, float *m, float *v, void *w_bf16, float lr,
             float beta1, float beta2, float eps, int step, float weight_decay, void *stream);
+/* mk_adam with the step in device memory: step t = *step + 1 and learning
+ * rate lr_sched[*step - step0], so that a captured training step replays
+ * with advancing steps; mk_counter_add(step, 1) ends each captured step. */
+int mk_adam_sched(long long n, float *w, const float *g, float *m, float *v, void *w_bf16,
+                  const float *lr_sched, const int *step, int step0, float beta1, float beta2,
+                  float eps, float weight_decay, void *stream);
+int mk_counter_add(int *counter, int delta, void *stream);
 
 /* --- diagnostics ------------------------------------------------------ */
 /* Pipe-throughput microbenchmark (no counterpart in the reference): results

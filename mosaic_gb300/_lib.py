@@ -186,6 +186,10 @@ SIGNATURES = {
     "mk_mse": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp]),
     "mk_mse_weighted": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _vp, _vp, _vp, _vp, _vp,
                                        _vp, _vp]),
+    "mk_adam_sched": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                     ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float, _vp]),
+    "mk_counter_add": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "mk_adam": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int,
                                ctypes.c_float, _vp]),

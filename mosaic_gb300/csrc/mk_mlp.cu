@@ -271,6 +271,55 @@ __global__ void mk_adam_kernel(long long n, float *__restrict__ w, const float *
     if (wb) wb[i] = __float2bfloat16(wi);
 }
 
+// The same step with its step number in device memory (t = *step + 1) and
+// the learning rate from a schedule (lr_sched[*step - step0]), so that one
+// captured training step replays with advancing steps.
+__global__ void mk_adam_sched_kernel(long long n, float *__restrict__ w, const float *__restrict__ g,
+                                     float *__restrict__ m, float *__restrict__ v,
+                                     __nv_bfloat16 *__restrict__ wb,
+                                     const float *__restrict__ lr_sched,
+                                     const int *__restrict__ step, int step0, float b1, float b2,
+                                     float eps, float wd)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = *step;
+    const float t = (float)(s + 1);
+    const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
+    const float lr = lr_sched[s - step0];
+    const float gi = g[i] + wd * w[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+extern "C" int mk_adam_sched(long long n, float *w, const float *g, float *m, float *v,
+                             void *w_bf16, const float *lr_sched, const int *step, int step0,
+                             float beta1, float beta2, float eps, float weight_decay, void *stream)
+{
+    MK_REQUIRE(n > 0 && w && g && m && v && lr_sched && step && step0 >= 0,
+               "mk_adam_sched: bad arguments");
+    mk_adam_sched_kernel<<<(unsigned)((n + 255) / 256), 256, 0, mk_stream(stream)>>>(
+        n, w, g, m, v, static_cast<__nv_bfloat16 *>(w_bf16), lr_sched, step, step0, beta1, beta2,
+        eps, weight_decay);
+    MK_CHECK_CUDA(cudaGetLastError());
+    return MK_OK;
+}
+
+__global__ void mk_counter_add_kernel(int *c, int d) { *c += d; }
+
+extern "C" int mk_counter_add(int *counter, int delta, void *stream)
+{
+    MK_REQUIRE(counter, "mk_counter_add: null counter");
+    mk_counter_add_kernel<<<1, 1, 0, mk_stream(stream)>>>(counter, delta);
+    MK_CHECK_CUDA(cudaGetLastError());
+    return MK_OK;
+}
+
 extern "C" int mk_adam(long long n, float *w, const float *g, float *m, float *v, void *w_bf16,
                        float lr, float beta1, float beta2, float eps, int step, float weight_decay,
                        void *stream)

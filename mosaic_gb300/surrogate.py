@@ -157,6 +157,48 @@ class MLP:
             losses.append(loss)
         return torch.stack(losses).cpu().numpy()
 
+    def fit_graph(self, X, T, steps=1500, lr=2e-3, lr_final=1e-4, col_w=None):
+        """``fit`` on the full batch with one training step (forward, loss,
+        backward, Adam) captured as a CUDA graph and replayed ``steps`` times:
+        the same arithmetic and cosine schedule, without a host round trip per
+        step (the step number and learning rate live in device memory,
+        mk_adam_sched). Returns the final loss (1-element array)."""
+        if steps <= 0:
+            return np.zeros(0)
+        sh = engine._stream_handle
+        sched = lr_final + 0.5 * (lr - lr_final) * (
+            1 + np.cos(np.pi * np.arange(steps) / max(steps - 1, 1)))
+        lr_d = torch.tensor(sched, dtype=torch.float32, device=self.dev)
+        step0 = int(self.steps)
+        counter = torch.tensor([step0], dtype=torch.int32, device=self.dev)
+        # load the step's kernels before capture (on throw-away buffers)
+        tmp = torch.zeros(4, dtype=torch.float32, device=self.dev)
+        check(self.L.mk_adam_sched(1, _p(tmp[0:]), _p(tmp[1:]), _p(tmp[2:]), _p(tmp[3:]), None,
+                                   _p(lr_d), _p(counter), step0, 0.9, 0.999, 1e-8, 0.0, sh()))
+        cnt2 = counter.clone()
+        check(self.L.mk_counter_add(_p(cnt2), 1, sh()))
+        torch.cuda.synchronize(self.dev)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            acts, posts, Y = self.forward(X)
+            loss, G, Gb = self.mse(Y, T, col_w)
+            dW, db = self.backward(acts, posts, G, Gb)
+            s = sh()
+            for l in range(len(self.W)):
+                check(self.L.mk_adam_sched(self.W[l].numel(), _p(self.W[l]), _p(dW[l]),
+                                           _p(self.mW[l]), _p(self.vW[l]), _p(self.Wb[l]), _p(lr_d),
+                                           _p(counter), step0, 0.9, 0.999, 1e-8, 0.0, s))
+                check(self.L.mk_adam_sched(self.b[l].numel(), _p(self.b[l]), _p(db[l]),
+                                           _p(self.mb[l]), _p(self.vb[l]), None, _p(lr_d),
+                                           _p(counter), step0, 0.9, 0.999, 1e-8, 0.0, s))
+            check(self.L.mk_counter_add(_p(counter), 1, s))
+        for _ in range(int(steps)):
+            g.replay()
+        self.steps += int(steps)
+        out = np.array([float(loss)])
+        del g
+        return out
+
     def predict(self, X, chunk=4096):
         outs = []
         for i in range(0, int(X.shape[0]), chunk):
@@ -298,6 +340,7 @@ class SurrogateScan:
                       device=self.dev)
             T = torch.zeros((6, b.rank + 1), dtype=torch.float32, device=self.dev)
             net.fit(feats, T, steps=2, col_w=torch.ones(b.rank + 1, device=self.dev))
+            net.fit_graph(feats, T, steps=2, col_w=torch.ones(b.rank + 1, device=self.dev))
             Y = net.predict(feats)
             sh = b.decode(net, Y[:, : b.rank].contiguous()).clamp_min_(0.0) * torch.exp(Y[:, b.rank:])
             frame_rel_error(sh, sh + 1.0)
@@ -357,8 +400,8 @@ class SurrogateScan:
                            torch.tensor([self.scale_weight], device=self.dev)]).float().contiguous()
         feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=self.f_max, f_min=self.f_min)
         self.net = MLP(feats.shape[1], basis.rank + 1, self.hidden, self.n_hidden, self.seed, self.dev)
-        self.losses = self.net.fit(feats[torch.as_tensor(tr, device=self.dev)], T,
-                                   steps=self.fit_steps, lr=self.lr, col_w=col_w)
+        self.losses = self.net.fit_graph(feats[torch.as_tensor(tr, device=self.dev)].contiguous(), T,
+                                         steps=self.fit_steps, lr=self.lr, col_w=col_w)
         sync()
         t["fit"] = time.perf_counter() - t0
         t0 = time.perf_counter()
@@ -392,8 +435,8 @@ class SurrogateScan:
             Cj = (I_j / Mj - basis.mu) @ basis.V.T
             Tj = torch.cat([Cj / cs, (torch.log(Mj) - lmu) / lsd], 1)
             sel = torch.as_tensor(np.concatenate([tr, pred_idx[judged]]), device=self.dev)
-            self.losses = np.concatenate([self.losses, self.net.fit(
-                feats[sel], torch.cat([T, Tj]).contiguous(), steps=self.refine_steps,
+            self.losses = np.concatenate([self.losses, self.net.fit_graph(
+                feats[sel].contiguous(), torch.cat([T, Tj]).contiguous(), steps=self.refine_steps,
                 lr=0.3 * self.lr, col_w=col_w)])
             redo = np.concatenate([blk[1:] for blk in failed])
             if redo.size:

@@ -79,6 +79,26 @@ def test_mlp_fits_a_smooth_field(cuda):
     assert float(((net.predict(feats) - T) ** 2).mean()) < 2e-2
 
 
+def test_graph_captured_training_matches_eager(cuda):
+    """fit_graph (one captured step replayed, step and learning rate in device
+    memory) trains the same network as the eager loop."""
+    rng = np.random.default_rng(4)
+    X = torch.tensor(omlp.bf16(rng.standard_normal((40, 24))), dtype=torch.bfloat16, device=cuda)
+    T = torch.tensor(rng.standard_normal((40, 9)), dtype=torch.float32, device=cuda)
+    w = torch.tensor(rng.uniform(0.5, 2.0, 9), dtype=torch.float32, device=cuda)
+    a = MLP(24, 9, hidden=32, n_hidden=2, seed=3, device=cuda)
+    b = MLP(24, 9, hidden=32, n_hidden=2, seed=3, device=cuda)
+    la = a.fit(X, T, steps=60, lr=3e-3, col_w=w)
+    lb = b.fit_graph(X, T, steps=60, lr=3e-3, col_w=w)
+    assert a.steps == b.steps == 60
+    for wa, wb in zip(a.W + a.b, b.W + b.b):
+        assert torch.allclose(wa, wb, rtol=1e-4, atol=1e-6), float((wa - wb).abs().max())
+    assert abs(float(la[-1]) - float(lb[-1])) <= 1e-4 * abs(float(la[-1])) + 1e-7
+    # continuing (the refinement step) keeps the Adam step count
+    b.fit_graph(X, T, steps=10, lr=1e-3, col_w=w)
+    assert b.steps == 70
+
+
 def test_frame_basis_decode_on_the_gemm(cuda):
     """Principal components of a set of frames and their decoding through
     the BF16 GEMM with hi/lo splitting: full rank reproduces the frames."""
