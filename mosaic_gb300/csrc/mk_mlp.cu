@@ -41,6 +41,11 @@ __global__ void __launch_bounds__(128) mk_gemm_bf16_kernel(
     __shared__ __align__(16) __nv_bfloat16 Bs[MLP_BN][MLP_BK + MLP_PAD];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.y * MLP_BM, n0 = blockIdx.x * MLP_BN;
+    // split-K: slice blockIdx.z of gridDim.z sums k in [k_lo, k_hi) and adds
+    // its partial product into C (which the host has zeroed or holds the
+    // accumulation base); one slice: the whole K and the full epilogue
+    const int kper = ((K + gridDim.z - 1) / gridDim.z + MLP_BK - 1) / MLP_BK * MLP_BK;
+    const int k_lo = blockIdx.z * kper, k_hi = min(K, k_lo + kper);
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;   // warp sub-tile
     const int g = lane >> 2, t4 = lane & 3;                   // mma group / thread in group
     float acc[2][4][4];
@@ -52,16 +57,16 @@ __global__ void __launch_bounds__(128) mk_gemm_bf16_kernel(
             for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
 
     const __nv_bfloat16 zero = __float2bfloat16(0.f);
-    for (int k0 = 0; k0 < K; k0 += MLP_BK) {
+    for (int k0 = k_lo; k0 < k_hi; k0 += MLP_BK) {
         for (int e = tid; e < MLP_BM * MLP_BK; e += 128) {
             const int r = e / MLP_BK, c = e % MLP_BK;
             const int m = m0 + r, k = k0 + c;
-            As[r][c] = (m < M && k < K) ? A[(long long)m * sam + (long long)k * sak] : zero;
+            As[r][c] = (m < M && k < k_hi) ? A[(long long)m * sam + (long long)k * sak] : zero;
         }
         for (int e = tid; e < MLP_BN * MLP_BK; e += 128) {
             const int r = e / MLP_BK, c = e % MLP_BK;
             const int n = n0 + r, k = k0 + c;
-            Bs[r][c] = (n < N && k < K) ? B[(long long)k * sbk + (long long)n * sbn] : zero;
+            Bs[r][c] = (n < N && k < k_hi) ? B[(long long)k * sbk + (long long)n * sbn] : zero;
         }
         __syncthreads();
 #pragma unroll
@@ -99,6 +104,10 @@ __global__ void __launch_bounds__(128) mk_gemm_bf16_kernel(
                 const int n = n0 + wn + j * 8 + 2 * t4 + (r & 1);
                 if (m >= M || n >= N) continue;
                 float v = acc[i][j][r];
+                if (gridDim.z > 1) {
+                    atomicAdd(&C[(long long)m * ldc + n], v);
+                    continue;
+                }
                 if (flags & MK_GEMM_BIAS) v += bias[n];
                 if (flags & MK_GEMM_ACCUMULATE) v += C[(long long)m * ldc + n];
                 if (flags & MK_GEMM_RELU) v = fmaxf(v, 0.f);
@@ -117,7 +126,21 @@ extern "C" int mk_gemm_bf16(int M, int N, int K, const void *A, long long sam, l
     MK_REQUIRE(!(flags & MK_GEMM_BIAS) || bias, "mk_gemm_bf16: bias flag without bias");
     dim3 grid((N + MLP_BN - 1) / MLP_BN, (M + MLP_BM - 1) / MLP_BM);
     MK_REQUIRE(grid.y < 65536, "mk_gemm_bf16: M too large");
-    mk_gemm_bf16_kernel<<<grid, 128, 0, mk_stream(stream)>>>(
+    cudaStream_t st = mk_stream(stream);
+    // Few output tiles and a long K (the weight gradients: K = batch): split
+    // K over up to 8 slices that add into C, when the epilogue is a plain
+    // store or accumulate into C.
+    const int tiles = (int)(grid.x * grid.y);
+    if (tiles < 64 && K >= 4 * MLP_BK && C && !Cb && !(flags & (MK_GEMM_BIAS | MK_GEMM_RELU))) {
+        int z = std::min(8, std::min(K / (2 * MLP_BK), (128 + tiles - 1) / tiles));
+        if (z > 1) {
+            grid.z = (unsigned)z;
+            if (!(flags & MK_GEMM_ACCUMULATE))
+                MK_CHECK_CUDA(cudaMemset2DAsync(C, sizeof(float) * (size_t)ldc, 0,
+                                                sizeof(float) * (size_t)N, (size_t)M, st));
+        }
+    }
+    mk_gemm_bf16_kernel<<<grid, 128, 0, st>>>(
         M, N, K, static_cast<const __nv_bfloat16 *>(A), sam, sak,
         static_cast<const __nv_bfloat16 *>(B), sbk, sbn, C, ldc, bias, flags,
         static_cast<__nv_bfloat16 *>(Cb), ldcb);
