@@ -402,7 +402,10 @@ def run_ours(args):
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    h2d = pos_h.nbytes + idx_h.astype(np.int32).nbytes + B._beam_E0_map.nbytes + coords_m.nbytes
+    # what the entry point copies: the streamed chunks (positions, species
+    # codes), the beam map and the pixel coordinates
+    h2d = int(getattr(B, "last_stream_bytes", pos_h.nbytes + 4 * n_atoms)) + \
+        B._beam_E0_map.astype(np.complex64).nbytes + coords_m.nbytes
     d2h = n_pix * 16
 
     # FP64 plain (same GPU) on the central pixel subset: speed bar and error.

@@ -246,14 +246,16 @@ class beam:
         cache = getattr(self, "_staging", None)
         if cache is None or cache[0][0].shape[0] < big:
             cache = ([torch.empty((big, 3), dtype=torch.float32).pin_memory() for _ in range(2)],
-                     [torch.empty(big, dtype=torch.int32).pin_memory() for _ in range(2)])
+                     [torch.empty(big, dtype=torch.int32).pin_memory() for _ in range(2)],
+                     [torch.empty(big, dtype=torch.uint8).pin_memory() for _ in range(2)])
             self._staging = cache                # pinned once, reused by later calls
-        st_pos, st_idx = cache
+        st_pos, st_idx, st_u8 = cache
         done = [None, None]
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
-        labels, lab_index, counts = [], {}, []
+        labels, lab_index = [], {}
         off = 0
+        self.last_stream_bytes = 0               # host -> device bytes of this call
         with ThreadPoolExecutor(max_workers=1) as ex:
             nxt = ex.submit(self._load_chunk, sample, 1) if n_chunks else None
             for cid in range(1, n_chunks + 1):
@@ -268,25 +270,37 @@ class beam:
                     if el not in lab_index:
                         lab_index[el] = len(labels)
                         labels.append(el)
-                        counts.append(0)
                     remap[i] = lab_index[el]
-                g = remap[codes]
-                keep = g >= 0
-                if not keep.all():
-                    pos, g = pos[keep], g[keep]
+                # byte codes of known labels go to the device as they are and
+                # are mapped to the global species there; anything else is
+                # mapped (and filtered) on the host
+                on_device = codes.dtype == np.uint8 and bool((remap >= 0).all())
+                g = None
+                if not on_device:
+                    g = remap[codes]
+                    keep = g >= 0
+                    if not keep.all():
+                        pos, g = pos[keep], g[keep]
                 n = int(pos.shape[0])
                 if n == 0:
                     continue
-                for j, c in enumerate(np.bincount(g, minlength=len(labels))):
-                    counts[j] += int(c)
                 b = cid & 1
                 if done[b] is not None:
                     done[b].synchronize()        # staging buffer b is free again
                 st_pos[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(pos)))
-                st_idx[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(g, dtype=np.int32)))
+                self.last_stream_bytes += 12 * n + (n + 4 * len(remap) if on_device else 4 * n)
+                if on_device:
+                    st_u8[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(codes)))
+                else:
+                    st_idx[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(g, dtype=np.int32)))
                 with torch.cuda.stream(side):
                     pos_d[off:off + n].copy_(st_pos[b][:n], non_blocking=True)
-                    idx_d[off:off + n].copy_(st_idx[b][:n], non_blocking=True)
+                    if on_device:
+                        lut = torch.from_numpy(remap).to(dev)      # ordered on this stream
+                        raw = st_u8[b][:n].to(dev, non_blocking=True)
+                        idx_d[off:off + n] = lut[raw.long()]
+                    else:
+                        idx_d[off:off + n].copy_(st_idx[b][:n], non_blocking=True)
                     ev = torch.cuda.Event()
                     ev.record(side)
                     done[b] = ev
@@ -296,7 +310,9 @@ class beam:
         for ev in done:
             if ev is not None:
                 ev.synchronize()
-        return pos_d[:off], idx_d[:off], labels, np.asarray(counts, dtype=np.int64)
+        counts = (torch.bincount(idx_d[:off].long(), minlength=len(labels)).cpu().numpy()
+                  if off and labels else np.zeros(len(labels), dtype=np.int64))
+        return pos_d[:off], idx_d[:off], labels, counts.astype(np.int64)
 
     def stage_atoms(self, sample, stage, device="cuda"):
         """All atoms on the device, lab frame, with their incident amplitudes
