@@ -195,7 +195,7 @@ def probe_pipes(dev):
 
 
 def scan_leg(args, dev):
-    """Batched scan (BASELINE config 4): the first `scan_frames` frames of the
+    """Batched scan (the 724-frame rocking scan): the first `scan_frames` frames of the
     4M-atom rocking x chi scan (ROI sides cycling 64/128/256/512), all in one
     persistent launch captured in a CUDA graph; frames/s over graph replays."""
     import torch
