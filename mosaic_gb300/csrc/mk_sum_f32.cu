@@ -320,7 +320,7 @@ __device__ __forceinline__ mk_f2 f2_splat(float x) { return f2_pack(x, x); }
 // shared memory); the two halves of the accumulators are added at the end.
 #define MK_PAIR_SHORT_DELTA 0.07f
 #ifndef MK_PAIR_UNROLL
-#define MK_PAIR_UNROLL 8
+#define MK_PAIR_UNROLL 32
 #endif
 constexpr int kPairUnroll = MK_PAIR_UNROLL / 2;   // atom pairs per unrolled step
 template <int NPAIR, bool FR, bool CPLX, bool SHORT>
