@@ -36,9 +36,11 @@ def _cache_path():
 
 
 def _src_hash():
-    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "mk_sum_f32.cu")
-    with open(d, "rb") as fh:
-        return hashlib.sha1(fh.read()).hexdigest()[:12]
+    h = hashlib.sha1()
+    for name in ("mk_split.cuh", "mk_sum_f32.cu"):
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", name), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:12]
 
 
 def _key(n_pix, tiles, pairs_ok=False):

@@ -1,0 +1,8 @@
+// Split-phase kernel instances for blocks of 256 threads (all pixel
+// counts, Fresnel/complex/pair/analyser variants the picker allows).
+#include "mk_split.cuh"
+
+mk_split_fn mk_pick_nt256(int pix, bool fresnel, bool cplx, bool pair, bool ana)
+{
+    MK_PIX_CASES(256)
+}

@@ -33,7 +33,7 @@
 #include <algorithm>
 #include <mutex>
 
-#include "mk_common.cuh"
+#include "mk_split.cuh"
 
 static __device__ int g_split_status;
 
@@ -53,613 +53,6 @@ static int mk_split_read_status(cudaStream_t st)
         return MK_ETIMEOUT;
     }
     return MK_OK;
-}
-
-struct MkSplitArgs {
-    MkSpecies sp;
-    int n_tiles, tile_atoms, n_frames;
-    long long n_items;
-    mk_frame_desc f0;                // the frame when n_frames == 1
-    const mk_frame_desc *frames;     // device, n_frames (n_frames > 1)
-    unsigned long long *counter;
-    const double4 *q;                // per pixel (qx, qy, qz, qcut)
-    const float4 *u;                 // per pixel (ux, uy, uz, 1/|P|)
-    const double4 *origin;
-    const int *tspecies;
-    const float4 *tpos;
-    const float2 *tamp;
-    double2 *partial;
-    int *status;
-    float kappa;       // k / 2 pi [cycles/m]
-    float k;           // [1/m]
-    float s2fac;       // (k 0.25e-10 / pi)^2: s^2 = s2fac |b - u'|^2 [1/A^2]
-    int apply_pol, decay, remove_forward;
-    float pdeg;
-    float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
-    float pair_short_r; // PAIR kernels: tiles up to this radius [m] use the short polynomial
-    // analyser (ANA kernels, single exposures): kind 1 top-hat / 2 Darwin,
-    // beam direction and analyser axis in FP64, 4 sin^2(alpha/2), half-width
-    int analyser;
-    double an_b[3], an_c[3];
-    double an_xacc, an_hw, inv_kappa;
-};
-
-#define TWO_PI_F 6.28318530717958647692f
-// 1.5 * 2^23: for |x| < 2^22, (x + C) - C is x rounded to the nearest
-// integer (round-to-nearest-even of the FP32 add), two full-rate FMA-pipe
-// adds instead of rintf, whose FRND shares the quarter-rate pipe with the
-// MUFU sin/cos (measured 16 per clock per SM for each on sm_103).
-#define MK_ROUND_MAGIC 12582912.0f
-
-// x - nearest integer(x), exact in FP32 for |x| < 2^22.
-__device__ __forceinline__ float mk_frac_nearest(float x)
-{
-    return __fsub_rn(x, __fsub_rn(__fadd_rn(x, MK_ROUND_MAGIC), MK_ROUND_MAGIC));
-}
-
-// Scattering factor of species s at direction u' = b - w.
-__device__ __forceinline__ float2 mk_factor(const MkSplitArgs &A, int s, const mk_frame_desc &F,
-                                           float wx, float wy, float wz, float qcut,
-                                           float decay_ratio)
-{
-    const float upx = F.b[0] - wx, upy = F.b[1] - wy, upz = F.b[2] - wz;
-    const float w2 = fmaf(wz, wz, fmaf(wy, wy, wx * wx));
-    const float s2 = A.s2fac * w2;
-    const float *wk = A.sp.wk[s];
-    float f0 = wk[5];
-#pragma unroll
-    for (int i = 0; i < 5; ++i) f0 = fmaf(wk[i], __expf(-wk[6 + i] * s2), f0);
-    float fr = f0 + A.sp.anr[s], fi = A.sp.ani[s];
-    if (A.remove_forward && A.k * sqrtf(w2) < qcut) {
-        fr -= A.sp.f0z[s] + A.sp.anr[s];
-        fi -= A.sp.ani[s];
-    }
-    float scale = 1.f;
-    if (A.sp.has_dw) scale = __expf(-A.sp.dwb[s] * s2);
-    if (A.apply_pol) {
-        const float dotv = fmaf(F.b[2], upz, fmaf(F.b[1], upy, F.b[0] * upx));
-        const float er = fmaf(F.e[2], upz, fmaf(F.e[1], upy, F.e[0] * upx));
-        float P = 0.5f * (1.f - A.pdeg) * fmaf(dotv, dotv, 1.f) + A.pdeg * fmaf(-er, er, 1.f);
-        P = fminf(1.f, fmaxf(0.f, P));
-        scale *= sqrtf(P);
-    }
-    if (A.decay) scale *= decay_ratio;
-    return make_float2(fr * scale, fi * scale);
-}
-
-__device__ __forceinline__ void mk_issue_tile(const MkSplitArgs &A, float4 *s_pos, float2 *s_amp,
-                                              uint64_t *bar, int buf, int tile, int T,
-                                              uint32_t tile_bytes)
-{
-    mk_mbar_expect_tx(&bar[buf], tile_bytes);
-    mk_tma_load_1d(s_pos + buf * T, A.tpos + (size_t)tile * T, T * sizeof(float4), &bar[buf]);
-    mk_tma_load_1d(s_amp + buf * T, A.tamp + (size_t)tile * T, T * sizeof(float2), &bar[buf]);
-}
-
-// Tile atoms in shared memory come in interleaved pairs (see mk_tiles_build):
-// float4 P[2q] = (x0, x1, y0, y1), P[2q+1] = (z0, z1, w0, w1) and
-// float4 E[q] = (re0, re1, im0, im1) for atoms 2q, 2q+1.
-struct MkAtom {
-    float4 a;   // x, y, z (cycles), |D|^2
-    float2 e;   // amplitude
-};
-__device__ __forceinline__ void mk_atom_pair(const float4 *__restrict__ P,
-                                             const float4 *__restrict__ E, int q, MkAtom &u,
-                                             MkAtom &v)
-{
-    const float4 A = P[2 * q], B = P[2 * q + 1], M = E[q];
-    u.a = make_float4(A.x, A.z, B.x, B.z);
-    v.a = make_float4(A.y, A.w, B.y, B.w);
-    u.e = make_float2(M.x, M.z);
-    v.e = make_float2(M.y, M.w);
-}
-
-// The terms of one tile against PIX pixels: csr/csi += E_j exp(2 pi i phase).
-// FR adds the |d|^2 term of the in-tile distance (db = D.b per atom).
-template <int PIX, bool FR, bool CPLX>
-__device__ __forceinline__ void mk_atom_terms(const MkAtom &at, const float (&wx)[PIX],
-                                              const float (&wy)[PIX], const float (&wz)[PIX],
-                                              const float (&hq)[PIX], float bx, float by,
-                                              float bz, float (&csr)[PIX], float (&csi)[PIX])
-{
-    const float4 a = at.a;
-    const float2 e = at.e;
-    float db = 0.f;
-    if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
-#pragma unroll
-    for (int p = 0; p < PIX; ++p) {
-        float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
-        if (FR) {
-            const float sp = db - lin;
-            lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
-        }
-        const float r = mk_frac_nearest(lin);
-        float sn, cs;
-        __sincosf(r * TWO_PI_F, &sn, &cs);
-        if (CPLX) {
-            csr[p] = fmaf(e.x, cs, fmaf(-e.y, sn, csr[p]));
-            csi[p] = fmaf(e.x, sn, fmaf(e.y, cs, csi[p]));
-        } else {
-            csr[p] = fmaf(e.x, cs, csr[p]);
-            csi[p] = fmaf(e.x, sn, csi[p]);
-        }
-    }
-}
-
-template <int PIX, bool FR, bool CPLX>
-__device__ __forceinline__ void mk_tile_terms(const float4 *__restrict__ P,
-                                              const float4 *__restrict__ E, int T,
-                                              const float (&wx)[PIX], const float (&wy)[PIX],
-                                              const float (&wz)[PIX], const float (&hq)[PIX],
-                                              float bx, float by, float bz, float (&csr)[PIX],
-                                              float (&csi)[PIX])
-{
-#pragma unroll 2
-    for (int q = 0; q < T / 2; ++q) {
-        MkAtom u, v;
-        mk_atom_pair(P, E, q, u, v);
-        mk_atom_terms<PIX, FR, CPLX>(u, wx, wy, wz, hq, bx, by, bz, csr, csi);
-        mk_atom_terms<PIX, FR, CPLX>(v, wx, wy, wz, hq, bx, by, bz, csr, csi);
-    }
-}
-
-// The terms of one tile with a per-atom analyser multiplier
-//   m = (t <= th) ? g0 + g1 t : 0,   t = D.g (the change of the squared chord
-// |r_hat - c|^2 across the tile, linear in the offset D). Top-hat pixels that
-// straddle the acceptance edge in this tile use (th = x_accept - x0, g0 = 1,
-// g1 = 0); Darwin pixels the first-order expansion of the roll-off
-// (th = inf); pixels with one factor for the whole tile (g0, g1 = 0, inf).
-template <int PIX, bool FR, bool CPLX>
-__device__ __forceinline__ void mk_atom_terms_ana(
-    const MkAtom &at, const float (&wx)[PIX], const float (&wy)[PIX], const float (&wz)[PIX],
-    const float (&hq)[PIX], float bx, float by, float bz, const float (&gx)[PIX],
-    const float (&gy)[PIX], const float (&gz)[PIX], const float (&th)[PIX],
-    const float (&g0)[PIX], const float (&g1)[PIX], float (&csr)[PIX], float (&csi)[PIX])
-{
-    const float4 a = at.a;
-    const float2 e = at.e;
-    float db = 0.f;
-    if (FR) db = fmaf(a.z, bz, fmaf(a.y, by, a.x * bx));
-#pragma unroll
-    for (int p = 0; p < PIX; ++p) {
-        float lin = fmaf(a.z, wz[p], fmaf(a.y, wy[p], a.x * wx[p]));
-        if (FR) {
-            const float sp = db - lin;
-            lin = fmaf(fmaf(-sp, sp, a.w), hq[p], lin);
-        }
-        const float t = fmaf(a.z, gz[p], fmaf(a.y, gy[p], a.x * gx[p]));
-        const float m = t <= th[p] ? fmaf(g1[p], t, g0[p]) : 0.f;
-        const float r = mk_frac_nearest(lin);
-        float sn, cs;
-        __sincosf(r * TWO_PI_F, &sn, &cs);
-        const float er = e.x * m;
-        if (CPLX) {
-            const float ei = e.y * m;
-            csr[p] = fmaf(er, cs, fmaf(-ei, sn, csr[p]));
-            csi[p] = fmaf(er, sn, fmaf(ei, cs, csi[p]));
-        } else {
-            csr[p] = fmaf(er, cs, csr[p]);
-            csi[p] = fmaf(er, sn, csi[p]);
-        }
-    }
-}
-
-template <int PIX, bool FR, bool CPLX>
-__device__ __forceinline__ void mk_tile_terms_ana(
-    const float4 *__restrict__ P, const float4 *__restrict__ E, int T, const float (&wx)[PIX],
-    const float (&wy)[PIX], const float (&wz)[PIX], const float (&hq)[PIX], float bx, float by,
-    float bz, const float (&gx)[PIX], const float (&gy)[PIX], const float (&gz)[PIX],
-    const float (&th)[PIX], const float (&g0)[PIX], const float (&g1)[PIX], float (&csr)[PIX],
-    float (&csi)[PIX])
-{
-    for (int q = 0; q < T / 2; ++q) {
-        MkAtom u, v;
-        mk_atom_pair(P, E, q, u, v);
-        mk_atom_terms_ana<PIX, FR, CPLX>(u, wx, wy, wz, hq, bx, by, bz, gx, gy, gz, th, g0, g1, csr, csi);
-        mk_atom_terms_ana<PIX, FR, CPLX>(v, wx, wy, wz, hq, bx, by, bz, gx, gy, gz, th, g0, g1, csr, csi);
-    }
-}
-
-// Packed FP32 pairs: f32x2 instructions (sm_100 and later) apply one IEEE
-// fp32 operation to both halves of a 64-bit register pair. The pair loop
-// below keeps two atoms in the two halves, so one instruction does the work
-// of two (the FMA pipe's float rate is unchanged; issue slots halve).
-typedef unsigned long long mk_f2;
-__device__ __forceinline__ mk_f2 f2_pack(float lo, float hi)
-{
-    mk_f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ float2 f2_unpack(mk_f2 v)
-{
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-    return r;
-}
-__device__ __forceinline__ mk_f2 f2_fma(mk_f2 a, mk_f2 b, mk_f2 c)
-{
-    mk_f2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ mk_f2 f2_mul(mk_f2 a, mk_f2 b)
-{
-    mk_f2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ mk_f2 f2_add(mk_f2 a, mk_f2 b)
-{
-    mk_f2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ mk_f2 f2_sub(mk_f2 a, mk_f2 b)
-{
-    mk_f2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ mk_f2 f2_splat(float x) { return f2_pack(x, x); }
-
-// Pixel pairs (a, b) that are neighbours on the detector: with
-// sigma = D.(w_a + w_b)/2 (cycles) and delta = pi D.(w_a - w_b) (radians),
-//   exp(2 pi i D.w_a) = exp(2 pi i sigma) exp(+i delta),
-//   exp(2 pi i D.w_b) = exp(2 pi i sigma) exp(-i delta).
-// sigma takes the MUFU sin/cos; delta is small (|delta| <= pi |D| |w_a - w_b|,
-// bounded by the host), so cos/sin(delta) are Taylor polynomials on the FMA
-// pipe, with the atom's (real) amplitude e folded into their coefficients:
-//   SHORT (|delta| <= MK_PAIR_SHORT_DELTA): e cos = e - (e/2) d^2,
-//         e sin = delta (e - (e/6) d^2); truncation below delta^4/24 = 1e-6;
-//   long  (|delta| <= 0.5): through d^6 and d^5; below delta^7/7! = 1.6e-6.
-// One MUFU sin/cos for two terms instead of two. Sums kept as
-// P = sum e e^{i sigma} cos(delta) and S = sum e e^{i sigma} sin(delta)
-// (Q = i S); pixel a = P + i S, pixel b = P - i S. Every quantity of the
-// loop is an f32x2 pair over the tile's atoms 2q and 2q+1 (interleaved in
-// shared memory); the two halves of the accumulators are added at the end.
-#define MK_PAIR_SHORT_DELTA 0.07f
-#ifndef MK_PAIR_UNROLL
-#define MK_PAIR_UNROLL 32
-#endif
-constexpr int kPairUnroll = MK_PAIR_UNROLL / 2;   // atom pairs per unrolled step
-template <int NPAIR, bool FR, bool CPLX, bool SHORT>
-__device__ __forceinline__ void mk_tile_terms_pair(
-    const float4 *__restrict__ P, const float4 *__restrict__ E, int T, const mk_f2 (&sx)[NPAIR],
-    const mk_f2 (&sy)[NPAIR], const mk_f2 (&sz)[NPAIR], const mk_f2 (&dx)[NPAIR],
-    const mk_f2 (&dy)[NPAIR], const mk_f2 (&dz)[NPAIR], const mk_f2 (&hq)[NPAIR], mk_f2 bx,
-    mk_f2 by, mk_f2 bz, mk_f2 (&pr)[NPAIR], mk_f2 (&pi)[NPAIR], mk_f2 (&sr)[NPAIR],
-    mk_f2 (&si)[NPAIR])
-{
-    const mk_f2 magic = f2_splat(MK_ROUND_MAGIC), two_pi = f2_splat(TWO_PI_F);
-    const mk_f2 one = f2_splat(1.f), m_one = f2_splat(-1.f);
-    const mk_f2 k2 = f2_splat(-0.5f), k3 = f2_splat(-1.f / 6.f);
-    const mk_f2 k4 = f2_splat(1.f / 24.f), k5 = f2_splat(1.f / 120.f), k6 = f2_splat(-1.f / 720.f);
-    const ulonglong2 *P2 = reinterpret_cast<const ulonglong2 *>(P);
-    const ulonglong2 *E2 = reinterpret_cast<const ulonglong2 *>(E);
-#pragma unroll (kPairUnroll)
-    for (int q = 0; q < T / 2; ++q) {
-        const ulonglong2 A = P2[2 * q], B = P2[2 * q + 1], M = E2[q];
-        const mk_f2 X = A.x, Y = A.y, Z = B.x, W = B.y, ER = M.x, EI = M.y;
-        mk_f2 db = 0ull;
-        if (FR) db = f2_fma(Z, bz, f2_fma(Y, by, f2_mul(X, bx)));
-        // per-atom polynomial coefficients (amplitude folded in when real)
-        const mk_f2 e0 = CPLX ? one : ER;
-        const mk_f2 c2 = f2_mul(e0, k2), s2 = f2_mul(e0, k3);
-        mk_f2 c4 = 0ull, s4 = 0ull, c6 = 0ull;
-        if (!SHORT) {
-            c4 = f2_mul(e0, k4);
-            s4 = f2_mul(e0, k5);
-            c6 = f2_mul(e0, k6);
-        }
-        mk_f2 EIn = 0ull;
-        if (CPLX) EIn = f2_mul(EI, m_one);
-#pragma unroll
-        for (int p = 0; p < NPAIR; ++p) {
-            mk_f2 sig = f2_fma(Z, sz[p], f2_fma(Y, sy[p], f2_mul(X, sx[p])));
-            if (FR) {
-                const mk_f2 sp = f2_sub(db, sig);
-                sig = f2_fma(f2_fma(f2_mul(sp, m_one), sp, W), hq[p], sig);
-            }
-            const mk_f2 del = f2_fma(Z, dz[p], f2_fma(Y, dy[p], f2_mul(X, dx[p])));
-            const mk_f2 rr = f2_mul(f2_sub(sig, f2_sub(f2_add(sig, magic), magic)), two_pi);
-            const float2 r = f2_unpack(rr);
-            float s0, c0, s1, c1;
-            __sincosf(r.x, &s0, &c0);
-            __sincosf(r.y, &s1, &c1);
-            mk_f2 ec = f2_pack(c0, c1), es = f2_pack(s0, s1);
-            const mk_f2 d2 = f2_mul(del, del);
-            mk_f2 cd, sd;
-            if (SHORT) {
-                cd = f2_fma(d2, c2, e0);
-                sd = f2_mul(del, f2_fma(d2, s2, e0));
-            } else {
-                cd = f2_fma(d2, f2_fma(d2, f2_fma(d2, c6, c4), c2), e0);
-                sd = f2_mul(del, f2_fma(d2, f2_fma(d2, s4, s2), e0));
-            }
-            if (CPLX) {
-                const mk_f2 c = ec;
-                ec = f2_fma(ER, c, f2_mul(EIn, es));
-                es = f2_fma(ER, es, f2_mul(EI, c));
-            }
-            pr[p] = f2_fma(ec, cd, pr[p]);
-            pi[p] = f2_fma(es, cd, pi[p]);
-            sr[p] = f2_fma(es, sd, sr[p]);
-            si[p] = f2_fma(ec, sd, si[p]);
-        }
-    }
-}
-
-template <int NT, int PIX, bool FRESNEL, bool CPLX, bool PAIR, bool ANA>
-__global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ MkSplitArgs A)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    const int T = A.tile_atoms;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    long long *s_item = reinterpret_cast<long long *>(smem + 64);
-    float4 *s_pos = reinterpret_cast<float4 *>(smem + 128);     // [2][T]
-    float2 *s_amp = reinterpret_cast<float2 *>(s_pos + 2 * T);   // [2][T]
-    const int tid = threadIdx.x;
-    const uint32_t tile_bytes = (uint32_t)T * (uint32_t)(sizeof(float4) + sizeof(float2));
-
-    if (tid == 0) {
-        mk_mbar_init(&bar[0], 1);
-        mk_mbar_init(&bar[1], 1);
-        mk_fence_barrier_init();
-    }
-    __syncthreads();
-    unsigned it = 0;   // tiles consumed by this block: selects buffer and phase
-
-    for (;;) {
-        if (tid == 0) *s_item = (long long)atomicAdd(A.counter, 1ull);
-        __syncthreads();
-        const long long item = *s_item;
-        __syncthreads();                    // s_item may be rewritten next round
-        if (item >= A.n_items) break;
-
-        // item -> (frame, pixel block, slice)
-        int f = 0;
-        if (A.n_frames > 1) {
-            int lo = 0, hi = A.n_frames - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (A.frames[mid].item_off <= item) lo = mid; else hi = mid - 1;
-            }
-            f = lo;
-        }
-        const mk_frame_desc F = A.n_frames > 1 ? A.frames[f] : A.f0;
-        const long long local = item - F.item_off;
-        const int pb = (int)(local % F.pix_blocks);
-        const int slice = (int)(local / F.pix_blocks);
-        const int t_lo = slice * F.tiles_per_slice;
-        const int t_hi = min(A.n_tiles, t_lo + F.tiles_per_slice);
-        if (tid == 0) {
-            mk_issue_tile(A, s_pos, s_amp, bar, it & 1, t_lo, T, tile_bytes);
-            if (t_lo + 1 < t_hi) mk_issue_tile(A, s_pos, s_amp, bar, (it + 1) & 1, t_lo + 1, T, tile_bytes);
-        }
-
-        int pix[PIX];
-        float accr[PIX], acci[PIX], cmpr[PIX], cmpi[PIX];
-#pragma unroll
-        for (int p = 0; p < PIX; ++p) {
-            // PAIR: pixels 2j, 2j+1 of the thread are detector neighbours
-            // (consecutive indices; the host only pairs within rows)
-            pix[p] = PAIR ? pb * (NT * PIX) + 2 * ((p >> 1) * NT + tid) + (p & 1)
-                          : pb * (NT * PIX) + p * NT + tid;
-            accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
-        }
-
-        for (int t = t_lo; t < t_hi; ++t, ++it) {
-            const int buf = it & 1;
-            const uint32_t parity = (it >> 1) & 1u;
-            const double4 o = A.origin[t];
-            const float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
-            // Per (tile, pixel): w = b - u' in registers for the atom loop.
-            float wx[PIX], wy[PIX], wz[PIX], hq[PIX];
-#pragma unroll
-            for (int p = 0; p < PIX; ++p) {
-                const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
-                const float4 uu = A.u[g];
-                const float uo = fmaf(uu.z, oz, fmaf(uu.y, oy, uu.x * ox));
-                wx[p] = F.b[0] - (uu.x - (ox - uo * uu.x) * uu.w);
-                wy[p] = F.b[1] - (uu.y - (oy - uo * uu.y) * uu.w);
-                wz[p] = F.b[2] - (uu.z - (oz - uo * uu.z) * uu.w);
-                // 1 / (2 kappa |P - o|) for the |d|^2 term (D is in cycles).
-                hq[p] = FRESNEL ? 0.5f * uu.w / (A.kappa * fmaf(-uo, uu.w, 1.f)) : 0.f;
-            }
-            // Analyser per (tile, pixel), in FP64: x0 = |u' - c|^2 at the tile
-            // origin and its gradient in the offset D; a top-hat factor is one
-            // number for the whole tile unless the tile's spread of x crosses
-            // the acceptance edge.
-            float agx[PIX], agy[PIX], agz[PIX], ath[PIX], ag0[PIX], ag1[PIX];
-            bool warp_atom = false, warp_zero = false;
-            if constexpr (ANA) {
-                bool need_atom = false, all_zero = true;
-#pragma unroll
-                for (int p = 0; p < PIX; ++p) {
-                    const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
-                    const double4 qq = A.q[g];
-                    const double ip = (double)A.u[g].w;
-                    const double ux = A.an_b[0] - qq.x * A.inv_kappa;
-                    const double uy = A.an_b[1] - qq.y * A.inv_kappa;
-                    const double uz = A.an_b[2] - qq.z * A.inv_kappa;
-                    const double uo = ux * o.x + uy * o.y + uz * o.z;
-                    const double px_ = ux - (o.x - uo * ux) * ip;
-                    const double py_ = uy - (o.y - uo * uy) * ip;
-                    const double pz_ = uz - (o.z - uo * uz) * ip;
-                    const double vx = px_ - A.an_c[0], vy = py_ - A.an_c[1], vz = pz_ - A.an_c[2];
-                    const double x0 = vx * vx + vy * vy + vz * vz;
-                    const double ro = ip / (1.0 - uo * ip);          // 1 / |P - o|
-                    const double vu = vx * px_ + vy * py_ + vz * pz_;
-                    const double gs = -2.0 * ro * A.inv_kappa;       // per cycle of D
-                    const double gxd = gs * (vx - vu * px_), gyd = gs * (vy - vu * py_),
-                                 gzd = gs * (vz - vu * pz_);
-                    agx[p] = (float)gxd; agy[p] = (float)gyd; agz[p] = (float)gzd;
-                    const double rho = o.w;
-                    const double spread = sqrt(gxd * gxd + gyd * gyd + gzd * gzd) * rho / A.inv_kappa +
-                                          4.0 * rho * rho * ro * ro;
-                    ath[p] = INFINITY;
-                    ag1[p] = 0.f;
-                    if (A.analyser == 1) {
-                        if (x0 + spread <= A.an_xacc) {
-                            ag0[p] = 1.f;
-                        } else if (x0 - spread > A.an_xacc) {
-                            ag0[p] = 0.f;
-                        } else {
-                            ag0[p] = 1.f;
-                            ath[p] = (float)(A.an_xacc - x0);
-                            need_atom = true;
-                        }
-                    } else if (A.analyser == 2 && A.an_hw > 0.0) {
-                        // G(x) = 1 / (1 + theta^2 / hw^2), theta = 2 asin(sqrt(x)/2);
-                        // dtheta^2/dx = (theta / sqrt x) / sqrt(1 - x/4)
-                        const double sx = sqrt(x0);
-                        const double thv = 2.0 * asin(fmin(0.5 * sx, 1.0));
-                        const double ts = sx > 1e-6 ? thv / sx : 1.0 + x0 / 24.0;
-                        const double r = thv / A.an_hw;
-                        const double G0 = 1.0 / (1.0 + r * r);
-                        const double G1 = -G0 * G0 * ts / sqrt(fmax(1.0 - 0.25 * x0, 1e-30)) /
-                                          (A.an_hw * A.an_hw);
-                        ag0[p] = (float)G0;
-                        ag1[p] = (float)G1;
-                        need_atom = true;
-                    } else {
-                        ag0[p] = 1.f;
-                    }
-                    if (pix[p] < F.n_pix && ag0[p] != 0.f) all_zero = false;
-                }
-                warp_atom = __any_sync(0xffffffffu, need_atom);
-                warp_zero = __all_sync(0xffffffffu, all_zero && !need_atom);
-            }
-            const bool ok = mk_mbar_wait_bounded(&bar[buf], parity, MK_WAIT_LIMIT_NS);
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
-                    atomicExch(A.status, MK_DEV_TIMEOUT_TMA);
-                    // Let any copy still in flight land before the block's
-                    // shared memory is released (bounded as well).
-                    mk_mbar_wait_bounded(&bar[buf ^ 1], ((it + 1) >> 1) & 1u, MK_WAIT_LIMIT_NS / 2);
-                }
-                return;
-            }
-            const float4 *P = s_pos + buf * T;
-            // T float2 amplitudes = T/2 float4 (interleaved atom pairs)
-            const float4 *E = reinterpret_cast<const float4 *>(s_amp + buf * T);
-            float csr[PIX], csi[PIX];
-#pragma unroll
-            for (int p = 0; p < PIX; ++p) csr[p] = csi[p] = 0.f;
-            // The |d|^2 term only for tiles wide enough to need it (uniform
-            // across the block: no divergence).
-            const bool fr_tile = FRESNEL && (float)o.w > A.fres_r;
-            if constexpr (PAIR) {
-                constexpr int NP = PIX / 2;
-                mk_f2 sx[NP], sy[NP], sz[NP], dx[NP], dy[NP], dz[NP], hp[NP];
-                mk_f2 pr[NP], pi_[NP], sr[NP], si[NP];
-#pragma unroll
-                for (int q = 0; q < NP; ++q) {
-                    const int a = 2 * q, b = 2 * q + 1;
-                    sx[q] = f2_splat(0.5f * (wx[a] + wx[b]));
-                    sy[q] = f2_splat(0.5f * (wy[a] + wy[b]));
-                    sz[q] = f2_splat(0.5f * (wz[a] + wz[b]));
-                    dx[q] = f2_splat(3.14159265358979f * (wx[a] - wx[b]));
-                    dy[q] = f2_splat(3.14159265358979f * (wy[a] - wy[b]));
-                    dz[q] = f2_splat(3.14159265358979f * (wz[a] - wz[b]));
-                    hp[q] = f2_splat(0.5f * (hq[a] + hq[b]));
-                    pr[q] = pi_[q] = sr[q] = si[q] = 0ull;    // +0.0f in both halves
-                }
-                const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
-                // the short delta polynomial for tiles small enough (uniform
-                // across the block, like fr_tile)
-                const bool short_tile = (float)o.w <= A.pair_short_r;
-                if (fr_tile) {
-                    if (short_tile)
-                        mk_tile_terms_pair<NP, true, CPLX, true>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                 bx, by, bz, pr, pi_, sr, si);
-                    else
-                        mk_tile_terms_pair<NP, true, CPLX, false>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                  bx, by, bz, pr, pi_, sr, si);
-                } else {
-                    if (short_tile)
-                        mk_tile_terms_pair<NP, false, CPLX, true>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                  bx, by, bz, pr, pi_, sr, si);
-                    else
-                        mk_tile_terms_pair<NP, false, CPLX, false>(P, E, T, sx, sy, sz, dx, dy, dz, hp,
-                                                                   bx, by, bz, pr, pi_, sr, si);
-                }
-#pragma unroll
-                for (int q = 0; q < NP; ++q) {
-                    // halves = even and odd atoms of the tile
-                    const float2 a = f2_unpack(pr[q]), b = f2_unpack(pi_[q]);
-                    const float2 c = f2_unpack(sr[q]), d = f2_unpack(si[q]);
-                    const float P_re = a.x + a.y, P_im = b.x + b.y;
-                    const float S_im = c.x + c.y, S_re = d.x + d.y;   // Q = i S
-                    csr[2 * q] = P_re - S_im;
-                    csi[2 * q] = P_im + S_re;
-                    csr[2 * q + 1] = P_re + S_im;
-                    csi[2 * q + 1] = P_im - S_re;
-                }
-            } else if (ANA && warp_zero) {
-                // every pixel of the warp is outside the acceptance for this tile
-            } else if (ANA && warp_atom) {
-                if (fr_tile)
-                    mk_tile_terms_ana<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
-                                                       agx, agy, agz, ath, ag0, ag1, csr, csi);
-                else
-                    mk_tile_terms_ana<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
-                                                        agx, agy, agz, ath, ag0, ag1, csr, csi);
-            } else {
-                if (fr_tile)
-                    mk_tile_terms<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
-                else
-                    mk_tile_terms<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
-                if constexpr (ANA) {
-#pragma unroll
-                    for (int p = 0; p < PIX; ++p) {   // one analyser factor per (tile, pixel)
-                        csr[p] *= ag0[p];
-                        csi[p] *= ag0[p];
-                    }
-                }
-            }
-            __syncthreads();   // every thread is done with buffer `buf`
-            if (tid == 0 && t + 2 < t_hi) {
-                mk_fence_proxy_async();
-                mk_issue_tile(A, s_pos, s_amp, bar, buf, t + 2, T, tile_bytes);
-            }
-            // Fold: tile sum x factor x exp(2 pi i phi0), Kahan-compensated.
-            const int s = A.tspecies[t];
-            const float oo = fmaf(oz, oz, fmaf(oy, oy, ox * ox));
-#pragma unroll
-            for (int p = 0; p < PIX; ++p) {
-                const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
-                const float4 uu = A.u[g];
-                const double4 qq = A.q[g];
-                const float uo = fmaf(uu.z, oz, fmaf(uu.y, oy, uu.x * ox));
-                const double q0 = qq.x * o.x + qq.y * o.y + qq.z * o.z;
-                float ph = (float)(q0 - rint(q0)) + A.kappa * 0.5f * fmaf(-uo, uo, oo) * uu.w;
-                ph -= rintf(ph);
-                float s0, c0;
-                __sincosf(ph * TWO_PI_F, &s0, &c0);
-                const float2 Fc = mk_factor(A, s, F, wx[p], wy[p], wz[p], (float)qq.w,
-                                            1.f / fmaf(-uo, uu.w, 1.f));
-                const float gr = Fc.x * c0 - Fc.y * s0, gi = Fc.x * s0 + Fc.y * c0;
-                const float tr = csr[p] * gr - csi[p] * gi;
-                const float ti = csr[p] * gi + csi[p] * gr;
-                float y = tr - cmpr[p];
-                float z = accr[p] + y;
-                cmpr[p] = (z - accr[p]) - y;
-                accr[p] = z;
-                y = ti - cmpi[p];
-                z = acci[p] + y;
-                cmpi[p] = (z - acci[p]) - y;
-                acci[p] = z;
-            }
-        }
-#pragma unroll
-        for (int p = 0; p < PIX; ++p) {
-            if (pix[p] < F.n_pix)
-                A.partial[F.part_off + (long long)slice * F.n_pix + pix[p]] =
-                    make_double2((double)accr[p] - (double)cmpr[p], (double)acci[p] - (double)cmpi[p]);
-        }
-    }
 }
 
 // Test hook for the bounded-wait path: one block waits on an mbarrier that
@@ -770,53 +163,14 @@ int mk_launch_reduce(const double2 *partial, int slices, int n_pix, const double
 }
 
 // ----------------------------------------------------------------- launch
-typedef void (*mk_split_fn)(const MkSplitArgs);
-
-template <int NT, int PIX, bool PAIR, bool ANA>
-static mk_split_fn mk_pick4(bool fresnel, bool cplx)
-{
-    if (fresnel)
-        return cplx ? mk_split_kernel<NT, PIX, true, true, PAIR, ANA>
-                    : mk_split_kernel<NT, PIX, true, false, PAIR, ANA>;
-    return cplx ? mk_split_kernel<NT, PIX, false, true, PAIR, ANA>
-                : mk_split_kernel<NT, PIX, false, false, PAIR, ANA>;
-}
-
-// Pairs need an even PIX; the analyser kernels (no pairs) exist for
-// 128/256 threads and 2 or 4 pixels per thread.
-template <int NT, int PIX>
-static mk_split_fn mk_pick3(bool fresnel, bool cplx, bool pair, bool ana)
-{
-    if (ana) {
-        if constexpr ((NT == 128 || NT == 256) && (PIX == 2 || PIX == 4))
-            return pair ? nullptr : mk_pick4<NT, PIX, false, true>(fresnel, cplx);
-        return nullptr;
-    }
-    if constexpr (PIX % 2 == 0) {
-        if (pair) return mk_pick4<NT, PIX, true, false>(fresnel, cplx);
-    } else {
-        if (pair) return nullptr;
-    }
-    return mk_pick4<NT, PIX, false, false>(fresnel, cplx);
-}
-
 static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, bool pair, bool ana)
 {
-#define MK_PIX_CASES(NT_)                                                  \
-    switch (pix) {                                                         \
-    case 1: return mk_pick3<NT_, 1>(fresnel, cplx, pair, ana);             \
-    case 2: return mk_pick3<NT_, 2>(fresnel, cplx, pair, ana);             \
-    case 4: return mk_pick3<NT_, 4>(fresnel, cplx, pair, ana);             \
-    case 8: return mk_pick3<NT_, 8>(fresnel, cplx, pair, ana);             \
-    default: return nullptr;                                               \
-    }
     switch (nt) {
-    case 64: MK_PIX_CASES(64)
-    case 128: MK_PIX_CASES(128)
-    case 256: MK_PIX_CASES(256)
+    case 64: return mk_pick_nt64(pix, fresnel, cplx, pair, ana);
+    case 128: return mk_pick_nt128(pix, fresnel, cplx, pair, ana);
+    case 256: return mk_pick_nt256(pix, fresnel, cplx, pair, ana);
     default: return nullptr;
     }
-#undef MK_PIX_CASES
 }
 
 static size_t mk_split_smem(int T) { return 128 + (size_t)2 * T * (sizeof(float4) + sizeof(float2)); }
