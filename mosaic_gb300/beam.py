@@ -388,8 +388,35 @@ class beam:
                                                     fresnel_rad=fresnel_term,
                                                     fresnel_radius_m=fresnel_radius)
 
-    def scatter_device(self, atoms, pix, phys, out=None, accumulate=False, launch=None):
-        """Run the configured sum on staged atoms/pixels; float64 (P, 2) on the device."""
+    MAX_SPLIT_DEPTH = 6
+
+    def scatter_device(self, atoms, pix, phys, out=None, accumulate=False, launch=None, _depth=0):
+        """Run the configured sum on staged atoms/pixels; float64 (P, 2) on the
+        device. When device memory runs out the atoms are summed in halves
+        into the same field, down to 1/64 of the sample, as the reference
+        retries its chunks (Beam.py:1496-1502); then RuntimeError."""
+        try:
+            return self._scatter_once(atoms, pix, phys, out, accumulate, launch)
+        except (torch.cuda.OutOfMemoryError, MemoryError) as e:
+            if _depth >= self.MAX_SPLIT_DEPTH or atoms.n < 2:
+                raise RuntimeError("out of device memory even for one kernel chunk") from e
+        torch.cuda.empty_cache()
+        if out is None:
+            out = torch.zeros((pix.n, 2), dtype=torch.float64, device=pix.xyz.device)
+            accumulate = True
+        half = atoms.n // 2
+        for k, sl in enumerate((slice(0, half), slice(half, atoms.n))):
+            sp = atoms.species[sl]
+            counts = torch.bincount(sp.long(), minlength=len(atoms.table.labels)).cpu().numpy()
+            part = engine.Atoms(atoms.pos[sl], sp, atoms.amp[sl], counts.astype(np.int64),
+                                atoms.table)
+            self.scatter_device(part, pix, phys, out=out, accumulate=accumulate or k > 0,
+                                launch=launch, _depth=_depth + 1)
+        self.last_run = dict(self.last_run,
+                             memory_splits=max(self.last_run.get("memory_splits", 0), _depth + 1))
+        return out
+
+    def _scatter_once(self, atoms, pix, phys, out=None, accumulate=False, launch=None):
         if self._use_fast_kernel and atoms.n > 0:
             tiles = engine.Tiles(atoms, self.k, self._kernel_tile_atoms, device=atoms.pos.device)
             third, fresnel, tol, diag = self.split_budget(tiles, pix.r0_min())

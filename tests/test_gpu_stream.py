@@ -44,3 +44,41 @@ def test_disk_sample_through_the_entry_point(cuda, tmp_path):
     b = B.atomic_scattering_kinematic(ChunkedSample(chunks, thermal=th), D, st, **kw)
     assert np.array_equal(a, b)
     assert np.abs(a).max() > 0
+
+
+def test_device_memory_exhaustion_sums_in_halves(cuda, monkeypatch):
+    """Out of device memory while tiling: the atoms are summed in halves into
+    the same field (the failure is raised on the host by a stand-in; no GPU
+    memory is actually exhausted)."""
+    from mosaic_gb300 import engine
+    w, chunks = _crystal()
+    B = workloads._beam(10000.0, 200.0, pol_perp_rate=1.0)
+    D = Detector()
+    D.create_detector((24, 20), (5.5e5, 5.5e5))
+    D.position_detector_absolute(2.0e9, 2.0 * w.meta["theta_deg"], 0.0)
+    st = StaticStage(w.stage.rotation, w.stage.translation)
+    s = ChunkedSample(chunks)
+    kw = dict(apply_polarization=True, return_double=True)
+    ref = B.atomic_scattering_kinematic(s, D, st, **kw)
+    n_all = sum(len(p) for p, _ in chunks)
+    real_tiles = engine.Tiles
+
+    class TightTiles(real_tiles):
+        def __init__(self, atoms, *a, **k):
+            if atoms.n > n_all // 3:
+                raise torch.cuda.OutOfMemoryError("stand-in: tiles do not fit")
+            super().__init__(atoms, *a, **k)
+
+    monkeypatch.setattr(engine, "Tiles", TightTiles)
+    got = B.atomic_scattering_kinematic(s, D, st, **kw)
+    assert B.last_run.get("memory_splits") == 2 and B.last_run["path"] == "split_f32"
+    I, Ir = np.abs(got) ** 2, np.abs(ref) ** 2
+    assert np.abs(I - Ir).max() <= 1e-5 * Ir.max()
+
+    class NoTiles(real_tiles):
+        def __init__(self, atoms, *a, **k):
+            raise torch.cuda.OutOfMemoryError("stand-in: nothing fits")
+
+    monkeypatch.setattr(engine, "Tiles", NoTiles)
+    with pytest.raises(RuntimeError, match="out of device memory"):
+        B.atomic_scattering_kinematic(s, D, st, **kw)
