@@ -57,16 +57,49 @@ __global__ void __launch_bounds__(128) mk_gemm_bf16_kernel(
             for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
 
     const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    // operands contiguous in k (the forward pass): 8 bf16 per 16-byte load
+    const bool a_vec = sak == 1 && (sam & 7) == 0 && ((uintptr_t)A & 15) == 0;
+    const bool b_vec = sbk == 1 && (sbn & 7) == 0 && ((uintptr_t)B & 15) == 0;
     for (int k0 = k_lo; k0 < k_hi; k0 += MLP_BK) {
-        for (int e = tid; e < MLP_BM * MLP_BK; e += 128) {
-            const int r = e / MLP_BK, c = e % MLP_BK;
-            const int m = m0 + r, k = k0 + c;
-            As[r][c] = (m < M && k < k_hi) ? A[(long long)m * sam + (long long)k * sak] : zero;
+        if (a_vec) {
+            for (int e = tid; e < MLP_BM * MLP_BK / 8; e += 128) {
+                const int r = e / (MLP_BK / 8), c = (e % (MLP_BK / 8)) * 8;
+                const int m = m0 + r, k = k0 + c;
+                if (m < M && k + 7 < k_hi) {
+                    *reinterpret_cast<uint4 *>(&As[r][c]) =
+                        *reinterpret_cast<const uint4 *>(A + (long long)m * sam + k);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        As[r][c + q] = (m < M && k + q < k_hi) ? A[(long long)m * sam + k + q] : zero;
+                }
+            }
+        } else {
+            for (int e = tid; e < MLP_BM * MLP_BK; e += 128) {
+                const int r = e / MLP_BK, c = e % MLP_BK;
+                const int m = m0 + r, k = k0 + c;
+                As[r][c] = (m < M && k < k_hi) ? A[(long long)m * sam + (long long)k * sak] : zero;
+            }
         }
-        for (int e = tid; e < MLP_BN * MLP_BK; e += 128) {
-            const int r = e / MLP_BK, c = e % MLP_BK;
-            const int n = n0 + r, k = k0 + c;
-            Bs[r][c] = (n < N && k < k_hi) ? B[(long long)k * sbk + (long long)n * sbn] : zero;
+        if (b_vec) {
+            for (int e = tid; e < MLP_BN * MLP_BK / 8; e += 128) {
+                const int r = e / (MLP_BK / 8), c = (e % (MLP_BK / 8)) * 8;
+                const int n = n0 + r, k = k0 + c;
+                if (n < N && k + 7 < k_hi) {
+                    *reinterpret_cast<uint4 *>(&Bs[r][c]) =
+                        *reinterpret_cast<const uint4 *>(B + (long long)n * sbn + k);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        Bs[r][c + q] = (n < N && k + q < k_hi) ? B[(long long)n * sbn + k + q] : zero;
+                }
+            }
+        } else {
+            for (int e = tid; e < MLP_BN * MLP_BK; e += 128) {
+                const int r = e / MLP_BK, c = e % MLP_BK;
+                const int n = n0 + r, k = k0 + c;
+                Bs[r][c] = (n < N && k < k_hi) ? B[(long long)k * sbk + (long long)n * sbn] : zero;
+            }
         }
         __syncthreads();
 #pragma unroll

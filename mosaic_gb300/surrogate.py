@@ -344,6 +344,13 @@ class SurrogateScan:
             Y = net.predict(feats)
             sh = b.decode(net, Y[:, : b.rank].contiguous()).clamp_min_(0.0) * torch.exp(Y[:, b.rank:])
             frame_rel_error(sh, sh + 1.0)
+            # the Gram and projection products at the scan's own shapes
+            n_tr, P = max(int(self.train.sum()), 2), self.roi * self.roi
+            Xw = torch.zeros((n_tr, P), dtype=torch.float32, device=self.dev)
+            G = Xw @ Xw.T
+            torch.zeros((self.rank, n_tr), dtype=torch.float32, device=self.dev) @ Xw
+            Xw[: min(n_tr, 64)] @ torch.zeros((P, self.rank), dtype=torch.float32, device=self.dev)
+            del Xw, G
             torch.cuda.synchronize()
 
     def exact(self, idx):
