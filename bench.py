@@ -52,6 +52,14 @@ MUFU_PER_TERM, FP32_PER_TERM = 2, 12   # canonical split-phase term
 # short cos/sin polynomials 3, four accumulators 4, sin/cos argument scaling
 # 1, per-atom coefficients 1), run as packed f32x2 over atom pairs
 MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR = 1, 10
+# 2x2 pixel-quad form: one sin/cos per four terms; per quad and atom 36 FP32
+# lane operations (three dot products 9, rounding 3, scale 1, u^2 and v^2 2,
+# short cos/sin polynomials of u and v 6, the four products with the phasor 4,
+# eight accumulators 8, sin/cos argument scaling 1, per-atom coefficients 2)
+MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD = 0.5, 9
+FORMS = {0: ("one sin/cos per term", MUFU_PER_TERM, FP32_PER_TERM),
+         1: ("pixel pairs (one sin/cos per two terms)", MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR),
+         2: ("2x2 pixel quads (one sin/cos per four terms)", MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD)}
 
 
 def _dist():
@@ -332,16 +340,19 @@ def run_ours(args):
     tiles = engine.Tiles(atoms, B.k, B._kernel_tile_atoms, device=dev)
     pix = engine.Pixels(coords_m, ny, nz, phys, device=dev)
     third, fresnel, tol, diag = B.split_budget(tiles, pix.r0_min())
-    pair_delta = engine.pair_delta(tiles, pix, B.k)
-    diag["pair_delta_rad"] = pair_delta
-    pairs_ok = pair_delta <= engine.PAIR_DELTA_MAX and not args.no_pairs
+    level, ginfo = engine.pixel_grouping(tiles, pix, B.k, tol - third,
+                                         fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0)
+    diag.update(ginfo)
+    if args.no_pairs:
+        level = 0
+    elif args.no_quads:
+        level = min(level, 1)
     if args.profile:
-        launch, tune_tbl = autotune.lookup(pix.n, tiles, pairs_ok), []
+        launch, tune_tbl = autotune.lookup(pix.n, tiles, level), []
     else:
         launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel),
-                                         fresnel_radius=diag["fresnel_radius_m"], pairs_ok=pairs_ok)
-    if launch.get("pairs"):
-        launch = dict(launch, pair_short_radius_m=engine.pair_short_radius(tiles, pix, B.k))
+                                         fresnel_radius=diag["fresnel_radius_m"], level=level)
+    launch = engine.grouping_launch(launch, level, tiles, pix, B.k, ginfo)
     B._kernel_launch = launch
     amp_real = tiles.amp_is_real()
     split_times = []
@@ -435,11 +446,11 @@ def run_ours(args):
     mufu = pipes.get("sincos", MUFU_PER_CLK_SM)
     fma = pipes.get("ffma", FP32_PER_CLK_SM)
     # canonical term (2 MUFU + 12 FP32) for the roofline, whatever form runs;
-    # the pixel-pair form's own bound beside it
-    paired = bool(launch.get("pairs", 0))
+    # the running form's own bound (pixel pairs or quads) beside it
+    mode = int(launch.get("pairs", 0) or 0)
     peak_terms = min(mufu / MUFU_PER_TERM, fma / FP32_PER_TERM) * n_sm * clk * 1e6
     bound = "mufu" if mufu / MUFU_PER_TERM <= fma / FP32_PER_TERM else "fp32"
-    mufu_pt, fp32_pt = (MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR) if paired else (MUFU_PER_TERM, FP32_PER_TERM)
+    form_name, mufu_pt, fp32_pt = FORMS[mode]
     form_peak = min(mufu / mufu_pt, fma / fp32_pt) * n_sm * clk * 1e6
     achieved = terms / (split_ms * 1e-3)
     gpu_launches = args.steps * 8
@@ -477,8 +488,7 @@ def run_ours(args):
                                         f"{FP32_PER_TERM} per term), both pipes measured on this "
                                         f"GPU by mk_probe_throughput, x {n_sm} SMs x {clk:.0f} MHz "
                                         f"({peak_src} max clock)",
-                         "form": {"name": "pixel pairs (one sin/cos per two terms)" if paired
-                                  else "one sin/cos per term",
+                         "form": {"name": form_name,
                                   "mufu_per_term": mufu_pt, "fp32_per_term": fp32_pt,
                                   "peak": form_peak / 1e9, "frac": achieved / form_peak},
                          "pipe_probe_ops_per_clk_per_sm": pipes,
@@ -517,7 +527,9 @@ def main():
     ap.add_argument("--surrogate-verify", type=int, default=64,
                     help="unjudged predicted frames checked against the exact sum (untimed)")
     ap.add_argument("--no-pairs", action="store_true",
-                    help="one sin/cos per term (the pixel-pair form off)")
+                    help="one sin/cos per term (the pixel-pair and quad forms off)")
+    ap.add_argument("--no-quads", action="store_true",
+                    help="at most one sin/cos per pixel pair (the 2x2 quad form off)")
     ap.add_argument("--scan-frames", type=int, default=48,
                     help="frames of the batched-scan leg (0: skip)")
     ap.add_argument("--profile", action="store_true",

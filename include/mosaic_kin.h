@@ -96,7 +96,7 @@ typedef struct {
  * ROI), as filled by mk_scan_plan and read by the kernel from device
  * memory. The frames' pixels are consecutive in one set of mk_pixels
  * arrays; b and e are the incident direction and polarization vector in the
- * frame of the atoms (the sample frame for scans). 64 bytes. */
+ * frame of the atoms (the sample frame for scans). 80 bytes. */
 typedef struct {
     long long pix_off;    /* first pixel of the frame in the concatenated pixel arrays */
     long long part_off;   /* first entry of its partial fields in the workspace */
@@ -107,6 +107,9 @@ typedef struct {
     int pix_blocks;       /* ceil(n_pix / (threads * pix_per_thread)) */
     float b[3];
     float e[3];
+    int row;              /* pixels per detector row (0: unknown); pixel quads need it even,
+                             with an even number of rows */
+    int reserved[3];
 } mk_frame_desc;
 
 /* Atom tiles for the split-phase kernel, filled by mk_tiles_build. Tiles
@@ -137,9 +140,16 @@ typedef struct {
     int pairs;            /* 1: pixels 2j, 2j+1 of every frame share one MUFU sin/cos (their
                              phase difference on FMA-pipe polynomials); the caller checks that
                              the half difference pi |D| |w_a - w_b| stays below 0.5 rad for
-                             every tile (pix_per_thread even) */
-    double pair_short_radius_m; /* with pairs: tiles up to this radius keep the half
-                             difference below 0.07 rad and use the short polynomial
+                             every tile (pix_per_thread even).
+                             2: 2x2 pixel quads (two neighbours in a row and the two below
+                             them) share one sin/cos; the two half differences along the row
+                             and across rows go to polynomials and the quad's mixed second
+                             difference (pi/2) D.(w_a + w_d - w_b - w_c) is dropped: the caller
+                             checks the half differences as for pairs and the dropped term
+                             against its phase budget (pix_per_thread 4 or 8; every frame
+                             needs an even row length and an even number of rows) */
+    double pair_short_radius_m; /* with pairs or quads: tiles up to this radius keep the half
+                             differences below 0.07 rad and use the short polynomials
                              (0: none does) */
 } mk_launch;
 
@@ -262,14 +272,17 @@ int mk_kin_split_f32_noalloc(const mk_tiles *tiles, const mk_species *sp,
 
 /* --- batched scans ------------------------------------------------------ */
 /* Plan a batched launch of n_frames frames (host only, no GPU work):
- * frame_pixels (n_frames) pixels per frame; beam_dirs / pol_es (n_frames, 3)
+ * frame_pixels (n_frames) pixels per frame; frame_rows (n_frames) pixels per
+ * detector row of each frame, or NULL (then no pixel quads); beam_dirs /
+ * pol_es (n_frames, 3)
  * incident direction and polarization vector per frame in the sample frame.
  * Fills frames_out (host, n_frames) and the totals of work items and
  * partial-field entries. Copy frames_out to the device for mk_kin_scan_f32.
  * Replaces the per-step loop of experiment.scan_nD (Experiment.py:285-336),
  * which re-runs the whole exposure per step. */
-int mk_scan_plan(int n_frames, const int *frame_pixels, const double *beam_dirs,
-                 const double *pol_es, const mk_tiles *tiles, const mk_launch *launch,
+int mk_scan_plan(int n_frames, const int *frame_pixels, const int *frame_rows,
+                 const double *beam_dirs, const double *pol_es, const mk_tiles *tiles,
+                 const mk_launch *launch,
                  mk_frame_desc *frames_out, long long *n_items, long long *n_partial);
 size_t mk_scan_workspace_size(long long n_partial);
 

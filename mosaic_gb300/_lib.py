@@ -132,7 +132,8 @@ class MkFrameDesc(ctypes.Structure):
     _fields_ = [("pix_off", ctypes.c_longlong), ("part_off", ctypes.c_longlong),
                 ("item_off", ctypes.c_longlong), ("n_pix", ctypes.c_int), ("slices", ctypes.c_int),
                 ("tiles_per_slice", ctypes.c_int), ("pix_blocks", ctypes.c_int),
-                ("b", ctypes.c_float * 3), ("e", ctypes.c_float * 3)]
+                ("b", ctypes.c_float * 3), ("e", ctypes.c_float * 3), ("row", ctypes.c_int),
+                ("reserved", ctypes.c_int * 3)]
 
 
 class MkTiles(ctypes.Structure):
@@ -206,7 +207,7 @@ SIGNATURES = {
     "mk_kin_split_f32_noalloc": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkSpecies),
                                                 ctypes.POINTER(MkPhysics), ctypes.POINTER(MkPixels),
                                                 ctypes.POINTER(MkLaunch), _vp, ctypes.c_int, _vp]),
-    "mk_scan_plan": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, ctypes.POINTER(MkTiles),
+    "mk_scan_plan": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.POINTER(MkTiles),
                                     ctypes.POINTER(MkLaunch), _vp, ctypes.POINTER(ctypes.c_longlong),
                                     ctypes.POINTER(ctypes.c_longlong)]),
     "mk_scan_workspace_size": (ctypes.c_size_t, [ctypes.c_longlong]),

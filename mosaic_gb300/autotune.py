@@ -1,9 +1,10 @@
 """Autotuner for the split-phase kernel's launch shape.
 
-Candidates are (pixels per thread, threads per block, pixel pairs); the
+Candidates are (pixels per thread, threads per block, pixel mode); the
 slice count is then chosen inside the library to fill whole waves of the GPU.
-Pair candidates (one sin/cos shared by two neighbouring pixels) are only
-tried where the caller says the geometry allows them. Each candidate
+Pair candidates (one sin/cos shared by two neighbouring pixels) and quad
+candidates (one by a 2x2 block) are only tried where the caller says the
+geometry allows them (``level`` 1 and 2). Each candidate
 is timed with CUDA events on a probe -- the first ``PROBE_TILES`` tiles
 against every pixel, the same per-term work as the full problem -- and the
 winner is cached per (device, detector-size bucket, tile size, kernel source
@@ -23,6 +24,7 @@ from . import engine
 
 CANDIDATES = [(4, 128), (4, 256), (2, 256), (8, 128), (2, 128), (8, 64), (4, 64), (1, 256)]
 PAIR_CANDIDATES = [(4, 128), (4, 256), (8, 128), (2, 256), (8, 64)]
+QUAD_CANDIDATES = [(4, 128), (4, 256), (8, 128), (8, 64), (4, 64)]
 DEFAULT = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
 PROBE_TILES = 96
 _mem = {}
@@ -37,16 +39,16 @@ def _cache_path():
 
 def _src_hash():
     h = hashlib.sha1()
-    for name in ("mk_split.cuh", "mk_sum_f32.cu"):
+    for name in ("mk_split.cuh", "mk_sum_f32.cu", "mk_split_quad.cu"):
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", name), "rb") as fh:
             h.update(fh.read())
     return h.hexdigest()[:12]
 
 
-def _key(n_pix, tiles, pairs_ok=False):
+def _key(n_pix, tiles, level=0):
     dev = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
     bucket = 1 << max(0, (int(n_pix) - 1).bit_length())
-    return f"{dev}|{bucket}|{tiles.tile_atoms}|{'p' if pairs_ok else 's'}|{_src_hash()}"
+    return f"{dev}|{bucket}|{tiles.tile_atoms}|{'spq'[int(level)]}|{_src_hash()}"
 
 
 def _load():
@@ -72,35 +74,39 @@ def _store(key, val):
             pass
 
 
-def lookup(n_pix, tiles, pairs_ok=False):
-    key = _key(n_pix, tiles, pairs_ok)
+def lookup(n_pix, tiles, level=0):
+    key = _key(n_pix, tiles, level)
     if key in _mem:
         return dict(_mem[key])
     d = _load().get(key)
     if d:
         _mem[key] = d
         return dict(d)
-    return dict(DEFAULT, pairs=int(bool(pairs_ok)))
+    return dict(DEFAULT, pairs=int(level))
 
 
 def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, reps=3,
-         fresnel_radius=0.0, pairs_ok=False):
+         fresnel_radius=0.0, level=0):
     """Time every candidate on a probe of the tiles; cache and return the winner."""
     amp_real = tiles.amp_is_real() if amp_real is None else bool(amp_real)
+    level = int(level)
     probe = engine.TilesView(tiles, min(tiles.n_tiles, PROBE_TILES))
     if candidates is None:
         candidates = [(p, t, 0) for p, t in CANDIDATES]
-        if pairs_ok:
+        if level >= 1:
             candidates += [(p, t, 1) for p, t in PAIR_CANDIDATES]
-    short_r = engine.pair_short_radius(tiles, pix, phys.k) if pairs_ok else 0.0
+        if level >= 2:
+            candidates += [(p, t, 2) for p, t in QUAD_CANDIDATES]
+    short = {1: engine.pair_short_radius(tiles, pix, phys.k) if level >= 1 else 0.0,
+             2: engine.quad_bounds(tiles, pix, phys.k)["short_radius_m"] if level >= 2 else 0.0}
     results = []
     for cand in candidates:
         pix_pt, nt = cand[0], cand[1]
         pr = int(cand[2]) if len(cand) > 2 else 0
-        if pr and not pairs_ok:
+        if pr > level:
             continue
         cfg = dict(pix_per_thread=pix_pt, threads=nt, slices=0, pairs=pr)
-        run_cfg = dict(cfg, pair_short_radius_m=short_r)
+        run_cfg = dict(cfg, pair_short_radius_m=short.get(pr, 0.0))
         try:
             engine.run_split(probe, pix, phys, table, launch=run_cfg, fresnel=fresnel,
                              amp_real=amp_real, fresnel_radius=fresnel_radius)
@@ -118,7 +124,7 @@ def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, rep
     if not results:
         return dict(DEFAULT), []
     best = min(results, key=lambda r: r[0])[1]
-    key = _key(pix.n, tiles, pairs_ok)
+    key = _key(pix.n, tiles, level)
     _mem[key] = best
     _store(key, best)
     return dict(best), results

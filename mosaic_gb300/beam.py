@@ -427,21 +427,23 @@ class beam:
                                      declined="Darwin analyser varies too fast across a tile", **diag)
                 return engine.run_plain(atoms, pix, phys, out=out, accumulate=accumulate)
             if third <= tol and excursion < 1e-6:
-                delta = engine.pair_delta(tiles, pix, self.k)
-                pairs_ok = delta <= engine.PAIR_DELTA_MAX and not phys.analyser
-                cfg = dict(launch or self._kernel_launch or tuned_launch(pix.n, tiles, pairs_ok))
-                if not pairs_ok:
-                    cfg["pairs"] = 0
-                elif cfg.get("pairs"):
-                    cfg["pair_short_radius_m"] = engine.pair_short_radius(tiles, pix, self.k)
+                # one sin/cos per pixel pair or 2x2 quad where the geometry
+                # allows it; the quad's dropped phase shares the budget with
+                # the third-order terms
+                level, ginfo = engine.pixel_grouping(
+                    tiles, pix, self.k, tol - third,
+                    fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0,
+                    analyser=bool(phys.analyser))
+                cfg = dict(launch or self._kernel_launch or tuned_launch(pix.n, tiles, level))
                 if phys.analyser and (int(cfg.get("threads", 128)), int(cfg.get("pix_per_thread", 4))) \
                         not in engine.ANALYSER_LAUNCHES:
                     cfg.update(pix_per_thread=4, threads=128)
+                cfg = engine.grouping_launch(cfg, level, tiles, pix, self.k, ginfo)
                 res = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg,
                                        fresnel=int(fresnel), out=out, accumulate=accumulate,
                                        fresnel_radius=diag["fresnel_radius_m"])
                 self.last_run = dict(path="split_f32", n_tiles=tiles.n_tiles, fresnel=fresnel,
-                                     launch=dict(cfg), pair_delta_rad=delta, **diag)
+                                     launch=dict(cfg), **ginfo, **diag)
                 return res
             self.last_run = dict(path="plain_f64", declined="split-phase error budget", **diag)
         else:
@@ -560,8 +562,9 @@ class beam:
         return E
 
 
-def tuned_launch(n_pix, tiles, pairs_ok=False):
+def tuned_launch(n_pix, tiles, level=0):
     """Launch shape for the split kernel: the autotuner's cached winner, or
-    the default when none is cached."""
+    the default when none is cached (``level``: 0 no pixel sharing, 1 pairs,
+    2 quads allowed)."""
     from . import autotune
-    return autotune.lookup(n_pix, tiles, pairs_ok)
+    return autotune.lookup(n_pix, tiles, level)

@@ -56,7 +56,7 @@ struct MkSplitArgs {
     int apply_pol, decay, remove_forward;
     float pdeg;
     float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
-    float pair_short_r; // PAIR kernels: tiles up to this radius [m] use the short polynomial
+    float pair_short_r; // pair/quad kernels: tiles up to this radius [m] use the short polynomials
     // analyser (ANA kernels, single exposures): kind 1 top-hat / 2 Darwin,
     // beam direction and analyser axis in FP64, 4 sin^2(alpha/2), half-width
     int analyser;
@@ -370,7 +370,101 @@ __device__ __forceinline__ void mk_tile_terms_pair(
     }
 }
 
-template <int NT, int PIX, bool FRESNEL, bool CPLX, bool PAIR, bool ANA>
+// 2x2 pixel quads: pixels a, b neighbours in one detector row, c, d the two
+// below them. With sigma = D.(w_a + w_b + w_c + w_d)/4 (cycles),
+// u = (pi/2) D.(w_b + w_d - w_a - w_c) (along the row, radians),
+// v = (pi/2) D.(w_c + w_d - w_a - w_b) (across rows), and signs
+// (s, t) = (-,-), (+,-), (-,+), (+,+) for a, b, c, d,
+//   2 pi D.w = 2 pi sigma + s u + t v + s t x,
+// x = (pi/2) D.(w_a + w_d - w_b - w_c) the mixed second difference, which is
+// dropped (bounded by the host against its phase budget; it is of order
+// k |D| (pixel / distance)^2). Then
+//   e^{2 pi i D.w} = e^{2 pi i sigma} (cos u + i s sin u)(cos v + i t sin v)
+//                  = e^{2 pi i sigma} [C_u C_v - s t S_u S_v + i (t C_u S_v + s S_u C_v)],
+// one MUFU sin/cos for four terms; cos/sin of u and v are the pair
+// polynomials (the atom's real amplitude folded into the u factor). The
+// four sums K = sum E e^{2 pi i sigma} C_u C_v, R = ... C_u S_v,
+// S = ... S_u C_v, Q = ... S_u S_v give every pixel of the quad:
+//   A(s, t) = K - s t Q + i t R + i s S.
+// acc[j][0..7] = K, R, S, Q (re, im) of quad j, f32x2 over atoms 2q, 2q+1.
+template <int NQ, bool FR, bool CPLX, bool SHORT>
+__device__ __forceinline__ void mk_tile_terms_quad(
+    const float4 *__restrict__ P, const float4 *__restrict__ E, int T, const mk_f2 (&sx)[NQ],
+    const mk_f2 (&sy)[NQ], const mk_f2 (&sz)[NQ], const mk_f2 (&ux)[NQ], const mk_f2 (&uy)[NQ],
+    const mk_f2 (&uz)[NQ], const mk_f2 (&vx)[NQ], const mk_f2 (&vy)[NQ], const mk_f2 (&vz)[NQ],
+    const mk_f2 (&hq)[NQ], mk_f2 bx, mk_f2 by, mk_f2 bz, mk_f2 (&acc)[NQ][8])
+{
+    const mk_f2 magic = f2_splat(MK_ROUND_MAGIC), two_pi = f2_splat(TWO_PI_F);
+    const mk_f2 one = f2_splat(1.f), m_one = f2_splat(-1.f);
+    const mk_f2 k2 = f2_splat(-0.5f), k3 = f2_splat(-1.f / 6.f);
+    const mk_f2 k4 = f2_splat(1.f / 24.f), k5 = f2_splat(1.f / 120.f), k6 = f2_splat(-1.f / 720.f);
+    const ulonglong2 *P2 = reinterpret_cast<const ulonglong2 *>(P);
+    const ulonglong2 *E2 = reinterpret_cast<const ulonglong2 *>(E);
+#pragma unroll (kPairUnroll)
+    for (int q = 0; q < T / 2; ++q) {
+        const ulonglong2 A = P2[2 * q], B = P2[2 * q + 1], M = E2[q];
+        const mk_f2 X = A.x, Y = A.y, Z = B.x, W = B.y, ER = M.x, EI = M.y;
+        mk_f2 db = 0ull;
+        if (FR) db = f2_fma(Z, bz, f2_fma(Y, by, f2_mul(X, bx)));
+        const mk_f2 e0 = CPLX ? one : ER;
+        const mk_f2 c2 = f2_mul(e0, k2), s2 = f2_mul(e0, k3);
+        mk_f2 c4 = 0ull, s4 = 0ull, c6 = 0ull;
+        if (!SHORT) {
+            c4 = f2_mul(e0, k4);
+            s4 = f2_mul(e0, k5);
+            c6 = f2_mul(e0, k6);
+        }
+        mk_f2 EIn = 0ull;
+        if (CPLX) EIn = f2_mul(EI, m_one);
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) {
+            mk_f2 sig = f2_fma(Z, sz[j], f2_fma(Y, sy[j], f2_mul(X, sx[j])));
+            if (FR) {
+                const mk_f2 sp = f2_sub(db, sig);
+                sig = f2_fma(f2_fma(f2_mul(sp, m_one), sp, W), hq[j], sig);
+            }
+            const mk_f2 du = f2_fma(Z, uz[j], f2_fma(Y, uy[j], f2_mul(X, ux[j])));
+            const mk_f2 dv = f2_fma(Z, vz[j], f2_fma(Y, vy[j], f2_mul(X, vx[j])));
+            const mk_f2 rr = f2_mul(f2_sub(sig, f2_sub(f2_add(sig, magic), magic)), two_pi);
+            const float2 r = f2_unpack(rr);
+            float s0, c0, s1, c1;
+            __sincosf(r.x, &s0, &c0);
+            __sincosf(r.y, &s1, &c1);
+            mk_f2 ec = f2_pack(c0, c1), es = f2_pack(s0, s1);
+            if (CPLX) {
+                const mk_f2 c = ec;
+                ec = f2_fma(ER, c, f2_mul(EIn, es));
+                es = f2_fma(ER, es, f2_mul(EI, c));
+            }
+            const mk_f2 u2 = f2_mul(du, du), v2 = f2_mul(dv, dv);
+            mk_f2 cu, su, cv, sv;
+            if (SHORT) {
+                cu = f2_fma(u2, c2, e0);
+                su = f2_mul(du, f2_fma(u2, s2, e0));
+                cv = f2_fma(v2, k2, one);
+                sv = f2_mul(dv, f2_fma(v2, k3, one));
+            } else {
+                cu = f2_fma(u2, f2_fma(u2, f2_fma(u2, c6, c4), c2), e0);
+                su = f2_mul(du, f2_fma(u2, f2_fma(u2, s4, s2), e0));
+                cv = f2_fma(v2, f2_fma(v2, f2_fma(v2, k6, k4), k2), one);
+                sv = f2_mul(dv, f2_fma(v2, f2_fma(v2, k5, k3), one));
+            }
+            const mk_f2 xc = f2_mul(ec, cu), yc = f2_mul(es, cu);
+            const mk_f2 xs = f2_mul(ec, su), ys = f2_mul(es, su);
+            acc[j][0] = f2_fma(xc, cv, acc[j][0]);
+            acc[j][1] = f2_fma(yc, cv, acc[j][1]);
+            acc[j][2] = f2_fma(xc, sv, acc[j][2]);
+            acc[j][3] = f2_fma(yc, sv, acc[j][3]);
+            acc[j][4] = f2_fma(xs, cv, acc[j][4]);
+            acc[j][5] = f2_fma(ys, cv, acc[j][5]);
+            acc[j][6] = f2_fma(xs, sv, acc[j][6]);
+            acc[j][7] = f2_fma(ys, sv, acc[j][7]);
+        }
+    }
+}
+
+// PM (pixel mode): 0 one sin/cos a term, 1 pixel pairs, 2 pixel quads.
+template <int NT, int PIX, bool FRESNEL, bool CPLX, int PM, bool ANA>
 __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ MkSplitArgs A)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -422,11 +516,31 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
         float accr[PIX], acci[PIX], cmpr[PIX], cmpi[PIX];
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
-            // PAIR: pixels 2j, 2j+1 of the thread are detector neighbours
+            // pairs: pixels 2j, 2j+1 of the thread are detector neighbours
             // (consecutive indices; the host only pairs within rows)
-            pix[p] = PAIR ? pb * (NT * PIX) + 2 * ((p >> 1) * NT + tid) + (p & 1)
-                          : pb * (NT * PIX) + p * NT + tid;
+            pix[p] = PM == 1 ? pb * (NT * PIX) + 2 * ((p >> 1) * NT + tid) + (p & 1)
+                             : pb * (NT * PIX) + p * NT + tid;
             accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
+        }
+        if constexpr (PM == 2) {
+            // quad j of the thread: pixels 4j..4j+3 = a, b (row 2 qz) and c, d
+            // (row 2 qz + 1) at columns 2 qy, 2 qy + 1; out-of-range quads get
+            // n_pix (loads clamp, stores skip)
+            const int half = F.row >> 1, n_quads = F.n_pix >> 2;
+#pragma unroll
+            for (int j = 0; j < PIX / 4; ++j) {
+                const int qi = pb * (NT * (PIX / 4)) + j * NT + tid;
+                if (qi < n_quads) {
+                    const int qz = qi / half, qy = qi - qz * half;
+                    const int base = 2 * qz * F.row + 2 * qy;
+                    pix[4 * j] = base;
+                    pix[4 * j + 1] = base + 1;
+                    pix[4 * j + 2] = base + F.row;
+                    pix[4 * j + 3] = base + F.row + 1;
+                } else {
+                    pix[4 * j] = pix[4 * j + 1] = pix[4 * j + 2] = pix[4 * j + 3] = F.n_pix;
+                }
+            }
         }
 
         for (int t = t_lo; t < t_hi; ++t, ++it) {
@@ -530,7 +644,66 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
             // The |d|^2 term only for tiles wide enough to need it (uniform
             // across the block: no divergence).
             const bool fr_tile = FRESNEL && (float)o.w > A.fres_r;
-            if constexpr (PAIR) {
+            if constexpr (PM == 2) {
+                constexpr int NQ = PIX / 4;
+                mk_f2 sx[NQ], sy[NQ], sz[NQ], ux[NQ], uy[NQ], uz[NQ], vx[NQ], vy[NQ], vz[NQ],
+                    hp[NQ];
+                mk_f2 acc[NQ][8];
+#pragma unroll
+                for (int j = 0; j < NQ; ++j) {
+                    const int a = 4 * j, b = a + 1, c = a + 2, d = a + 3;
+                    const float hpi = 1.57079632679490f;
+                    sx[j] = f2_splat(0.25f * ((wx[a] + wx[b]) + (wx[c] + wx[d])));
+                    sy[j] = f2_splat(0.25f * ((wy[a] + wy[b]) + (wy[c] + wy[d])));
+                    sz[j] = f2_splat(0.25f * ((wz[a] + wz[b]) + (wz[c] + wz[d])));
+                    ux[j] = f2_splat(hpi * ((wx[b] - wx[a]) + (wx[d] - wx[c])));
+                    uy[j] = f2_splat(hpi * ((wy[b] - wy[a]) + (wy[d] - wy[c])));
+                    uz[j] = f2_splat(hpi * ((wz[b] - wz[a]) + (wz[d] - wz[c])));
+                    vx[j] = f2_splat(hpi * ((wx[c] - wx[a]) + (wx[d] - wx[b])));
+                    vy[j] = f2_splat(hpi * ((wy[c] - wy[a]) + (wy[d] - wy[b])));
+                    vz[j] = f2_splat(hpi * ((wz[c] - wz[a]) + (wz[d] - wz[b])));
+                    hp[j] = f2_splat(0.25f * ((hq[a] + hq[b]) + (hq[c] + hq[d])));
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) acc[j][m] = 0ull;
+                }
+                const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
+                const bool short_tile = (float)o.w <= A.pair_short_r;
+                if (fr_tile) {
+                    if (short_tile)
+                        mk_tile_terms_quad<NQ, true, CPLX, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx,
+                                                                 vy, vz, hp, bx, by, bz, acc);
+                    else
+                        mk_tile_terms_quad<NQ, true, CPLX, false>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                                  vx, vy, vz, hp, bx, by, bz, acc);
+                } else {
+                    if (short_tile)
+                        mk_tile_terms_quad<NQ, false, CPLX, true>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                                  vx, vy, vz, hp, bx, by, bz, acc);
+                    else
+                        mk_tile_terms_quad<NQ, false, CPLX, false>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                                   vx, vy, vz, hp, bx, by, bz, acc);
+                }
+#pragma unroll
+                for (int j = 0; j < NQ; ++j) {
+                    float h[8];
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) {
+                        const float2 t2 = f2_unpack(acc[j][m]);   // halves: even, odd atoms
+                        h[m] = t2.x + t2.y;
+                    }
+                    const float Kr = h[0], Ki = h[1], Rr = h[2], Ri = h[3];
+                    const float Sr = h[4], Si = h[5], Qr = h[6], Qi = h[7];
+                    // A(s, t) = K - s t Q + i t R + i s S
+                    csr[4 * j] = (Kr - Qr) + (Ri + Si);       // a (-, -)
+                    csi[4 * j] = (Ki - Qi) - (Rr + Sr);
+                    csr[4 * j + 1] = (Kr + Qr) + (Ri - Si);   // b (+, -)
+                    csi[4 * j + 1] = (Ki + Qi) - (Rr - Sr);
+                    csr[4 * j + 2] = (Kr + Qr) - (Ri - Si);   // c (-, +)
+                    csi[4 * j + 2] = (Ki + Qi) + (Rr - Sr);
+                    csr[4 * j + 3] = (Kr - Qr) - (Ri + Si);   // d (+, +)
+                    csi[4 * j + 3] = (Ki - Qi) + (Rr + Sr);
+                }
+            } else if constexpr (PM == 1) {
                 constexpr int NP = PIX / 2;
                 mk_f2 sx[NP], sy[NP], sz[NP], dx[NP], dy[NP], dz[NP], hp[NP];
                 mk_f2 pr[NP], pi_[NP], sr[NP], si[NP];
@@ -645,14 +818,14 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
 // ----------------------------------------------------------------- pickers
 typedef void (*mk_split_fn)(const MkSplitArgs);
 
-template <int NT, int PIX, bool PAIR, bool ANA>
+template <int NT, int PIX, int PM, bool ANA>
 static mk_split_fn mk_pick4(bool fresnel, bool cplx)
 {
     if (fresnel)
-        return cplx ? mk_split_kernel<NT, PIX, true, true, PAIR, ANA>
-                    : mk_split_kernel<NT, PIX, true, false, PAIR, ANA>;
-    return cplx ? mk_split_kernel<NT, PIX, false, true, PAIR, ANA>
-                : mk_split_kernel<NT, PIX, false, false, PAIR, ANA>;
+        return cplx ? mk_split_kernel<NT, PIX, true, true, PM, ANA>
+                    : mk_split_kernel<NT, PIX, true, false, PM, ANA>;
+    return cplx ? mk_split_kernel<NT, PIX, false, true, PM, ANA>
+                : mk_split_kernel<NT, PIX, false, false, PM, ANA>;
 }
 
 // Pairs need an even PIX; the analyser kernels (no pairs) exist for
@@ -662,15 +835,15 @@ static mk_split_fn mk_pick3(bool fresnel, bool cplx, bool pair, bool ana)
 {
     if (ana) {
         if constexpr ((NT == 128 || NT == 256) && (PIX == 2 || PIX == 4))
-            return pair ? nullptr : mk_pick4<NT, PIX, false, true>(fresnel, cplx);
+            return pair ? nullptr : mk_pick4<NT, PIX, 0, true>(fresnel, cplx);
         return nullptr;
     }
     if constexpr (PIX % 2 == 0) {
-        if (pair) return mk_pick4<NT, PIX, true, false>(fresnel, cplx);
+        if (pair) return mk_pick4<NT, PIX, 1, false>(fresnel, cplx);
     } else {
         if (pair) return nullptr;
     }
-    return mk_pick4<NT, PIX, false, false>(fresnel, cplx);
+    return mk_pick4<NT, PIX, 0, false>(fresnel, cplx);
 }
 
 // Kernel instance for a launch shape of one block size (nullptr when no
@@ -678,6 +851,9 @@ static mk_split_fn mk_pick3(bool fresnel, bool cplx, bool pair, bool ana)
 mk_split_fn mk_pick_nt64(int pix, bool fresnel, bool cplx, bool pair, bool ana);
 mk_split_fn mk_pick_nt128(int pix, bool fresnel, bool cplx, bool pair, bool ana);
 mk_split_fn mk_pick_nt256(int pix, bool fresnel, bool cplx, bool pair, bool ana);
+// Pixel-quad instances (64/128/256 threads, 4 or 8 pixels a thread, no
+// analyser); defined in mk_split_quad.cu.
+mk_split_fn mk_pick_quad(int nt, int pix, bool fresnel, bool cplx);
 
 #define MK_PIX_CASES(NT_)                                                  \
     switch (pix) {                                                         \

@@ -163,8 +163,9 @@ int mk_launch_reduce(const double2 *partial, int slices, int n_pix, const double
 }
 
 // ----------------------------------------------------------------- launch
-static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, bool pair, bool ana)
+static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, int pair, bool ana)
 {
+    if (pair == 2) return ana ? nullptr : mk_pick_quad(nt, pix, fresnel, cplx);
     switch (nt) {
     case 64: return mk_pick_nt64(pix, fresnel, cplx, pair, ana);
     case 128: return mk_pick_nt128(pix, fresnel, cplx, pair, ana);
@@ -184,10 +185,11 @@ static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShap
                            bool ana = false)
 {
     mk_split_fn fn = mk_pick(launch->threads, launch->pix_per_thread, launch->fresnel != 0,
-                             launch->amp_real == 0, launch->pairs != 0, ana);
+                             launch->amp_real == 0, launch->pairs, ana);
     MK_REQUIRE(fn, "split kernel: unsupported launch shape threads=%d pix=%d pairs=%d%s",
                launch->threads, launch->pix_per_thread, launch->pairs,
-               ana ? " with the analyser (128/256 threads, 2/4 pixels, no pairs)" : "");
+               ana ? " with the analyser (128/256 threads, 2/4 pixels, no pairs)"
+                   : (launch->pairs == 2 ? " (quads: 4 or 8 pixels a thread)" : ""));
     const size_t smem = mk_split_smem(tile_atoms);
     MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
@@ -213,15 +215,25 @@ static int mk_frame_slices(int pix_blocks, int n_tiles, int resident, long long 
     return (int)std::min<long long>(s, n_tiles);
 }
 
-extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const double *beam_dirs,
-                            const double *pol_es, const mk_tiles *tiles, const mk_launch *launch,
-                            mk_frame_desc *frames_out, long long *n_items_out,
-                            long long *n_partial_out)
+extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const int *frame_rows,
+                            const double *beam_dirs, const double *pol_es, const mk_tiles *tiles,
+                            const mk_launch *launch, mk_frame_desc *frames_out,
+                            long long *n_items_out, long long *n_partial_out)
 {
     MK_REQUIRE(n_frames >= 1 && frame_pixels && beam_dirs && tiles && launch && frames_out &&
                    n_items_out && n_partial_out,
                "mk_scan_plan: null argument or no frames");
     MK_REQUIRE(tiles->n_tiles >= 1, "mk_scan_plan: no tiles");
+    MK_REQUIRE(launch->pairs >= 0 && launch->pairs <= 2, "mk_scan_plan: pairs must be 0, 1 or 2");
+    if (launch->pairs == 2) {
+        MK_REQUIRE(frame_rows, "mk_scan_plan: pixel quads need the row length of every frame");
+        for (int f = 0; f < n_frames; ++f)
+            MK_REQUIRE(frame_rows[f] >= 2 && frame_rows[f] % 2 == 0 &&
+                           frame_pixels[f] % (2 * frame_rows[f]) == 0,
+                       "mk_scan_plan: pixel quads need an even row length and an even number "
+                       "of rows (frame %d: %d pixels, rows of %d)",
+                       f, frame_pixels[f], frame_rows[f]);
+    }
     MkLaunchShape sh;
     int rc = mk_launch_shape(tiles->tile_atoms, launch, &sh);
     if (rc != MK_OK) return rc;
@@ -236,6 +248,7 @@ extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const double 
         mk_frame_desc &F = frames_out[f];
         memset(&F, 0, sizeof(F));
         F.n_pix = frame_pixels[f];
+        F.row = frame_rows ? frame_rows[f] : 0;
         F.pix_blocks = (F.n_pix + ppb - 1) / ppb;
         int s = launch->slices > 0 ? std::min(launch->slices, tiles->n_tiles)
                                    : mk_frame_slices(F.pix_blocks, tiles->n_tiles, sh.resident, total_blocks);
@@ -349,7 +362,8 @@ static int mk_single_plan(const mk_tiles *tiles, const mk_physics *phys, const m
                           long long *n_partial)
 {
     const int n_pix = px->ny * px->nz;
-    return mk_scan_plan(1, &n_pix, phys->beam_dir, phys->pol_e, tiles, launch, F, n_items, n_partial);
+    return mk_scan_plan(1, &n_pix, &px->ny, phys->beam_dir, phys->pol_e, tiles, launch, F, n_items,
+                        n_partial);
 }
 
 extern "C" int mk_split_plan(const mk_tiles *tiles, const mk_pixels *px, const mk_launch *launch,

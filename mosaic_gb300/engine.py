@@ -144,11 +144,13 @@ class Pixels:
                             self.q.data_ptr(), self.u.data_ptr(), self.phasor.data_ptr())
         sh = _stream_handle(stream)
         self.spans = [(0, P)]
+        self.shapes = [(self.ny, self.nz)]
         if frames is None:
             check(L.mk_pixels_prepare(ctypes.byref(self.abi), ctypes.byref(phys), sh))
             return
         off = 0
         self.spans = []
+        self.shapes = [(int(fny), int(fnz)) for fny, fnz, _ in frames]
         for fny, fnz, bdir in frames:
             m = int(fny) * int(fnz)
             sub = MkPixels(int(fny), int(fnz), self.xyz[off:].data_ptr(), self.r0[off:].data_ptr(),
@@ -180,6 +182,33 @@ class Pixels:
                 d = u[off:off + 2 * h:2] - u[off + 1:off + 2 * h:2]
                 worst = max(worst, float(torch.linalg.vector_norm(d, dim=1).max()))
         return worst
+
+    def row_lengths(self):
+        """Pixels per detector row of every frame (the kernel's quad layout)."""
+        return [ny for ny, _ in self.shapes]
+
+    def quad_steps(self):
+        """Differences of the FP64 unit vectors u to the pixels over the 2x2
+        quads (a b / c d: a, b neighbours in a row, c, d below them) of every
+        frame, or None when a frame has an odd row length or an odd number of
+        rows (no quad layout). Returns the largest norms of the row
+        difference (b - a) + (d - c), the cross-row difference
+        (c - a) + (d - b), the mixed difference (a - b) + (d - c) and the
+        diagonals d - a, c - b."""
+        if any(ny % 2 or nz % 2 for ny, nz in self.shapes):
+            return None
+        x = self.xyz
+        u = x / torch.linalg.vector_norm(x, dim=1, keepdim=True)
+        out = dict(row=0.0, col=0.0, mixed=0.0, diag=0.0)
+        for (off, m), (ny, nz) in zip(self.spans, self.shapes):
+            U = u[off:off + m].reshape(nz, ny, 3)
+            a, b, c, d = U[0::2, 0::2], U[0::2, 1::2], U[1::2, 0::2], U[1::2, 1::2]
+            nrm = lambda t: float(torch.linalg.vector_norm(t, dim=-1).max())
+            out["row"] = max(out["row"], nrm((b - a) + (d - c)))
+            out["col"] = max(out["col"], nrm((c - a) + (d - b)))
+            out["mixed"] = max(out["mixed"], nrm((a - b) + (d - c)))
+            out["diag"] = max(out["diag"], nrm(d - a), nrm(c - b))
+        return out
 
 
 @dataclass
@@ -380,6 +409,74 @@ def pairs_allowed(tiles, pix: Pixels, k):
     return pair_delta(tiles, pix, k) <= PAIR_DELTA_MAX
 
 
+def quad_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
+    """Error bounds of the 2x2 pixel-quad form over all tiles, or None when
+    a frame has no quad layout (odd sides).
+
+    ``delta`` [rad] bounds the two half differences u, v that go to the
+    polynomials (as ``pair_delta`` does for pairs); ``short_radius_m`` is the
+    largest tile radius whose u, v stay within PAIR_SHORT_DELTA; ``cross``
+    [rad] bounds the phase the quad form drops: the mixed second difference
+    (pi/2) D.(w_a + w_d - w_b - w_c), of order k |D| (pixel/distance)^2,
+    widened for the tile-origin term of w, plus the change of the |d|^2 term
+    across the quad, which the quad shares (2 ``fresnel_rad`` x the quad's
+    diagonal step)."""
+    st = pix.quad_steps()
+    if st is None:
+        return None
+    if not tiles.n_tiles:
+        return dict(delta=0.0, short_radius_m=1.0, cross=0.0, **st)
+    r0 = max(pix.r0_min(), 1e-300)
+    o_ratio = tiles.max_origin_norm() / r0
+    grow = 1.0 + 2.0 * o_ratio
+    rate = 0.25 * float(k) * max(st["row"], st["col"]) * grow * 1.05
+    r = tiles.max_radius()
+    step = 0.5 * max(st["row"], st["col"])
+    mixed = st["mixed"] * grow + 4.0 * o_ratio * step * step
+    cross = 0.25 * float(k) * r * mixed * 1.05 + 2.0 * float(fresnel_rad) * st["diag"]
+    return dict(delta=rate * r, short_radius_m=(PAIR_SHORT_DELTA / rate if rate > 0 else 1.0),
+                cross=cross, **st)
+
+
+def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=False):
+    """Widest legal sharing of one sin/cos between neighbouring pixels:
+    (level, info) with level 2 quads, 1 pairs, 0 none. Pairs need
+    ``pair_delta`` <= PAIR_DELTA_MAX; quads also need their half differences
+    within it and their dropped phase within ``budget_rad``; the analyser
+    kernels have neither."""
+    info = dict(pair_delta_rad=pair_delta(tiles, pix, k))
+    if analyser or info["pair_delta_rad"] > PAIR_DELTA_MAX:
+        return 0, info
+    q = quad_bounds(tiles, pix, k, fresnel_rad)
+    if q is not None:
+        info.update(quad_delta_rad=q["delta"], quad_cross_rad=q["cross"],
+                    quad_short_radius_m=q["short_radius_m"])
+        if q["delta"] <= PAIR_DELTA_MAX and q["cross"] <= budget_rad:
+            return 2, info
+    return 1, info
+
+
+def grouping_launch(cfg, level, tiles, pix, k, info):
+    """Clamp a launch dict's ``pairs`` to the legal ``level`` and the pixels
+    per thread the kernels have (quads: 4 or 8; pairs: even), and set the
+    short-polynomial radius for the mode kept."""
+    cfg = dict(cfg)
+    mode = min(int(cfg.get("pairs", 0) or 0), int(level))
+    ppt = int(cfg.get("pix_per_thread", 4))
+    if mode == 2 and ppt not in (4, 8):
+        mode = 1
+    if mode == 1 and ppt % 2:
+        mode = 0
+    cfg["pairs"] = mode
+    if mode == 2:
+        cfg["pair_short_radius_m"] = info["quad_short_radius_m"]
+    elif mode == 1:
+        cfg["pair_short_radius_m"] = pair_short_radius(tiles, pix, k)
+    else:
+        cfg["pair_short_radius_m"] = 0.0
+    return cfg
+
+
 def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None, fresnel=-1,
               amp_real=None, out=None, accumulate=False, stream=None, fresnel_radius=0.0):
     """FP32 split-phase sum; returns float64 (P, 2) (a view of `out` if given).
@@ -390,12 +487,13 @@ def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None,
     the short delta polynomial for the tiles up to that radius."""
     L = _require_cuda()
     cfg = dict(DEFAULT_LAUNCH, **(launch or {}))
-    pairs = bool(cfg.get("pairs", 0))
+    pairs = int(cfg.get("pairs", 0) or 0)
     short_r = 0.0
     if pairs:
         short_r = cfg.get("pair_short_radius_m")
         if short_r is None:
-            short_r = pair_short_radius(tiles, pix, phys.k)
+            short_r = (quad_bounds(tiles, pix, phys.k)["short_radius_m"] if pairs == 2
+                       else pair_short_radius(tiles, pix, phys.k))
     ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
                   int(tiles.amp_is_real() if amp_real is None else bool(amp_real)),
                   float(fresnel_radius), int(pairs), short_r)

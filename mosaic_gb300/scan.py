@@ -114,25 +114,26 @@ class BatchedScan:
                                     f"scan geometry outside the split-phase error budget "
                                     f"({third:.2e} rad > {tol:.0e})")
         self.diag = diag
-        delta = engine.pair_delta(self.tiles, self.pix, beam.k)
-        self.diag["pair_delta_rad"] = delta
-        pairs_ok = delta <= engine.PAIR_DELTA_MAX
-        cfg = dict(engine.DEFAULT_LAUNCH, pairs=int(pairs_ok))
+        # one sin/cos per pixel pair or 2x2 quad where every frame allows it
+        level, ginfo = engine.pixel_grouping(self.tiles, self.pix, beam.k, tol - third,
+                                             fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0)
+        self.diag.update(ginfo)
+        cfg = dict(engine.DEFAULT_LAUNCH, pairs=level)
         cfg.update(launch or beam._kernel_launch or {})
-        if not pairs_ok:
-            cfg["pairs"] = 0
-        short_r = engine.pair_short_radius(self.tiles, self.pix, beam.k) if cfg["pairs"] else 0.0
-        cfg["pair_short_radius_m"] = short_r
+        cfg = engine.grouping_launch(cfg, level, self.tiles, self.pix, beam.k, ginfo)
+        short_r = cfg["pair_short_radius_m"]
         self.cfg = cfg
         self.launch = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]),
                                int(fresnel), int(self.tiles.amp_is_real()),
-                               float(diag["fresnel_radius_m"]), int(bool(cfg["pairs"])), short_r)
+                               float(diag["fresnel_radius_m"]), int(cfg["pairs"]), short_r)
         nf = len(self.frames)
         desc = (MkFrameDesc * nf)()
         n_items, n_part = ctypes.c_longlong(0), ctypes.c_longlong(0)
         bd = np.ascontiguousarray(np.array(bdirs, dtype=np.float64))
         pe = np.ascontiguousarray(np.array(pols, dtype=np.float64))
-        check(self.L.mk_scan_plan(nf, self.frame_pixels.ctypes.data, bd.ctypes.data, pe.ctypes.data,
+        self.frame_rows = np.array([int(s[0]) for s in fr], dtype=np.int32)
+        check(self.L.mk_scan_plan(nf, self.frame_pixels.ctypes.data, self.frame_rows.ctypes.data,
+                                  bd.ctypes.data, pe.ctypes.data,
                                   ctypes.byref(self.tiles.abi), ctypes.byref(self.launch),
                                   ctypes.cast(desc, ctypes.c_void_p), ctypes.byref(n_items),
                                   ctypes.byref(n_part)))

@@ -1,0 +1,100 @@
+"""Host logic of the pixel-sharing forms (no GPU): the quad differences of a
+flat detector, the bounds that admit pairs and quads, and the clamping of a
+launch shape to what the geometry and the kernels allow."""
+import types
+
+import numpy as np
+import pytest
+import torch
+
+from mosaic_gb300 import engine
+
+
+def _flat_pixels(ny, nz, pitch, dist, y0=0.0, z0=0.0, frames=None):
+    """Stub with the attributes Pixels' bound methods read: a flat detector
+    at x = dist, row index z, column index y (index iz * ny + iy)."""
+    shapes = frames or [(ny, nz)]
+    xyz, spans, off = [], [], 0
+    for fny, fnz in shapes:
+        y = y0 + pitch * (np.arange(fny) - 0.5 * (fny - 1))
+        z = z0 + pitch * (np.arange(fnz) - 0.5 * (fnz - 1))
+        Z, Y = np.meshgrid(z, y, indexing="ij")
+        xyz.append(np.stack([np.full(Y.size, dist), Y.ravel(), Z.ravel()], 1))
+        spans.append((off, fny * fnz))
+        off += fny * fnz
+    st = types.SimpleNamespace(xyz=torch.tensor(np.concatenate(xyz)), spans=spans, shapes=shapes)
+    st.n = off
+    st.quad_steps = lambda: engine.Pixels.quad_steps(st)
+    u = st.xyz / torch.linalg.vector_norm(st.xyz, dim=1, keepdim=True)
+    st.u = torch.cat([u.float(), torch.zeros(off, 1)], 1)
+    st.pair_step = lambda: engine.Pixels.pair_step(st)
+    st.r0_min = lambda: float(torch.linalg.vector_norm(st.xyz, dim=1).min())
+    return st
+
+
+def _tiles(radius, origin=0.0):
+    return types.SimpleNamespace(n_tiles=4, max_radius=lambda: radius,
+                                 max_origin_norm=lambda: origin)
+
+
+def test_quad_steps_of_a_flat_detector():
+    p, R = 55e-6, 1.0
+    pix = _flat_pixels(16, 12, p, R)
+    st = pix.quad_steps()
+    # row and cross-row differences: two pixel steps; mixed: second order
+    assert st["row"] == pytest.approx(2 * p / R, rel=1e-3)
+    assert st["col"] == pytest.approx(2 * p / R, rel=1e-3)
+    assert st["diag"] == pytest.approx(np.sqrt(2) * p / R, rel=1e-3)
+    assert st["mixed"] < 3 * (p / R) ** 2 * (16 * p / R)
+    # off-centre the mixed difference grows like y z / R^2 (p/R)^2
+    far = _flat_pixels(16, 12, p, R, y0=0.05, z0=0.04).quad_steps()
+    assert st["mixed"] < far["mixed"] < 10 * (p / R) ** 2
+    assert _flat_pixels(15, 12, p, R).quad_steps() is None
+    assert _flat_pixels(16, 11, p, R).quad_steps() is None
+    multi = _flat_pixels(0, 0, p, R, frames=[(8, 4), (16, 16), (6, 2)])
+    assert multi.quad_steps() is not None
+    assert _flat_pixels(0, 0, p, R, frames=[(8, 4), (7, 2)]).quad_steps() is None
+
+
+def test_grouping_levels():
+    k = 2 * np.pi / 1.2398e-10
+    pix = _flat_pixels(16, 16, 55e-6, 1.0)
+    tiles = _tiles(4.6e-8, 6e-8)
+    level, info = engine.pixel_grouping(tiles, pix, k, 1e-6)
+    assert level == 2
+    assert info["quad_cross_rad"] < 1e-6
+    # the quad half differences match the pair half difference
+    assert info["quad_delta_rad"] == pytest.approx(info["pair_delta_rad"], rel=2e-2)
+    # no budget left: pairs only; an odd number of rows: pairs only; odd
+    # rows: a pair spans the row end, so not even pairs; analyser: none
+    assert engine.pixel_grouping(tiles, pix, k, 1e-12)[0] == 1
+    assert engine.pixel_grouping(tiles, _flat_pixels(16, 15, 55e-6, 1.0), k, 1e-6)[0] == 1
+    assert engine.pixel_grouping(tiles, _flat_pixels(15, 16, 55e-6, 1.0), k, 1e-6)[0] == 0
+    assert engine.pixel_grouping(tiles, pix, k, 1e-6, analyser=True)[0] == 0
+    # pitch so coarse that the half difference passes 0.5 rad: none
+    assert engine.pixel_grouping(tiles, _flat_pixels(16, 16, 2e-2, 1.0), k, 1e-6)[0] == 0
+    # the |d|^2 term's change across the quad counts against the budget
+    c0 = engine.quad_bounds(tiles, pix, k)["cross"]
+    c1 = engine.quad_bounds(tiles, pix, k, fresnel_rad=1e-3)["cross"]
+    assert c1 == pytest.approx(c0 + 2e-3 * pix.quad_steps()["diag"], rel=1e-9)
+
+
+def test_grouping_launch_clamps_the_mode():
+    k = 2 * np.pi / 1.2398e-10
+    pix = _flat_pixels(16, 16, 55e-6, 1.0)
+    tiles = _tiles(4.6e-8, 6e-8)
+    level, info = engine.pixel_grouping(tiles, pix, k, 1e-6)
+    cfg = engine.grouping_launch(dict(pix_per_thread=4, threads=128, pairs=2), level, tiles, pix, k,
+                                 info)
+    assert cfg["pairs"] == 2 and cfg["pair_short_radius_m"] == info["quad_short_radius_m"]
+    cfg = engine.grouping_launch(dict(pix_per_thread=2, threads=128, pairs=2), level, tiles, pix, k,
+                                 info)
+    assert cfg["pairs"] == 1
+    assert cfg["pair_short_radius_m"] == engine.pair_short_radius(tiles, pix, k)
+    cfg = engine.grouping_launch(dict(pix_per_thread=1, threads=256, pairs=2), level, tiles, pix, k,
+                                 info)
+    assert cfg["pairs"] == 0 and cfg["pair_short_radius_m"] == 0.0
+    cfg = engine.grouping_launch(dict(pix_per_thread=8, threads=64, pairs=2), 1, tiles, pix, k, info)
+    assert cfg["pairs"] == 1
+    cfg = engine.grouping_launch(dict(pix_per_thread=4, threads=128, pairs=1), 0, tiles, pix, k, info)
+    assert cfg["pairs"] == 0
