@@ -151,6 +151,10 @@ typedef struct {
     double pair_short_radius_m; /* with pairs or quads: tiles up to this radius keep the half
                              differences below 0.07 rad and use the short polynomials
                              (0: none does) */
+    double sin_direct_max_rad; /* with quads: tiles without the |d|^2 term whose in-tile phase
+                             bound stays below this [rad] pass the phase to the MUFU sin/cos
+                             without the mod-1 reduction (its error grows ~1e-7 |x|);
+                             0: the library default, 100 rad; < 0: never */
 } mk_launch;
 
 /* --- library ---------------------------------------------------------- */

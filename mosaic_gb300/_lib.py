@@ -145,7 +145,7 @@ class MkLaunch(ctypes.Structure):
     _fields_ = [("pix_per_thread", ctypes.c_int), ("threads", ctypes.c_int),
                 ("slices", ctypes.c_int), ("fresnel", ctypes.c_int), ("amp_real", ctypes.c_int),
                 ("fresnel_radius_m", ctypes.c_double), ("pairs", ctypes.c_int),
-                ("pair_short_radius_m", ctypes.c_double)]
+                ("pair_short_radius_m", ctypes.c_double), ("sin_direct_max_rad", ctypes.c_double)]
 
 
 # name -> (restype, argtypes)

@@ -39,7 +39,7 @@ def _cache_path():
 
 def _src_hash():
     h = hashlib.sha1()
-    for name in ("mk_split.cuh", "mk_sum_f32.cu", "mk_split_quad.cu"):
+    for name in ("mk_split.cuh", "mk_sum_f32.cu", "mk_split_quad.cu", "mk_split_quad8.cu"):
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", name), "rb") as fh:
             h.update(fh.read())
     return h.hexdigest()[:12]

@@ -57,6 +57,7 @@ struct MkSplitArgs {
     float pdeg;
     float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
     float pair_short_r; // pair/quad kernels: tiles up to this radius [m] use the short polynomials
+    float sin_direct;   // quad kernels: in-tile phase bound [rad] below which the reduction is skipped
     // analyser (ANA kernels, single exposures): kind 1 top-hat / 2 Darwin,
     // beam direction and analyser axis in FP64, 4 sin^2(alpha/2), half-width
     int analyser;
@@ -299,6 +300,16 @@ __device__ __forceinline__ mk_f2 f2_splat(float x) { return f2_pack(x, x); }
 // loop is an f32x2 pair over the tile's atoms 2q and 2q+1 (interleaved in
 // shared memory); the two halves of the accumulators are added at the end.
 #define MK_PAIR_SHORT_DELTA 0.07f
+// Default largest in-tile phase [rad] handed to the MUFU sin/cos without the
+// mod-1 reduction (quad kernels; mk_launch.sin_direct_max_rad). __sincosf's absolute error grows about linearly
+// with |x| (its argument scaling by 1/2pi rounds in FP32): measured on sm_103
+// over uniform sweeps, at most 3.5e-7 in [-pi, pi], 1.0e-5 below 32 pi and
+// 1.7e-5 just above. Below 100 rad the added error is of the size of the
+// rounding of the FP32 in-tile phase itself, and like it differs from atom to
+// atom.
+#ifndef MK_SIN_DIRECT_MAX
+#define MK_SIN_DIRECT_MAX 100.0f
+#endif
 #ifndef MK_PAIR_UNROLL
 #define MK_PAIR_UNROLL 32
 #endif
@@ -387,7 +398,10 @@ __device__ __forceinline__ void mk_tile_terms_pair(
 // S = ... S_u C_v, Q = ... S_u S_v give every pixel of the quad:
 //   A(s, t) = K - s t Q + i t R + i s S.
 // acc[j][0..7] = K, R, S, Q (re, im) of quad j, f32x2 over atoms 2q, 2q+1.
-template <int NQ, bool FR, bool CPLX, bool SHORT>
+// RAD (tiles without the |d|^2 term whose in-tile phase stays within
+// MK_SIN_DIRECT_MAX radians): (sx, sy, sz) come scaled by 2 pi, so sigma is
+// in radians and goes to the sin/cos without the mod-1 reduction.
+template <int NQ, bool FR, bool CPLX, bool SHORT, bool RAD = false>
 __device__ __forceinline__ void mk_tile_terms_quad(
     const float4 *__restrict__ P, const float4 *__restrict__ E, int T, const mk_f2 (&sx)[NQ],
     const mk_f2 (&sy)[NQ], const mk_f2 (&sz)[NQ], const mk_f2 (&ux)[NQ], const mk_f2 (&uy)[NQ],
@@ -425,7 +439,7 @@ __device__ __forceinline__ void mk_tile_terms_quad(
             }
             const mk_f2 du = f2_fma(Z, uz[j], f2_fma(Y, uy[j], f2_mul(X, ux[j])));
             const mk_f2 dv = f2_fma(Z, vz[j], f2_fma(Y, vy[j], f2_mul(X, vx[j])));
-            const mk_f2 rr = f2_mul(f2_sub(sig, f2_sub(f2_add(sig, magic), magic)), two_pi);
+            const mk_f2 rr = RAD ? sig : f2_mul(f2_sub(sig, f2_sub(f2_add(sig, magic), magic)), two_pi);
             const float2 r = f2_unpack(rr);
             float s0, c0, s1, c1;
             __sincosf(r.x, &s0, &c0);
@@ -668,7 +682,29 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                 }
                 const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
                 const bool short_tile = (float)o.w <= A.pair_short_r;
-                if (fr_tile) {
+                // direct sin/cos argument: warp-uniform, from the bound
+                // 2 pi |w_mean| kappa r of every quad of the warp
+                bool rad = false;
+                if (!fr_tile && short_tile) {
+                    float wmax = 0.f;
+#pragma unroll
+                    for (int j = 0; j < NQ; ++j) {
+                        const float2 a = f2_unpack(sx[j]), b = f2_unpack(sy[j]), c = f2_unpack(sz[j]);
+                        wmax = fmaxf(wmax, fmaf(c.x, c.x, fmaf(b.x, b.x, a.x * a.x)));
+                    }
+                    const float bound = TWO_PI_F * sqrtf(wmax) * A.kappa * (float)o.w;
+                    rad = __all_sync(0xffffffffu, bound <= A.sin_direct);
+                }
+                if (rad) {
+#pragma unroll
+                    for (int j = 0; j < NQ; ++j) {
+                        sx[j] = f2_mul(sx[j], f2_splat(TWO_PI_F));
+                        sy[j] = f2_mul(sy[j], f2_splat(TWO_PI_F));
+                        sz[j] = f2_mul(sz[j], f2_splat(TWO_PI_F));
+                    }
+                    mk_tile_terms_quad<NQ, false, CPLX, true, true>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                                    vx, vy, vz, hp, bx, by, bz, acc);
+                } else if (fr_tile) {
                     if (short_tile)
                         mk_tile_terms_quad<NQ, true, CPLX, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx,
                                                                  vy, vz, hp, bx, by, bz, acc);
@@ -852,7 +888,7 @@ mk_split_fn mk_pick_nt64(int pix, bool fresnel, bool cplx, bool pair, bool ana);
 mk_split_fn mk_pick_nt128(int pix, bool fresnel, bool cplx, bool pair, bool ana);
 mk_split_fn mk_pick_nt256(int pix, bool fresnel, bool cplx, bool pair, bool ana);
 // Pixel-quad instances (64/128/256 threads, 4 or 8 pixels a thread, no
-// analyser); defined in mk_split_quad.cu.
+// analyser); defined in mk_split_quad.cu and mk_split_quad8.cu.
 mk_split_fn mk_pick_quad(int nt, int pix, bool fresnel, bool cplx);
 
 #define MK_PIX_CASES(NT_)                                                  \

@@ -496,7 +496,8 @@ def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None,
                        else pair_short_radius(tiles, pix, phys.k))
     ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
                   int(tiles.amp_is_real() if amp_real is None else bool(amp_real)),
-                  float(fresnel_radius), int(pairs), short_r)
+                  float(fresnel_radius), int(pairs), short_r,
+                  float(cfg.get("sin_direct_max_rad", 0.0) or 0.0))
     wsb = ctypes.c_size_t(0)
     check(L.mk_split_plan(ctypes.byref(tiles.abi), ctypes.byref(pix.abi), ctypes.byref(ln),
                           ctypes.byref(wsb)))

@@ -125,7 +125,8 @@ class BatchedScan:
         self.cfg = cfg
         self.launch = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]),
                                int(fresnel), int(self.tiles.amp_is_real()),
-                               float(diag["fresnel_radius_m"]), int(cfg["pairs"]), short_r)
+                               float(diag["fresnel_radius_m"]), int(cfg["pairs"]), short_r,
+                               float(cfg.get("sin_direct_max_rad", 0.0) or 0.0))
         nf = len(self.frames)
         desc = (MkFrameDesc * nf)()
         n_items, n_part = ctypes.c_longlong(0), ctypes.c_longlong(0)

@@ -45,6 +45,36 @@ def test_split_quads_match_oracle(cuda, golden, pix_pt, threads):
     assert used >= 6
 
 
+def test_quads_direct_sincos_argument(cuda, golden):
+    """Tiles whose in-tile phase bound stays below the limit hand the phase
+    to the sin/cos without the mod-1 reduction: the limit forced up (every
+    short, |d|^2-free tile), the default (100 rad) and off agree with the
+    oracle and with each other (the skipped reduction adds at most ~1e-7 |x|
+    of phase per term, varying from atom to atom)."""
+    d = golden("kernel_cases.npz")
+    used = 0
+    for i in range(int(d["n"])):
+        c = _kernel_case(d, i)
+        if c["ny"] % 2 or c["nz"] % 2:
+            continue
+        table, idx = table_from_rows(c["wk"], c["f0z"], c["anom"])
+        atoms = atoms_from_arrays(c["pos"], idx, c["amp"], table, cuda)
+        phys = engine.physics(c["k"], (1, 0, 0), c["ap"], c["pol"], c["dc"], c["rf"])
+        pix = engine.Pixels(c["cxyz"], c["ny"], c["nz"], phys, device=cuda)
+        tiles = engine.Tiles(atoms, c["k"], 128, device=cuda)
+        used += 1
+        base = dict(pix_per_thread=4, threads=128, slices=0, pairs=2)
+        run = lambda lim: field(engine.run_split(tiles, pix, phys, table, fresnel=0,
+                                                 launch=dict(base, sin_direct_max_rad=lim)))
+        always, default, never = run(1e4), run(0.0), run(-1.0)
+        ref = _oracle_case(c)
+        for got in (always, default, never):
+            assert rel_intensity(got, ref) <= 1e-4, (i, rel_intensity(got, ref))
+        assert rel_max(always, never) <= 2e-5, (i, rel_max(always, never))
+        assert rel_max(default, never) <= 2e-5, (i, rel_max(default, never))
+    assert used >= 6
+
+
 def _cu_ni_case():
     rng = np.random.default_rng(5)
     w = workloads.fcc_cu_32k(cells=8, npix=20)
