@@ -347,7 +347,10 @@ def run_ours(args):
         level = 0
     elif args.no_quads:
         level = min(level, 1)
-    if args.profile:
+    if args.launch:
+        ppt, nt, mode = (int(v) for v in args.launch.split(","))
+        launch, tune_tbl = dict(pix_per_thread=ppt, threads=nt, slices=0, pairs=mode), []
+    elif args.profile:
         launch, tune_tbl = autotune.lookup(pix.n, tiles, level), []
     else:
         launch, tune_tbl = autotune.tune(tiles, pix, phys, table, fresnel=int(fresnel),
@@ -477,7 +480,7 @@ def run_ours(args):
                          "unit": "Gterm/s", "frac": achieved / peak_terms, "traffic": None,
                          "traffic_profile": {"workload": "nacl_screw_8m_px128 (same 8.19M atoms, 128^2 "
                                              "pixels; tiles exceed L2 as here)",
-                                             "dram_bytes_per_launch": 294395136,
+                                             "dram_bytes_per_launch": 200094464 + 90783488,
                                              "terms_per_launch": 8192000 * 16384,
                                              "note": "ncu dram__bytes_read+write of one launch; reads "
                                                      "~ the tile data once (concurrent items share "
@@ -528,6 +531,10 @@ def main():
                     help="unjudged predicted frames checked against the exact sum (untimed)")
     ap.add_argument("--no-pairs", action="store_true",
                     help="one sin/cos per term (the pixel-pair and quad forms off)")
+    ap.add_argument("--launch", default="",
+                    help="fixed launch shape 'pixels_per_thread,threads,mode' (mode 0 one sin/cos "
+                         "per term, 1 pairs, 2 quads; clamped to what the geometry allows) "
+                         "instead of the autotuner's")
     ap.add_argument("--no-quads", action="store_true",
                     help="at most one sin/cos per pixel pair (the 2x2 quad form off)")
     ap.add_argument("--scan-frames", type=int, default=48,

@@ -82,7 +82,7 @@ def lookup(n_pix, tiles, level=0):
     if d:
         _mem[key] = d
         return dict(d)
-    return dict(DEFAULT, pairs=int(level))
+    return engine.default_launch(level)
 
 
 def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, reps=3,

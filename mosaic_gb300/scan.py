@@ -118,7 +118,7 @@ class BatchedScan:
         level, ginfo = engine.pixel_grouping(self.tiles, self.pix, beam.k, tol - third,
                                              fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0)
         self.diag.update(ginfo)
-        cfg = dict(engine.DEFAULT_LAUNCH, pairs=level)
+        cfg = engine.default_launch(level)
         cfg.update(launch or beam._kernel_launch or {})
         cfg = engine.grouping_launch(cfg, level, self.tiles, self.pix, beam.k, ginfo)
         short_r = cfg["pair_short_radius_m"]
