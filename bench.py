@@ -346,7 +346,7 @@ def run_ours(args):
     if args.no_pairs:
         level = 0
     elif args.no_quads:
-        level = min(level, 1)
+        level = min(level, 1 if ginfo["pairs_ok"] else 0)
     if args.launch:
         ppt, nt, mode = (int(v) for v in args.launch.split(","))
         launch, tune_tbl = dict(pix_per_thread=ppt, threads=nt, slices=0, pairs=mode), []

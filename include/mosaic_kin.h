@@ -104,11 +104,11 @@ typedef struct {
     int n_pix;            /* pixels in the frame */
     int slices;           /* tile ranges summed separately (FP64 reduction) */
     int tiles_per_slice;
-    int pix_blocks;       /* ceil(n_pix / (threads * pix_per_thread)) */
+    int pix_blocks;       /* ceil(pixel slots / (threads * pix_per_thread)); slots = n_pix,
+                             or with quads 4 ceil(row/2) ceil(rows/2) */
     float b[3];
     float e[3];
-    int row;              /* pixels per detector row (0: unknown); pixel quads need it even,
-                             with an even number of rows */
+    int row;              /* pixels per detector row (0: unknown; pixel quads need it) */
     int reserved[3];
 } mk_frame_desc;
 
@@ -146,8 +146,8 @@ typedef struct {
                              and across rows go to polynomials and the quad's mixed second
                              difference (pi/2) D.(w_a + w_d - w_b - w_c) is dropped: the caller
                              checks the half differences as for pairs and the dropped term
-                             against its phase budget (pix_per_thread 4 or 8; every frame
-                             needs an even row length and an even number of rows) */
+                             against its phase budget (pix_per_thread 4 or 8; an odd last
+                             column or row repeats its pixels inside the quad) */
     double pair_short_radius_m; /* with pairs or quads: tiles up to this radius keep the half
                              differences below 0.07 rad and use the short polynomials
                              (0: none does) */

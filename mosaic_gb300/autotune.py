@@ -91,19 +91,22 @@ def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, rep
     amp_real = tiles.amp_is_real() if amp_real is None else bool(amp_real)
     level = int(level)
     probe = engine.TilesView(tiles, min(tiles.n_tiles, PROBE_TILES))
+    # pairs only where their own bound holds (level 2 may come from quads
+    # on a detector whose odd rows rule pairs out)
+    pairs_ok = level >= 1 and engine.pair_delta(tiles, pix, phys.k) <= engine.PAIR_DELTA_MAX
     if candidates is None:
         candidates = [(p, t, 0) for p, t in CANDIDATES]
-        if level >= 1:
+        if pairs_ok:
             candidates += [(p, t, 1) for p, t in PAIR_CANDIDATES]
         if level >= 2:
             candidates += [(p, t, 2) for p, t in QUAD_CANDIDATES]
-    short = {1: engine.pair_short_radius(tiles, pix, phys.k) if level >= 1 else 0.0,
+    short = {1: engine.pair_short_radius(tiles, pix, phys.k) if pairs_ok else 0.0,
              2: engine.quad_bounds(tiles, pix, phys.k)["short_radius_m"] if level >= 2 else 0.0}
     results = []
     for cand in candidates:
         pix_pt, nt = cand[0], cand[1]
         pr = int(cand[2]) if len(cand) > 2 else 0
-        if pr > level:
+        if pr > level or (pr == 1 and not pairs_ok):
             continue
         cfg = dict(pix_per_thread=pix_pt, threads=nt, slices=0, pairs=pr)
         run_cfg = dict(cfg, pair_short_radius_m=short.get(pr, 0.0))

@@ -536,21 +536,29 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                              : pb * (NT * PIX) + p * NT + tid;
             accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
         }
+        // pixels this thread writes (a quad's repeated edge pixel is not)
+        unsigned keep = (1u << PIX) - 1u;
         if constexpr (PM == 2) {
             // quad j of the thread: pixels 4j..4j+3 = a, b (row 2 qz) and c, d
-            // (row 2 qz + 1) at columns 2 qy, 2 qy + 1; out-of-range quads get
-            // n_pix (loads clamp, stores skip)
-            const int half = F.row >> 1, n_quads = F.n_pix >> 2;
+            // (row 2 qz + 1) at columns 2 qy, 2 qy + 1. An odd last column or
+            // row repeats the edge pixel (u or v is then exactly 0) and only
+            // its first copy is stored; out-of-range quads get n_pix (loads
+            // clamp, stores skip).
+            const int row = max(F.row, 1), rows = F.n_pix / row;
+            const int half = (row + 1) >> 1, n_quads = half * ((rows + 1) >> 1);
 #pragma unroll
             for (int j = 0; j < PIX / 4; ++j) {
                 const int qi = pb * (NT * (PIX / 4)) + j * NT + tid;
                 if (qi < n_quads) {
                     const int qz = qi / half, qy = qi - qz * half;
-                    const int base = 2 * qz * F.row + 2 * qy;
-                    pix[4 * j] = base;
-                    pix[4 * j + 1] = base + 1;
-                    pix[4 * j + 2] = base + F.row;
-                    pix[4 * j + 3] = base + F.row + 1;
+                    const int r0 = 2 * qz, c0 = 2 * qy;
+                    const int r1 = min(r0 + 1, rows - 1), c1 = min(c0 + 1, row - 1);
+                    pix[4 * j] = r0 * row + c0;
+                    pix[4 * j + 1] = r0 * row + c1;
+                    pix[4 * j + 2] = r1 * row + c0;
+                    pix[4 * j + 3] = r1 * row + c1;
+                    if (c1 == c0) keep &= ~(0xAu << (4 * j));   // b, d repeat a, c
+                    if (r1 == r0) keep &= ~(0xCu << (4 * j));   // c, d repeat a, b
                 } else {
                     pix[4 * j] = pix[4 * j + 1] = pix[4 * j + 2] = pix[4 * j + 3] = F.n_pix;
                 }
@@ -844,7 +852,7 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
         }
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
-            if (pix[p] < F.n_pix)
+            if (pix[p] < F.n_pix && ((keep >> p) & 1u))
                 A.partial[F.part_off + (long long)slice * F.n_pix + pix[p]] =
                     make_double2((double)accr[p] - (double)cmpr[p], (double)acci[p] - (double)cmpi[p]);
         }

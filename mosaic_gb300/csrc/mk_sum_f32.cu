@@ -228,20 +228,25 @@ extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const int *fr
     if (launch->pairs == 2) {
         MK_REQUIRE(frame_rows, "mk_scan_plan: pixel quads need the row length of every frame");
         for (int f = 0; f < n_frames; ++f)
-            MK_REQUIRE(frame_rows[f] >= 2 && frame_rows[f] % 2 == 0 &&
-                           frame_pixels[f] % (2 * frame_rows[f]) == 0,
-                       "mk_scan_plan: pixel quads need an even row length and an even number "
-                       "of rows (frame %d: %d pixels, rows of %d)",
+            MK_REQUIRE(frame_rows[f] >= 1 && frame_pixels[f] % frame_rows[f] == 0,
+                       "mk_scan_plan: frame %d: %d pixels are not whole rows of %d",
                        f, frame_pixels[f], frame_rows[f]);
     }
     MkLaunchShape sh;
     int rc = mk_launch_shape(tiles->tile_atoms, launch, &sh);
     if (rc != MK_OK) return rc;
     const int ppb = launch->threads * launch->pix_per_thread;
+    // pixel slots of a frame: quads round both sides up to even (the odd
+    // edge repeats its pixels)
+    auto slots = [&](int f) -> long long {
+        if (launch->pairs != 2) return frame_pixels[f];
+        const long long row = frame_rows[f], rows = frame_pixels[f] / row;
+        return 4LL * ((row + 1) / 2) * ((rows + 1) / 2);
+    };
     long long total_blocks = 0;
     for (int f = 0; f < n_frames; ++f) {
         MK_REQUIRE(frame_pixels[f] >= 1, "mk_scan_plan: frame %d has no pixels", f);
-        total_blocks += (frame_pixels[f] + ppb - 1) / ppb;
+        total_blocks += (slots(f) + ppb - 1) / ppb;
     }
     long long pix_off = 0, part_off = 0, item_off = 0;
     for (int f = 0; f < n_frames; ++f) {
@@ -249,7 +254,7 @@ extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const int *fr
         memset(&F, 0, sizeof(F));
         F.n_pix = frame_pixels[f];
         F.row = frame_rows ? frame_rows[f] : 0;
-        F.pix_blocks = (F.n_pix + ppb - 1) / ppb;
+        F.pix_blocks = (int)((slots(f) + ppb - 1) / ppb);
         int s = launch->slices > 0 ? std::min(launch->slices, tiles->n_tiles)
                                    : mk_frame_slices(F.pix_blocks, tiles->n_tiles, sh.resident, total_blocks);
         F.tiles_per_slice = (tiles->n_tiles + s - 1) / s;

@@ -190,13 +190,11 @@ class Pixels:
     def quad_steps(self):
         """Differences of the FP64 unit vectors u to the pixels over the 2x2
         quads (a b / c d: a, b neighbours in a row, c, d below them) of every
-        frame, or None when a frame has an odd row length or an odd number of
-        rows (no quad layout). Returns the largest norms of the row
-        difference (b - a) + (d - c), the cross-row difference
-        (c - a) + (d - b), the mixed difference (a - b) + (d - c) and the
-        diagonals d - a, c - b."""
-        if any(ny % 2 or nz % 2 for ny, nz in self.shapes):
-            return None
+        frame, laid out as the kernel does: an odd last column or row repeats
+        its pixels (the quad's difference across it is then 0). Returns the
+        largest norms of the row difference (b - a) + (d - c), the cross-row
+        difference (c - a) + (d - b), the mixed difference (a - b) + (d - c)
+        and the diagonals d - a, c - b."""
         x = self.xyz
         u = x / torch.linalg.vector_norm(x, dim=1, keepdim=True)
         # frames of one shape at once (a scan has few distinct ROI shapes);
@@ -214,6 +212,10 @@ class Pixels:
                 idx = (torch.as_tensor(offs, device=u.device)[:, None] +
                        torch.arange(m, device=u.device)[None, :])
                 U = u[idx.reshape(-1)].reshape(len(offs), nz, ny, 3)
+            if ny % 2:
+                U = torch.cat([U, U[:, :, -1:]], dim=2)
+            if nz % 2:
+                U = torch.cat([U, U[:, -1:]], dim=1)
             a, b = U[:, 0::2, 0::2], U[:, 0::2, 1::2]
             c, d = U[:, 1::2, 0::2], U[:, 1::2, 1::2]
             parts.append(torch.stack([nrm((b - a) + (d - c)), nrm((c - a) + (d - b)),
@@ -429,8 +431,7 @@ def pairs_allowed(tiles, pix: Pixels, k):
 
 
 def quad_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
-    """Error bounds of the 2x2 pixel-quad form over all tiles, or None when
-    a frame has no quad layout (odd sides).
+    """Error bounds of the 2x2 pixel-quad form over all tiles.
 
     ``delta`` [rad] bounds the two half differences u, v that go to the
     polynomials (as ``pair_delta`` does for pairs); ``short_radius_m`` is the
@@ -441,8 +442,6 @@ def quad_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
     across the quad, which the quad shares (2 ``fresnel_rad`` x the quad's
     diagonal step)."""
     st = pix.quad_steps()
-    if st is None:
-        return None
     if not tiles.n_tiles:
         return dict(delta=0.0, short_radius_m=1.0, cross=0.0, **st)
     r0 = max(pix.r0_min(), 1e-300)
@@ -459,32 +458,36 @@ def quad_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
 
 def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=False):
     """Widest legal sharing of one sin/cos between neighbouring pixels:
-    (level, info) with level 2 quads, 1 pairs, 0 none. Pairs need
-    ``pair_delta`` <= PAIR_DELTA_MAX; quads also need their half differences
-    within it and their dropped phase within ``budget_rad``; the analyser
-    kernels have neither."""
+    (level, info) with level 2 quads, 1 pairs, 0 none, and info["pairs_ok"]
+    whether pairs alone are legal. Pairs need ``pair_delta`` <=
+    PAIR_DELTA_MAX (a pair across a row end, with an odd row length, breaks
+    it); quads need their half differences within it and their dropped phase
+    within ``budget_rad``, on any detector shape; the analyser kernels have
+    neither."""
     info = dict(pair_delta_rad=pair_delta(tiles, pix, k))
-    if analyser or info["pair_delta_rad"] > PAIR_DELTA_MAX:
+    info["pairs_ok"] = (not analyser) and info["pair_delta_rad"] <= PAIR_DELTA_MAX
+    if analyser:
         return 0, info
     q = quad_bounds(tiles, pix, k, fresnel_rad)
-    if q is not None:
-        info.update(quad_delta_rad=q["delta"], quad_cross_rad=q["cross"],
-                    quad_short_radius_m=q["short_radius_m"])
-        if q["delta"] <= PAIR_DELTA_MAX and q["cross"] <= budget_rad:
-            return 2, info
-    return 1, info
+    info.update(quad_delta_rad=q["delta"], quad_cross_rad=q["cross"],
+                quad_short_radius_m=q["short_radius_m"])
+    if q["delta"] <= PAIR_DELTA_MAX and q["cross"] <= budget_rad:
+        return 2, info
+    return (1 if info["pairs_ok"] else 0), info
 
 
 def grouping_launch(cfg, level, tiles, pix, k, info):
     """Clamp a launch dict's ``pairs`` to the legal ``level`` and the pixels
-    per thread the kernels have (quads: 4 or 8; pairs: even), and set the
-    short-polynomial radius for the mode kept."""
+    per thread the kernels have (quads: 4 or 8; pairs: even, and only where
+    ``info["pairs_ok"]``), and set the short-polynomial radius for the mode
+    kept."""
     cfg = dict(cfg)
+    pairs_ok = bool(info.get("pairs_ok", level >= 1))
     mode = min(int(cfg.get("pairs", 0) or 0), int(level))
     ppt = int(cfg.get("pix_per_thread", 4))
     if mode == 2 and ppt not in (4, 8):
         mode = 1
-    if mode == 1 and ppt % 2:
+    if mode == 1 and (ppt % 2 or not pairs_ok):
         mode = 0
     cfg["pairs"] = mode
     if mode == 2:

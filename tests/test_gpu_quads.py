@@ -131,26 +131,34 @@ def test_split_quads_near_the_bound(cuda, shape, complex_beam):
     assert rel_max(got, one) <= 2e-5 + run["quad_cross_rad"], (rel_max(got, one), run)
 
 
-def test_quads_decline_to_pairs_on_odd_rows(cuda):
-    """An odd number of detector rows has no quad layout: a launch that asks
-    for quads runs pairs, and still matches the oracle."""
+@pytest.mark.parametrize("shape,pix_pt", [((24, 21), 8), ((15, 12), 4), ((13, 11), 8),
+                                           ((1, 7), 4), ((7, 1), 8), ((1, 1), 4)])
+def test_quads_on_odd_detectors(cuda, shape, pix_pt):
+    """Odd row lengths and odd numbers of rows (and single rows/columns): the
+    quad at the ragged edge repeats its pixel, computes it twice and stores it
+    once. The entry point picks quads itself (pairs are illegal when a pair
+    would span a row end); every pixel matches the oracle and one sin/cos per
+    term."""
     w, pos, spc = _cu_ni_case()
     sample = ChunkedSample([(pos, spc)])
     B = workloads._beam(10000.0, 200.0, pol_perp_rate=1.0)
     B._kernel_tile_atoms = 256
     stage = StaticStage(w.stage.rotation, w.stage.translation)
-    D = _det((24, 21), 5.5e5, w.meta["theta_deg"])
-    B._kernel_launch = dict(pix_per_thread=8, threads=128, slices=0, pairs=2)
-    got = B.atomic_scattering_kinematic(sample, D, stage, apply_polarization=True,
-                                        spherical_decay=True, return_double=True)
-    assert B.last_run["launch"]["pairs"] == 1, B.last_run
-    assert "quad_delta_rad" not in B.last_run
+    D = _det(shape, 5.5e5, w.meta["theta_deg"])
+    kw = dict(apply_polarization=True, spherical_decay=True, return_double=True)
+    B._kernel_launch = dict(pix_per_thread=pix_pt, threads=128, slices=0, pairs=2)
+    got = B.atomic_scattering_kinematic(sample, D, stage, **kw)
+    assert B.last_run["launch"]["pairs"] == 2, B.last_run
+    B._kernel_launch = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
+    one = B.atomic_scattering_kinematic(sample, D, stage, **kw)
     ref = oracle.interact_cpu([(pos, spc)], D.pixel_coordinates, D.shape, stage.rotation,
                               stage.translation, B._energy, B.tables.f0,
                               {e: B.tables.f0_zero(e) for e in ("Cu", "Ni")}, B.tables.f1f2,
                               B._beam_E0_map, B._beam_grid(), B._polarization_state(),
                               apply_polarization=True, spherical_decay=True)
+    assert got.shape == ref.shape == (shape[1], shape[0])
     assert rel_intensity(got, ref) <= 1e-4, rel_intensity(got, ref)
+    assert rel_max(got, one) <= 2e-5, rel_max(got, one)
 
 
 def _scan_frames(rois):
@@ -182,11 +190,17 @@ def test_scan_quads_match_pairs_and_single_exposures(cuda):
         assert rel_intensity(got, ref) <= 1e-4, (f, rel_intensity(got, ref))
 
 
-def test_scan_with_an_odd_roi_runs_pairs(cuda):
-    w, frames = _scan_frames([16, 64, 15, 8, 40, 32])
-    scan = BatchedScan(w.beam, w.sample, frames, **w.sc_kwargs)
-    assert "quad_delta_rad" not in scan.diag
-    # the 15-pixel rows put a pair across each row end: pairs only if that
-    # step still keeps the half difference within the bound
-    ok = scan.diag["pair_delta_rad"] <= engine.PAIR_DELTA_MAX
-    assert scan.cfg["pairs"] == (1 if ok else 0), scan.cfg
+def test_scan_with_odd_rois_runs_quads(cuda):
+    """ROIs of odd side in one batched launch: quads with repeated edge
+    pixels, every frame equal to the pair-free form."""
+    w, frames = _scan_frames([16, 15, 9, 8, 1, 33])
+    B = w.beam
+    quad = BatchedScan(B, w.sample, frames, **w.sc_kwargs)
+    assert quad.cfg["pairs"] == 2, quad.cfg
+    quad.run()
+    one = BatchedScan(B, w.sample, frames, launch=dict(pairs=0), **w.sc_kwargs)
+    assert one.cfg["pairs"] == 0
+    one.run()
+    for f in range(len(frames)):
+        got, alt = quad.frame_field(f), one.frame_field(f)
+        assert rel_max(got, alt) <= 2e-5, (f, rel_max(got, alt))

@@ -49,11 +49,19 @@ def test_quad_steps_of_a_flat_detector():
     # off-centre the mixed difference grows like y z / R^2 (p/R)^2
     far = _flat_pixels(16, 12, p, R, y0=0.05, z0=0.04).quad_steps()
     assert st["mixed"] < far["mixed"] < 10 * (p / R) ** 2
-    assert _flat_pixels(15, 12, p, R).quad_steps() is None
-    assert _flat_pixels(16, 11, p, R).quad_steps() is None
-    multi = _flat_pixels(0, 0, p, R, frames=[(8, 4), (16, 16), (6, 2)])
-    assert multi.quad_steps() is not None
-    assert _flat_pixels(0, 0, p, R, frames=[(8, 4), (7, 2)]).quad_steps() is None
+    # odd sides: the kernel repeats the edge pixel, so the quads across it
+    # have a zero difference there and the bounds are those of the rest
+    odd = _flat_pixels(15, 11, p, R).quad_steps()
+    even = _flat_pixels(14, 10, p, R).quad_steps()
+    for key in ("row", "col", "diag"):
+        assert odd[key] == pytest.approx(even[key], rel=2e-3), key
+    assert odd["mixed"] < 3 * (p / R) ** 2 * (16 * p / R)
+    one_col = _flat_pixels(1, 7, p, R).quad_steps()
+    assert one_col["row"] == 0.0 and one_col["mixed"] == 0.0
+    assert one_col["col"] == pytest.approx(2 * p / R, rel=1e-3)
+    multi = _flat_pixels(0, 0, p, R, frames=[(8, 4), (15, 16), (7, 3), (8, 4)])
+    ms = multi.quad_steps()
+    assert ms["row"] == pytest.approx(2 * p / R, rel=2e-3)
 
 
 def test_grouping_levels():
@@ -65,12 +73,16 @@ def test_grouping_levels():
     assert info["quad_cross_rad"] < 1e-6
     # the quad half differences match the pair half difference
     assert info["quad_delta_rad"] == pytest.approx(info["pair_delta_rad"], rel=2e-2)
-    # no budget left: pairs only; an odd number of rows: pairs only; odd
-    # rows: a pair spans the row end, so not even pairs; analyser: none
+    # no budget left: pairs only; odd sides: quads still (the edge repeats),
+    # but an odd row length puts a pair across each row end, so no pairs;
+    # analyser: none
     assert engine.pixel_grouping(tiles, pix, k, 1e-12)[0] == 1
-    assert engine.pixel_grouping(tiles, _flat_pixels(16, 15, 55e-6, 1.0), k, 1e-6)[0] == 1
-    assert engine.pixel_grouping(tiles, _flat_pixels(15, 16, 55e-6, 1.0), k, 1e-6)[0] == 0
-    assert engine.pixel_grouping(tiles, pix, k, 1e-6, analyser=True)[0] == 0
+    assert engine.pixel_grouping(tiles, _flat_pixels(16, 15, 55e-6, 1.0), k, 1e-6)[0] == 2
+    lv, inf = engine.pixel_grouping(tiles, _flat_pixels(15, 16, 55e-6, 1.0), k, 1e-6)
+    assert lv == 2 and not inf["pairs_ok"]
+    assert engine.pixel_grouping(tiles, _flat_pixels(15, 16, 55e-6, 1.0), k, 1e-12)[0] == 0
+    lv, inf = engine.pixel_grouping(tiles, pix, k, 1e-6, analyser=True)
+    assert lv == 0 and not inf["pairs_ok"]
     # pitch so coarse that the half difference passes 0.5 rad: none
     assert engine.pixel_grouping(tiles, _flat_pixels(16, 16, 2e-2, 1.0), k, 1e-6)[0] == 0
     # the |d|^2 term's change across the quad counts against the budget
@@ -98,3 +110,12 @@ def test_grouping_launch_clamps_the_mode():
     assert cfg["pairs"] == 1
     cfg = engine.grouping_launch(dict(pix_per_thread=4, threads=128, pairs=1), 0, tiles, pix, k, info)
     assert cfg["pairs"] == 0
+    # quads legal, pairs not (odd rows): a 2-pixel shape falls to one sin/cos a term
+    odd = _flat_pixels(15, 16, 55e-6, 1.0)
+    lv, inf = engine.pixel_grouping(tiles, odd, k, 1e-6)
+    assert engine.grouping_launch(dict(pix_per_thread=8, threads=128, pairs=2), lv, tiles, odd, k,
+                                  inf)["pairs"] == 2
+    assert engine.grouping_launch(dict(pix_per_thread=2, threads=128, pairs=2), lv, tiles, odd, k,
+                                  inf)["pairs"] == 0
+    assert engine.grouping_launch(dict(pix_per_thread=4, threads=128, pairs=1), lv, tiles, odd, k,
+                                  inf)["pairs"] == 0
