@@ -351,7 +351,40 @@ class SurrogateScan:
             torch.zeros((self.rank, n_tr), dtype=torch.float32, device=self.dev) @ Xw
             Xw[: min(n_tr, 64)] @ torch.zeros((P, self.rank), dtype=torch.float32, device=self.dev)
             del Xw, G
+            # the target and refit arithmetic itself: on a fresh process the
+            # first use of a tensor operation loads its code (seconds on a
+            # cold file cache), which must not land in a timed phase
+            I = torch.rand((n_tr, P), dtype=torch.float32, device=self.dev) + 0.5
+            bb, cs, lmu, lsd, T, cw = self._targets(I)
+            T2 = torch.cat([T, self._frame_targets(I[:8], bb, cs, lmu, lsd)]).contiguous()
+            Yw = torch.zeros((8, bb.rank + 1), dtype=torch.float32, device=self.dev)
+            (Yw[:, : bb.rank] * cs).contiguous()
+            sh = I[:8].clamp_min_(0.0) * torch.exp(Yw[:, bb.rank:] * lsd + lmu)
+            idx = torch.as_tensor([0, 1], device=self.dev)
+            I[idx] = sh[:2] + I[idx]
+            del I, T2, sh
             torch.cuda.synchronize()
+
+    def _targets(self, I_train):
+        """Training targets from the exact training frames: the frame basis of
+        the peak-normalised frames, the standardised coefficients and log
+        peak per frame (T), and the loss's column weights."""
+        M = I_train.amax(1, keepdim=True).clamp_min(1e-300)
+        basis = FrameBasis(I_train / M, self.rank)
+        cs = basis.C.std(0, keepdim=True).clamp_min(1e-12)
+        lm = torch.log(M)
+        lmu, lsd = lm.mean(), lm.std().clamp_min(1e-6)
+        T = torch.cat([basis.C / cs, (lm - lmu) / lsd], 1).contiguous()
+        w = cs[0] ** 2
+        col_w = torch.cat([w / w.sum() * basis.rank,
+                           torch.tensor([self.scale_weight], device=self.dev)]).float().contiguous()
+        return basis, cs, lmu, lsd, T, col_w
+
+    def _frame_targets(self, I, basis, cs, lmu, lsd):
+        """Targets of further exact frames in an existing basis."""
+        M = I.amax(1, keepdim=True).clamp_min(1e-300)
+        C = (I / M - basis.mu) @ basis.V.T
+        return torch.cat([C / cs, (torch.log(M) - lmu) / lsd], 1)
 
     def exact(self, idx):
         """Exact intensities (len(idx), roi*roi) of the given frames, batched
@@ -396,15 +429,7 @@ class SurrogateScan:
         # targets: principal-component coefficients of the normalised frames
         # (standardised) and the log of each frame's peak
         t0 = time.perf_counter()
-        M = I_train.amax(1, keepdim=True).clamp_min(1e-300)
-        basis = FrameBasis(I_train / M, self.rank)
-        cs = basis.C.std(0, keepdim=True).clamp_min(1e-12)
-        lm = torch.log(M)
-        lmu, lsd = lm.mean(), lm.std().clamp_min(1e-6)
-        T = torch.cat([basis.C / cs, (lm - lmu) / lsd], 1).contiguous()
-        w = cs[0] ** 2
-        col_w = torch.cat([w / w.sum() * basis.rank,
-                           torch.tensor([self.scale_weight], device=self.dev)]).float().contiguous()
+        basis, cs, lmu, lsd, T, col_w = self._targets(I_train)
         feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=self.f_max, f_min=self.f_min)
         self.net = MLP(feats.shape[1], basis.rank + 1, self.hidden, self.n_hidden, self.seed, self.dev)
         self.losses = self.net.fit_graph(feats[torch.as_tensor(tr, device=self.dev)].contiguous(), T,
@@ -438,9 +463,7 @@ class SurrogateScan:
             # Every exact frame so far (training and judged) trains the network
             # further; the failed blocks are predicted again and one more frame
             # of each is judged; only blocks failing that too go to the exact sum.
-            Mj = I_j.amax(1, keepdim=True).clamp_min(1e-300)
-            Cj = (I_j / Mj - basis.mu) @ basis.V.T
-            Tj = torch.cat([Cj / cs, (torch.log(Mj) - lmu) / lsd], 1)
+            Tj = self._frame_targets(I_j, basis, cs, lmu, lsd)
             sel = torch.as_tensor(np.concatenate([tr, pred_idx[judged]]), device=self.dev)
             self.losses = np.concatenate([self.losses, self.net.fit_graph(
                 feats[sel].contiguous(), torch.cat([T, Tj]).contiguous(), steps=self.refine_steps,

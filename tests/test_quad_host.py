@@ -119,3 +119,15 @@ def test_grouping_launch_clamps_the_mode():
                                   inf)["pairs"] == 0
     assert engine.grouping_launch(dict(pix_per_thread=4, threads=128, pairs=1), lv, tiles, odd, k,
                                   inf)["pairs"] == 0
+
+
+def test_autotune_pick_keeps_the_default_within_noise():
+    from mosaic_gb300 import autotune
+    d = engine.default_launch(2)
+    a = dict(pix_per_thread=8, threads=64, slices=0, pairs=2)
+    b = dict(pix_per_thread=4, threads=128, slices=0, pairs=2)
+    assert autotune.pick([a, d, b], [6.40, 6.43, 6.50], 2) == d      # 0.5 %: keep
+    assert autotune.pick([a, d, b], [6.00, 6.43, 6.50], 2) == a      # 7 %: switch
+    assert autotune.pick([a, b], [6.40, 6.30], 2) == b               # no default
+    assert engine.default_launch(2)["pix_per_thread"] == 8
+    assert engine.default_launch(1) == dict(pix_per_thread=4, threads=128, slices=0, pairs=1)
