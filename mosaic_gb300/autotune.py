@@ -42,7 +42,8 @@ def _cache_path():
 
 def _src_hash():
     h = hashlib.sha1()
-    for name in ("mk_split.cuh", "mk_sum_f32.cu", "mk_split_quad.cu", "mk_split_quad8.cu"):
+    for name in ("mk_split.cuh", "mk_sum_f32.cu", "mk_split_quad.cu", "mk_split_quad8.cu",
+                 "mk_split_quad_ana.cu"):
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", name), "rb") as fh:
             h.update(fh.read())
     return h.hexdigest()[:12]

@@ -433,12 +433,11 @@ class beam:
                 level, ginfo = engine.pixel_grouping(
                     tiles, pix, self.k, tol - third,
                     fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0,
-                    analyser=bool(phys.analyser))
+                    analyser=int(phys.analyser))
                 cfg = dict(launch or self._kernel_launch or tuned_launch(pix.n, tiles, level))
-                if phys.analyser and (int(cfg.get("threads", 128)), int(cfg.get("pix_per_thread", 4))) \
-                        not in engine.ANALYSER_LAUNCHES:
-                    cfg.update(pix_per_thread=4, threads=128)
                 cfg = engine.grouping_launch(cfg, level, tiles, pix, self.k, ginfo)
+                if phys.analyser:
+                    cfg = engine.analyser_launch(cfg)
                 res = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg,
                                        fresnel=int(fresnel), out=out, accumulate=accumulate,
                                        fresnel_radius=diag["fresnel_radius_m"])

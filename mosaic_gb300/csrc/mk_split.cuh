@@ -666,7 +666,20 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
             // The |d|^2 term only for tiles wide enough to need it (uniform
             // across the block: no divergence).
             const bool fr_tile = FRESNEL && (float)o.w > A.fres_r;
-            if constexpr (PM == 2) {
+            // analyser: a warp whose pixels are all outside the acceptance
+            // skips the tile; one with a pixel the acceptance edge cuts (or
+            // any Darwin expansion) takes the per-atom loop; the rest run the
+            // pixel-sharing form and take one factor per (tile, pixel) below
+            const bool ana_skip = ANA && warp_zero, ana_atom = ANA && warp_atom && !warp_zero;
+            if (ana_skip) {
+            } else if (ana_atom) {
+                if (fr_tile)
+                    mk_tile_terms_ana<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
+                                                       agx, agy, agz, ath, ag0, ag1, csr, csi);
+                else
+                    mk_tile_terms_ana<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
+                                                        agx, agy, agz, ath, ag0, ag1, csr, csi);
+            } else if constexpr (PM == 2) {
                 constexpr int NQ = PIX / 4;
                 mk_f2 sx[NQ], sy[NQ], sz[NQ], ux[NQ], uy[NQ], uz[NQ], vx[NQ], vy[NQ], vz[NQ],
                     hp[NQ];
@@ -794,21 +807,14 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                     csr[2 * q + 1] = P_re + S_im;
                     csi[2 * q + 1] = P_im - S_re;
                 }
-            } else if (ANA && warp_zero) {
-                // every pixel of the warp is outside the acceptance for this tile
-            } else if (ANA && warp_atom) {
-                if (fr_tile)
-                    mk_tile_terms_ana<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
-                                                       agx, agy, agz, ath, ag0, ag1, csr, csi);
-                else
-                    mk_tile_terms_ana<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
-                                                        agx, agy, agz, ath, ag0, ag1, csr, csi);
             } else {
                 if (fr_tile)
                     mk_tile_terms<PIX, true, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
                 else
                     mk_tile_terms<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2], csr, csi);
-                if constexpr (ANA) {
+            }
+            if constexpr (ANA) {
+                if (!ana_skip && !ana_atom) {
 #pragma unroll
                     for (int p = 0; p < PIX; ++p) {   // one analyser factor per (tile, pixel)
                         csr[p] *= ag0[p];
@@ -895,9 +901,10 @@ static mk_split_fn mk_pick3(bool fresnel, bool cplx, bool pair, bool ana)
 mk_split_fn mk_pick_nt64(int pix, bool fresnel, bool cplx, bool pair, bool ana);
 mk_split_fn mk_pick_nt128(int pix, bool fresnel, bool cplx, bool pair, bool ana);
 mk_split_fn mk_pick_nt256(int pix, bool fresnel, bool cplx, bool pair, bool ana);
-// Pixel-quad instances (64/128/256 threads, 4 or 8 pixels a thread, no
-// analyser); defined in mk_split_quad.cu and mk_split_quad8.cu.
-mk_split_fn mk_pick_quad(int nt, int pix, bool fresnel, bool cplx);
+// Pixel-quad instances (64/128/256 threads, 4 or 8 pixels a thread; with the
+// analyser 128/256 threads); defined in mk_split_quad.cu, mk_split_quad8.cu
+// and mk_split_quad_ana.cu.
+mk_split_fn mk_pick_quad(int nt, int pix, bool fresnel, bool cplx, bool ana);
 
 #define MK_PIX_CASES(NT_)                                                  \
     switch (pix) {                                                         \

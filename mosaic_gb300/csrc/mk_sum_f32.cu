@@ -165,7 +165,7 @@ int mk_launch_reduce(const double2 *partial, int slices, int n_pix, const double
 // ----------------------------------------------------------------- launch
 static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, int pair, bool ana)
 {
-    if (pair == 2) return ana ? nullptr : mk_pick_quad(nt, pix, fresnel, cplx);
+    if (pair == 2) return mk_pick_quad(nt, pix, fresnel, cplx, ana);
     switch (nt) {
     case 64: return mk_pick_nt64(pix, fresnel, cplx, pair, ana);
     case 128: return mk_pick_nt128(pix, fresnel, cplx, pair, ana);
@@ -188,7 +188,7 @@ static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShap
                              launch->amp_real == 0, launch->pairs, ana);
     MK_REQUIRE(fn, "split kernel: unsupported launch shape threads=%d pix=%d pairs=%d%s",
                launch->threads, launch->pix_per_thread, launch->pairs,
-               ana ? " with the analyser (128/256 threads, 2/4 pixels, no pairs)"
+               ana ? " with the analyser (128/256 threads; 2/4 pixels, or quads with 4/8; no pairs)"
                    : (launch->pairs == 2 ? " (quads: 4 or 8 pixels a thread)" : ""));
     const size_t smem = mk_split_smem(tile_atoms);
     MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,

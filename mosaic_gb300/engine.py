@@ -462,11 +462,14 @@ def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=
     whether pairs alone are legal. Pairs need ``pair_delta`` <=
     PAIR_DELTA_MAX (a pair across a row end, with an odd row length, breaks
     it); quads need their half differences within it and their dropped phase
-    within ``budget_rad``, on any detector shape; the analyser kernels have
-    neither."""
+    within ``budget_rad``, on any detector shape. ``analyser`` (0 off, 1
+    top-hat, 2 Darwin): the analyser kernels have quads for the top-hat
+    (tiles the acceptance edge cuts take the per-atom loop) and no pairs; a
+    Darwin analyser expands per atom on every tile, so it shares nothing."""
+    analyser = int(analyser)
     info = dict(pair_delta_rad=pair_delta(tiles, pix, k))
     info["pairs_ok"] = (not analyser) and info["pair_delta_rad"] <= PAIR_DELTA_MAX
-    if analyser:
+    if analyser == 2:
         return 0, info
     q = quad_bounds(tiles, pix, k, fresnel_rad)
     info.update(quad_delta_rad=q["delta"], quad_cross_rad=q["cross"],
@@ -474,6 +477,19 @@ def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=
     if q["delta"] <= PAIR_DELTA_MAX and q["cross"] <= budget_rad:
         return 2, info
     return (1 if info["pairs_ok"] else 0), info
+
+
+def analyser_launch(cfg):
+    """A launch shape the analyser kernels have: quads with 128/256 threads
+    and 4/8 pixels, else one sin/cos per term with ANALYSER_LAUNCHES."""
+    cfg = dict(cfg)
+    nt, ppt = int(cfg.get("threads", 128)), int(cfg.get("pix_per_thread", 4))
+    if int(cfg.get("pairs", 0) or 0) == 2:
+        if nt not in (128, 256) or ppt not in (4, 8):
+            cfg.update(threads=128, pix_per_thread=8)
+    elif (nt, ppt) not in ANALYSER_LAUNCHES:
+        cfg.update(threads=128, pix_per_thread=4)
+    return cfg
 
 
 def grouping_launch(cfg, level, tiles, pix, k, info):

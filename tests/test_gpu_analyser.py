@@ -117,9 +117,9 @@ def test_darwin_declines_when_too_narrow(cuda):
 
 
 def test_analyser_launch_shapes(cuda):
-    """The analyser kernels exist for 128/256 threads x 2/4 pixels: another
-    shape is an argument error (never a silent drop of the analyser); the
-    default shape runs."""
+    """The analyser kernels exist for 128/256 threads x 2/4 pixels (quads: x
+    4/8 pixels): another shape is an argument error (never a silent drop of
+    the analyser); the default shape runs."""
     from mosaic_gb300 import _lib
     B, sample, D, stage, pos, spc = _setup()
     atoms = B.stage_atoms(sample, stage)
@@ -131,3 +131,34 @@ def test_analyser_launch_shapes(cuda):
         engine.run_split(tiles, pix, phys, atoms.table, launch=bad, fresnel=1)
     out = engine.run_split(tiles, pix, phys, atoms.table, fresnel=1)
     assert np.isfinite(field(out)).all()
+
+
+@pytest.mark.parametrize("launch", [dict(pix_per_thread=8, threads=128),
+                                    dict(pix_per_thread=4, threads=256)])
+def test_top_hat_runs_quads(cuda, launch):
+    """With a top-hat analyser the warps whose pixels take one factor per tile
+    run the 2x2 quad form, those the edge cuts the per-atom loop: the result
+    matches the oracle and one sin/cos per term (odd detector sides, so the
+    ragged edge quads are in it too); a Darwin analyser shares nothing."""
+    B, sample, D, stage, pos, spc = _setup(shape=(33, 31))
+    B._kernel_tile_atoms = 256
+    acc = 1.2e-3
+    kw = dict(apply_polarization=True, spherical_decay=True, return_double=True,
+              analyser_mode="top-hat", analyser_acceptance_angle_rad=acc)
+    ref = _oracle(B, D, stage, pos, spc, (1, _axis(D), acc, 0.0))
+    plain = _oracle(B, D, stage, pos, spc, None)
+    ratio = np.abs(ref) ** 2 / np.maximum(np.abs(plain) ** 2, 1e-300)
+    assert ratio.min() < 0.5 and ratio.max() > 0.5
+    B._use_fast_kernel = True
+    B._kernel_launch = dict(launch, slices=0, pairs=2)
+    got = B.atomic_scattering_kinematic(sample, D, stage, **kw).reshape(-1)
+    assert B.last_run["path"] == "split_f32" and B.last_run["launch"]["pairs"] == 2, B.last_run
+    B._kernel_launch = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
+    one = B.atomic_scattering_kinematic(sample, D, stage, **kw).reshape(-1)
+    assert B.last_run["launch"]["pairs"] == 0
+    assert rel_intensity(got, ref) <= 1e-4, rel_intensity(got, ref)
+    assert rel_max(got, one) <= 2e-5, rel_max(got, one)
+    B._kernel_launch = dict(launch, slices=0, pairs=2)
+    B.atomic_scattering_kinematic(sample, D, stage, apply_polarization=True, spherical_decay=True,
+                                  analyser_mode="darwin", analyser_darwin_halfwidth_rad=2e-3)
+    assert B.last_run["launch"]["pairs"] == 0, B.last_run

@@ -81,8 +81,12 @@ def test_grouping_levels():
     lv, inf = engine.pixel_grouping(tiles, _flat_pixels(15, 16, 55e-6, 1.0), k, 1e-6)
     assert lv == 2 and not inf["pairs_ok"]
     assert engine.pixel_grouping(tiles, _flat_pixels(15, 16, 55e-6, 1.0), k, 1e-12)[0] == 0
-    lv, inf = engine.pixel_grouping(tiles, pix, k, 1e-6, analyser=True)
+    lv, inf = engine.pixel_grouping(tiles, pix, k, 1e-6, analyser=1)     # top-hat: quads
+    assert lv == 2 and not inf["pairs_ok"]
+    lv, inf = engine.pixel_grouping(tiles, pix, k, 1e-6, analyser=2)     # Darwin: none
     assert lv == 0 and not inf["pairs_ok"]
+    lv, inf = engine.pixel_grouping(tiles, pix, k, 1e-12, analyser=1)    # no budget: none
+    assert lv == 0
     # pitch so coarse that the half difference passes 0.5 rad: none
     assert engine.pixel_grouping(tiles, _flat_pixels(16, 16, 2e-2, 1.0), k, 1e-6)[0] == 0
     # the |d|^2 term's change across the quad counts against the budget
@@ -131,3 +135,12 @@ def test_autotune_pick_keeps_the_default_within_noise():
     assert autotune.pick([a, b], [6.40, 6.30], 2) == b               # no default
     assert engine.default_launch(2)["pix_per_thread"] == 8
     assert engine.default_launch(1) == dict(pix_per_thread=4, threads=128, slices=0, pairs=1)
+
+
+def test_analyser_launch_shapes():
+    q = engine.analyser_launch(dict(pix_per_thread=8, threads=64, pairs=2))
+    assert (q["threads"], q["pix_per_thread"], q["pairs"]) == (128, 8, 2)
+    q = engine.analyser_launch(dict(pix_per_thread=4, threads=256, pairs=2))
+    assert (q["threads"], q["pix_per_thread"]) == (256, 4)
+    q = engine.analyser_launch(dict(pix_per_thread=8, threads=128, pairs=0))
+    assert (q["threads"], q["pix_per_thread"]) in engine.ANALYSER_LAUNCHES
