@@ -117,6 +117,17 @@ __device__ __forceinline__ void mk_issue_tile(const MkSplitArgs &A, float4 *s_po
     mk_tma_load_1d(s_amp + buf * T, A.tamp + (size_t)tile * T, T * sizeof(float2), &bar[buf]);
 }
 
+// A pixel's (u, 1/|P|) read again for the fold: an opaque load, so that the
+// compiler rebuilds w there instead of keeping the values from before the
+// atom loop live across it (registers the quad kernels need for occupancy).
+__device__ __forceinline__ float4 mk_ld_fold(const float4 *p)
+{
+    float4 v;
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+
 // Tile atoms in shared memory come in interleaved pairs (see mk_tiles_build):
 // float4 P[2q] = (x0, x1, y0, y1), P[2q+1] = (z0, z1, w0, w1) and
 // float4 E[q] = (re0, re1, im0, im1) for atoms 2q, 2q+1.
@@ -478,8 +489,21 @@ __device__ __forceinline__ void mk_tile_terms_quad(
 }
 
 // PM (pixel mode): 0 one sin/cos a term, 1 pixel pairs, 2 pixel quads.
+// Blocks per SM the register allocation is held to: the 8-pixel quad kernels
+// (their per-pixel state lives in shared memory) aim at MK_QUAD8_WARPS warps
+// per SM, the rest are free.
+#ifndef MK_QUAD8_WARPS
+#define MK_QUAD8_WARPS 12
+#endif
+template <int NT, int PIX, int PM, bool ANA>
+constexpr int mk_min_blocks()
+{
+    return (PM == 2 && PIX == 8 && !ANA && MK_QUAD8_WARPS * 32 / NT > 1) ? MK_QUAD8_WARPS * 32 / NT : 1;
+}
+
 template <int NT, int PIX, bool FRESNEL, bool CPLX, int PM, bool ANA>
-__global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ MkSplitArgs A)
+__global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
+    mk_split_kernel(const __grid_constant__ MkSplitArgs A)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int T = A.tile_atoms;
@@ -487,6 +511,13 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
     long long *s_item = reinterpret_cast<long long *>(smem + 64);
     float4 *s_pos = reinterpret_cast<float4 *>(smem + 128);     // [2][T]
     float2 *s_amp = reinterpret_cast<float2 *>(s_pos + 2 * T);   // [2][T]
+    // 8-pixel quad kernels keep each pixel's Kahan state (acc re, acc im,
+    // comp re, comp im) in shared memory, [PIX][NT] float4, not in registers:
+    // with it and w rebuilt in the fold they fit three 128-thread blocks per
+    // SM (152 registers) instead of two (234); measured +2 % on the 8.19M-atom
+    // step, while the 4-pixel kernels (126 registers already) lost 1.4 %.
+    constexpr bool KS = (PM == 2 && PIX == 8);
+    float4 *s_kahan = reinterpret_cast<float4 *>(s_amp + 2 * T);
     const int tid = threadIdx.x;
     const uint32_t tile_bytes = (uint32_t)T * (uint32_t)(sizeof(float4) + sizeof(float2));
 
@@ -535,6 +566,7 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
             pix[p] = PM == 1 ? pb * (NT * PIX) + 2 * ((p >> 1) * NT + tid) + (p & 1)
                              : pb * (NT * PIX) + p * NT + tid;
             accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
+            if constexpr (KS) s_kahan[p * NT + tid] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         // pixels this thread writes (a quad's repeated edge pixel is not)
         unsigned keep = (1u << PIX) - 1u;
@@ -833,7 +865,7 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
 #pragma unroll
             for (int p = 0; p < PIX; ++p) {
                 const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
-                const float4 uu = A.u[g];
+                const float4 uu = KS ? mk_ld_fold(A.u + g) : A.u[g];
                 const double4 qq = A.q[g];
                 const float uo = fmaf(uu.z, oz, fmaf(uu.y, oy, uu.x * ox));
                 const double q0 = qq.x * o.x + qq.y * o.y + qq.z * o.z;
@@ -841,23 +873,43 @@ __global__ void __launch_bounds__(NT) mk_split_kernel(const __grid_constant__ Mk
                 ph -= rintf(ph);
                 float s0, c0;
                 __sincosf(ph * TWO_PI_F, &s0, &c0);
-                const float2 Fc = mk_factor(A, s, F, wx[p], wy[p], wz[p], (float)qq.w,
+                float fx = wx[p], fy = wy[p], fz = wz[p];
+                if constexpr (KS && !ANA) {   // w again, from the fresh load
+                    fx = F.b[0] - (uu.x - (ox - uo * uu.x) * uu.w);
+                    fy = F.b[1] - (uu.y - (oy - uo * uu.y) * uu.w);
+                    fz = F.b[2] - (uu.z - (oz - uo * uu.z) * uu.w);
+                }
+                const float2 Fc = mk_factor(A, s, F, fx, fy, fz, (float)qq.w,
                                             1.f / fmaf(-uo, uu.w, 1.f));
                 const float gr = Fc.x * c0 - Fc.y * s0, gi = Fc.x * s0 + Fc.y * c0;
                 const float tr = csr[p] * gr - csi[p] * gi;
                 const float ti = csr[p] * gi + csi[p] * gr;
-                float y = tr - cmpr[p];
-                float z = accr[p] + y;
-                cmpr[p] = (z - accr[p]) - y;
-                accr[p] = z;
-                y = ti - cmpi[p];
-                z = acci[p] + y;
-                cmpi[p] = (z - acci[p]) - y;
-                acci[p] = z;
+                float ar = accr[p], ai = acci[p], kr = cmpr[p], ki = cmpi[p];
+                if constexpr (KS) {
+                    const float4 k4 = s_kahan[p * NT + tid];
+                    ar = k4.x; ai = k4.y; kr = k4.z; ki = k4.w;
+                }
+                float y = tr - kr;
+                float z = ar + y;
+                kr = (z - ar) - y;
+                ar = z;
+                y = ti - ki;
+                z = ai + y;
+                ki = (z - ai) - y;
+                ai = z;
+                if constexpr (KS) {
+                    s_kahan[p * NT + tid] = make_float4(ar, ai, kr, ki);
+                } else {
+                    accr[p] = ar; acci[p] = ai; cmpr[p] = kr; cmpi[p] = ki;
+                }
             }
         }
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
+            if constexpr (KS) {
+                const float4 k4 = s_kahan[p * NT + tid];
+                accr[p] = k4.x; acci[p] = k4.y; cmpr[p] = k4.z; cmpi[p] = k4.w;
+            }
             if (pix[p] < F.n_pix && ((keep >> p) & 1u))
                 A.partial[F.part_off + (long long)slice * F.n_pix + pix[p]] =
                     make_double2((double)accr[p] - (double)cmpr[p], (double)acci[p] - (double)cmpi[p]);

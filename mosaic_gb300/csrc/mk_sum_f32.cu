@@ -174,7 +174,14 @@ static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, int pair, b
     }
 }
 
-static size_t mk_split_smem(int T) { return 128 + (size_t)2 * T * (sizeof(float4) + sizeof(float2)); }
+// Two tile buffers; 8-pixel quad kernels add their per-pixel Kahan state.
+static size_t mk_split_smem(int T, const mk_launch *launch)
+{
+    size_t b = 128 + (size_t)2 * T * (sizeof(float4) + sizeof(float2));
+    if (launch->pairs == 2 && launch->pix_per_thread == 8)
+        b += sizeof(float4) * (size_t)launch->pix_per_thread * launch->threads;
+    return b;
+}
 
 struct MkLaunchShape {
     mk_split_fn fn;
@@ -190,7 +197,7 @@ static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShap
                launch->threads, launch->pix_per_thread, launch->pairs,
                ana ? " with the analyser (128/256 threads; 2/4 pixels, or quads with 4/8; no pairs)"
                    : (launch->pairs == 2 ? " (quads: 4 or 8 pixels a thread)" : ""));
-    const size_t smem = mk_split_smem(tile_atoms);
+    const size_t smem = mk_split_smem(tile_atoms, launch);
     MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
     int dev = 0, sms = 0, bps = 0;
@@ -349,7 +356,7 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
     }
     MK_CHECK_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned long long), st));
     const long long grid = std::min<long long>(n_items, sh.resident);
-    sh.fn<<<(unsigned)grid, launch->threads, mk_split_smem(T), st>>>(A);
+    sh.fn<<<(unsigned)grid, launch->threads, mk_split_smem(T, launch), st>>>(A);
     MK_CHECK_CUDA(cudaGetLastError());
     const unsigned rb = (unsigned)((n_total + 255) / 256);
     mk_reduce_kernel<<<rb, 256, 0, st>>>(A.partial, n_total, n_frames, f0, frames_dev,
