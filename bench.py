@@ -480,7 +480,7 @@ def run_ours(args):
                          "unit": "Gterm/s", "frac": achieved / peak_terms, "traffic": None,
                          "traffic_profile": {"workload": "nacl_screw_8m_px128 (same 8.19M atoms, 128^2 "
                                              "pixels; tiles exceed L2 as here)",
-                                             "dram_bytes_per_launch": 200094464 + 90783488,
+                                             "dram_bytes_per_launch": 207470848 + 140092928,
                                              "terms_per_launch": 8192000 * 16384,
                                              "note": "ncu dram__bytes_read+write of one launch; reads "
                                                      "~ the tile data once (concurrent items share "
