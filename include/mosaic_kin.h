@@ -291,6 +291,8 @@ int mk_scan_plan(int n_frames, const int *frame_pixels, const int *frame_rows,
 size_t mk_scan_workspace_size(long long n_partial);
 
 /* All frames of a scan in one persistent launch plus the FP64 reduction:
+ * frames_dev, n_items and n_partial come from mk_scan_plan called with this
+ * same launch (the pixel mode sets each frame's block count);
  * px holds the concatenated pixels of every frame (ny = total pixels,
  * nz = 1), each frame's prologue prepared with its own beam direction;
  * out (total pixels, 2) complex128 fields (r_e included);
