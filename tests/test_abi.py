@@ -80,3 +80,29 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_scan_plan_checks_quad_rows_before_any_cuda_call():
+    """Pixel quads need every frame's row length, and whole rows: both are
+    argument errors from mk_scan_plan, raised before it touches the GPU."""
+    L = _lib.load()
+    tiles = _lib.MkTiles(4, 128, None, None, None, None)
+    launch = _lib.MkLaunch(8, 128, 0, 1, 1, 0.0, 2, 0.0, 0.0)
+    npix = (ctypes.c_int * 2)(16, 12)
+    bdir = (ctypes.c_double * 6)(1, 0, 0, 1, 0, 0)
+    desc = (_lib.MkFrameDesc * 2)()
+    ni, npart = ctypes.c_longlong(0), ctypes.c_longlong(0)
+
+    def plan(rows):
+        return L.mk_scan_plan(2, ctypes.cast(npix, ctypes.c_void_p), rows,
+                              ctypes.cast(bdir, ctypes.c_void_p), None, ctypes.byref(tiles),
+                              ctypes.byref(launch), ctypes.cast(desc, ctypes.c_void_p),
+                              ctypes.byref(ni), ctypes.byref(npart))
+    assert plan(None) == _lib.MK_EINVAL
+    assert b"row length" in L.mk_last_error()
+    bad = (ctypes.c_int * 2)(4, 5)          # 12 pixels are not rows of 5
+    assert plan(ctypes.cast(bad, ctypes.c_void_p)) == _lib.MK_EINVAL
+    assert b"whole rows" in L.mk_last_error()
+    launch.pairs = 3
+    assert plan(ctypes.cast(bad, ctypes.c_void_p)) == _lib.MK_EINVAL
+    assert b"pairs must be" in L.mk_last_error()
