@@ -8,7 +8,7 @@ Tolerances
     contracts FMAs, which moves the ~1e10 rad absolute phase by ~1e-6 rad),
     vs its NumPy twin: 2e-7 (the reference rounds its output to float32).
   * FP32 split-phase vs FP64: 1e-4 relative intensity error
-    max|I - I_ref| / max I_ref (the spec budget), and 1e-4 of max |A|.
+    max|I - I_ref| / max I_ref (the accuracy target), and 1e-4 of max |A|.
 """
 import numpy as np
 import pytest

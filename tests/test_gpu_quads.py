@@ -1,5 +1,5 @@
 """GPU parity of the 2x2 pixel-quad form (one sin/cos for four neighbouring
-pixels): against the CPU oracle at the spec budget (1e-4 relative
+pixels): against the CPU oracle at the accuracy target (1e-4 relative
 intensity), and against one sin/cos per term at 2e-5 of max |A| (the
 truncated polynomials and the dropped mixed difference are each below
 ~2e-6 rad; the rest is FP32 rounding of two different summation orders)."""
