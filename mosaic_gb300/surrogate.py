@@ -9,8 +9,7 @@ coordinates (with Fourier features) to the standardised component
 coefficients and log M. The loss weights each coefficient by its variance, so
 that it measures the error of the frame in intensity relative to its peak --
 the quantity the exact check of predicted frames thresholds -- rather than
-in log intensity, which
-gives the dim pixels most of the weight. Every ``judge_every``-th predicted
+in log intensity, which gives the dim pixels most of the weight. Every ``judge_every``-th predicted
 frame is recomputed exactly; if its relative error max|I_pred - I| / max I
 exceeds ``tol``, the network trains further on every exact frame so far
 (training and judged), predicts that block again and one more of its frames
