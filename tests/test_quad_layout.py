@@ -1,0 +1,68 @@
+"""The pixel-quad layout, checked on the CPU: the index arithmetic of the
+quad kernels (mk_split.cuh, the PM == 2 pixel mapping and its store mask)
+and the plan's block count (mk_scan_plan's quad slots), replayed in NumPy.
+Every pixel of every frame shape must be stored exactly once, every load
+must stay inside the frame, and the blocks the plan allots must reach every
+quad."""
+import numpy as np
+import pytest
+
+
+def plan_blocks(n_pix, row, nt, ppt):
+    """mk_scan_plan: pixel slots of a quad frame and its pixel blocks."""
+    rows = n_pix // row
+    slots = 4 * ((row + 1) // 2) * ((rows + 1) // 2)
+    return (slots + nt * ppt - 1) // (nt * ppt)
+
+
+def kernel_pixels(n_pix, row, nt, ppt, pix_blocks):
+    """(loads, stores) of all threads of all pixel blocks: the kernel's quad
+    mapping, out-of-range quads set to n_pix (loads clamp, stores skip)."""
+    nq = ppt // 4
+    rows = n_pix // max(row, 1)
+    half = (row + 1) >> 1
+    n_quads = half * ((rows + 1) >> 1)
+    loads, stores = [], []
+    for pb in range(pix_blocks):
+        for tid in range(nt):
+            for j in range(nq):
+                qi = pb * (nt * nq) + j * nt + tid
+                if qi >= n_quads:
+                    loads += [n_pix - 1] * 4
+                    continue
+                qz, qy = divmod(qi, half)
+                r0, c0 = 2 * qz, 2 * qy
+                r1, c1 = min(r0 + 1, rows - 1), min(c0 + 1, row - 1)
+                pix = [r0 * row + c0, r0 * row + c1, r1 * row + c0, r1 * row + c1]
+                keep = [True, c1 != c0, r1 != r0, c1 != c0 and r1 != r0]
+                loads += pix
+                stores += [p for p, k in zip(pix, keep) if k]
+    return np.array(loads), np.array(stores)
+
+
+SHAPES = [(1, 1), (1, 7), (7, 1), (2, 2), (3, 3), (15, 12), (16, 16), (13, 11), (24, 21),
+          (64, 64), (33, 9), (128, 128), (487, 3)]
+
+
+@pytest.mark.parametrize("nt,ppt", [(64, 4), (64, 8), (128, 4), (128, 8), (256, 4), (256, 8)])
+def test_every_pixel_stored_once(nt, ppt):
+    for ny, nz in SHAPES:
+        n_pix = ny * nz
+        pb = plan_blocks(n_pix, ny, nt, ppt)
+        loads, stores = kernel_pixels(n_pix, ny, nt, ppt, pb)
+        assert loads.min() >= 0 and loads.max() < n_pix, (ny, nz)
+        assert len(stores) == n_pix, (ny, nz, len(stores))
+        assert np.array_equal(np.sort(stores), np.arange(n_pix)), (ny, nz)
+
+
+def test_quads_are_neighbours():
+    """The four pixels of a quad are a 2x2 block of the detector (row-major,
+    row length ny), or its repeated edge."""
+    ny, nz = 13, 11
+    loads, _ = kernel_pixels(ny * nz, ny, 64, 4, plan_blocks(ny * nz, ny, 64, 4))
+    for a, b, c, d in loads.reshape(-1, 4)[: ((ny + 1) // 2) * ((nz + 1) // 2)]:
+        ra, ca = divmod(a, ny)
+        assert divmod(b, ny) in ((ra, ca + 1), (ra, ca))
+        assert divmod(c, ny) in ((ra + 1, ca), (ra, ca))
+        rd, cd = divmod(d, ny)
+        assert (rd - ra, cd - ca) in ((1, 1), (0, 1), (1, 0), (0, 0))
