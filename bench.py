@@ -269,7 +269,24 @@ def surrogate_leg(args, dev):
             "unjudged_err_p50_p90_max": pct(ve), "unjudged_checked": int(len(ve)),
             "unjudged_frac_within_tol": float((ve <= 0.02).mean()) if len(ve) else None,
             "mlp": {"params": res["params"], "components": res["rank"], "final_loss": res["final_loss"],
-                    "dtype": "bf16 weights/activations, fp32 accumulate (mma.sync)"}}
+                    "dtype": "bf16 weights/activations, fp32 accumulate (mma.sync)",
+                    "training": _mlp_rate(res["params"], res["n_train"], sc.fit_steps,
+                                          res["times"]["fit"])}}
+
+
+def _mlp_rate(params, n_train, steps, seconds):
+    """The surrogate's training against the bf16 tensor peak: 6 flops per
+    parameter and sample a step (forward 2, backward 4), over the fit phase
+    (which also holds the frame basis and target set-up)."""
+    peaks, src = _peaks()
+    flops = 6.0 * float(params) * float(n_train) * float(steps)
+    tf = flops / max(seconds, 1e-12) / 1e12
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    return {"flops": flops, "tflops": tf, "peak_tflops": peak, "frac": tf / peak,
+            "peak_source": src,
+            "note": "latency-bound by design: the layers are 676 x 256 x 256 GEMMs "
+                    "(~0.1 GFLOP, a few microseconds each), far too small to fill "
+                    "the tensor cores; the whole fit is ~2 % of the scan's time"}
 
 
 def run_reference(args):
