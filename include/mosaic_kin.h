@@ -256,20 +256,23 @@ int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *sp, const mk_physi
 #define MK_NOALLOC_SCRATCH_BYTES (32u << 20)
 
 /* mk_kin_split_f32 for callers that cannot allocate device memory -- for
- * example a host application whose own pool owns all device memory and
- * hands this library only the buffers it computes on, or code recording a
- * CUDA graph, where allocating would fail or break the capture. Same
- * arguments and result as mk_kin_split_f32, without the workspace: the
- * scratch (a work counter and the per-slice partial fields) lives in one
- * fixed file-scope device array of MK_NOALLOC_SCRATCH_BYTES, and the call
- * allocates nothing (no cudaMalloc, no cudaFree, no allocating library
- * call). If the partial fields of its usual slice count do not fit, it uses
- * fewer slices; a detector of more than (MK_NOALLOC_SCRATCH_BYTES - 256)/16
- * pixels (about 2.1M) is rejected with MK_ENOMEM. The first call on a device
- * looks up the array's device address, so make it before any stream
- * capture. Every call shares the array: calls that may overlap on the GPU
- * (other streams, other host threads) race and must be serialised by the
- * caller. No counterpart in the reference. */
+ * example a host application whose own memory pool owns all of the GPU's
+ * memory and hands this library only the buffers it computes on, or a
+ * service whose device memory is fixed when it starts. Same arguments and
+ * result as mk_kin_split_f32, without the workspace: the scratch (a work
+ * counter and the per-slice partial fields) lives in one fixed file-scope
+ * device array of MK_NOALLOC_SCRATCH_BYTES, and the call allocates nothing
+ * (no cudaMalloc, no cudaFree, no allocating library call). If the partial
+ * fields of its usual slice count do not fit, it uses fewer slices; a
+ * detector of more than (MK_NOALLOC_SCRATCH_BYTES - 256)/16 pixels (about
+ * 2.1M) is rejected with MK_ENOMEM. The first call on a device (made with
+ * that device current) looks up the array's device address and keeps it for
+ * the life of the process, so make that first call before any stream
+ * capture; after cudaDeviceReset of that device the kept address is stale
+ * and this entry point must not be called again in the process. Every call
+ * shares the array, and the call clears what must start at zero: calls that
+ * may overlap on the GPU (other streams, other host threads) race and must
+ * be serialised by the caller. No counterpart in the reference. */
 int mk_kin_split_f32_noalloc(const mk_tiles *tiles, const mk_species *sp,
                              const mk_physics *phys, const mk_pixels *px,
                              const mk_launch *launch, double *out, int accumulate, void *stream);

@@ -28,6 +28,8 @@ EXTRA = {"mk_sum_f64.cu": ["--fmad=false"], "mk_depth.cu": ["--fmad=false"]}
 
 MK_OK, MK_EINVAL, MK_ENOMEM, MK_ETIMEOUT, MK_EDECLINE, MK_ECUDA = 0, -1, -2, -3, -4, -5
 MAX_SPECIES = 16
+# fixed scratch of mk_kin_split_f32_noalloc (include/mosaic_kin.h)
+MK_NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _lock = threading.Lock()
 _lib = None

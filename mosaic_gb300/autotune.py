@@ -1,23 +1,29 @@
-"""Autotuner for the split-phase kernel's launch shape.
+"""Autotuner for the split-phase kernel: atoms per tile and launch shape.
 
-Candidates are (pixels per thread, threads per block, pixel mode); the
-slice count is then chosen inside the library to fill whole waves of the GPU.
-Pair candidates (one sin/cos shared by two neighbouring pixels) and quad
-candidates (one by a 2x2 block) are only tried where the caller says the
-geometry allows them (``level`` 1 and 2). Each candidate
-is timed with CUDA events on a probe -- the first ``PROBE_TILES`` tiles
-against every pixel, the same per-term work as the full problem -- the
-three fastest again, interleaved, on a probe four times larger, and the
-winner is cached per (device, detector-size bucket, tile size, kernel source
-hash) in a JSON file, like the
-reference's tune store (Beam.py:8871-8940, hardware.py:1048-1081).
+Candidates are (atoms per tile, pixels per thread, threads per block, pixel
+mode); the slice count is then chosen inside the library to fill whole
+waves of the GPU. Tile sizes 512, 1024 and 2048 are tried where the caller
+passes the atoms (the tiles are rebuilt for each size); pair candidates
+(one sin/cos shared by two neighbouring pixels) and quad candidates (one by
+a 2x2 block) only where that tile size's geometry allows them. Each
+candidate is timed with CUDA events on a probe -- the first tiles holding
+``PROBE_ATOMS`` atoms against every pixel, the same per-term work as the
+full problem -- the three fastest again, interleaved, on a probe four times
+larger, and the winner is cached per (device, kind of run, detector-size
+bucket, kernel source hash) in a JSON file, like the reference's tune
+store (Beam.py:8850-8853, 8871-8940, hardware.py:1048-1081).
+
+Batched scans (``tune_scan``) are tuned the same way on a probe scan made of
+their first frames.
 """
 from __future__ import annotations
 
+import glob
 import hashlib
 import json
 import os
 import threading
+from dataclasses import dataclass, field
 
 import torch
 
@@ -26,10 +32,13 @@ from . import engine
 CANDIDATES = [(4, 128), (4, 256), (2, 256), (8, 128), (2, 128), (8, 64), (4, 64), (1, 256)]
 PAIR_CANDIDATES = [(4, 128), (4, 256), (8, 128), (2, 256), (8, 64)]
 QUAD_CANDIDATES = [(4, 128), (4, 256), (8, 128), (8, 64), (4, 64)]
+TILE_SIZES = (512, 1024, 2048)
+DEFAULT_TILE_ATOMS = 1024
 DEFAULT = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
-PROBE_TILES = 96
+PROBE_ATOMS = 96 * 1024
 FINALISTS, ROUNDS, FINAL_SCALE = 3, 3, 4
 KEEP_DEFAULT = 0.02
+SCAN_PROBE_FRAMES = 8
 _mem = {}
 _lock = threading.Lock()
 
@@ -41,18 +50,20 @@ def _cache_path():
 
 
 def _src_hash():
+    """Hash of every kernel source (a change to any of them retunes)."""
     h = hashlib.sha1()
-    for name in ("mk_split.cuh", "mk_sum_f32.cu", "mk_split_quad.cu", "mk_split_quad8.cu",
-                 "mk_split_quad_ana.cu"):
-        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", name), "rb") as fh:
+    csrc = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
+    for path in sorted(glob.glob(os.path.join(csrc, "*.cu")) + glob.glob(os.path.join(csrc, "*.cuh"))):
+        h.update(os.path.basename(path).encode())
+        with open(path, "rb") as fh:
             h.update(fh.read())
     return h.hexdigest()[:12]
 
 
-def _key(n_pix, tiles, level=0):
+def _key(n_pix, kind="exposure"):
     dev = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
     bucket = 1 << max(0, (int(n_pix) - 1).bit_length())
-    return f"{dev}|{bucket}|{tiles.tile_atoms}|{'spq'[int(level)]}|{_src_hash()}"
+    return f"{dev}|{kind}|{bucket}|{_src_hash()}"
 
 
 def _load():
@@ -78,14 +89,34 @@ def _store(key, val):
             pass
 
 
-def lookup(n_pix, tiles, level=0):
-    key = _key(n_pix, tiles, level)
+def cached(n_pix, kind="exposure"):
+    """The cached winner for this device, kind and detector-size bucket (a
+    launch dict with ``tile_atoms``), or None."""
+    key = _key(n_pix, kind)
     if key in _mem:
         return dict(_mem[key])
     d = _load().get(key)
     if d:
         _mem[key] = d
         return dict(d)
+    return None
+
+
+def tile_atoms(n_pix, kind="exposure"):
+    """Atoms per tile: the cached winner's, else DEFAULT_TILE_ATOMS."""
+    c = cached(n_pix, kind)
+    return int(c.get("tile_atoms", DEFAULT_TILE_ATOMS)) if c else DEFAULT_TILE_ATOMS
+
+
+def lookup(n_pix, level=0, kind="exposure", tile_atoms=None):
+    """Launch shape for a run at grouping ``level``: the cached winner when it
+    was tuned for this tile size and its pixel mode is legal here, else the
+    untuned default of the level."""
+    c = cached(n_pix, kind)
+    if c and int(c.get("pairs", 0)) <= int(level) and \
+            (tile_atoms is None or int(c.get("tile_atoms", DEFAULT_TILE_ATOMS)) == int(tile_atoms)):
+        c.pop("tile_atoms", None)
+        return c
     return engine.default_launch(level)
 
 
@@ -96,75 +127,156 @@ def pick(finalists, times, level):
     over to full problems (a 64-thread shape led the probe by 0.5 % and ran
     the 8.19M-atom step 3 % slower)."""
     best = finalists[min(range(len(times)), key=lambda i: times[i])]
-    dflt = engine.default_launch(level)
+    dflt = dict(engine.default_launch(level), tile_atoms=DEFAULT_TILE_ATOMS)
     for cfg, t in zip(finalists, times):
-        if cfg == dflt and t <= (1.0 + KEEP_DEFAULT) * min(times):
+        c = dict(cfg)
+        c.setdefault("tile_atoms", DEFAULT_TILE_ATOMS)
+        if c == dflt and t <= (1.0 + KEEP_DEFAULT) * min(times):
             return cfg
     return best
 
 
-def tune(tiles, pix, phys, table, fresnel=0, amp_real=None, candidates=None, reps=3,
-         fresnel_radius=0.0, level=0):
-    """Time every candidate on a probe of the tiles; cache and return the winner."""
-    amp_real = tiles.amp_is_real() if amp_real is None else bool(amp_real)
-    level = int(level)
-    probe = engine.TilesView(tiles, min(tiles.n_tiles, PROBE_TILES))
-    # pairs only where their own bound holds (level 2 may come from quads
-    # on a detector whose odd rows rule pairs out)
-    pairs_ok = level >= 1 and engine.pair_delta(tiles, pix, phys.k) <= engine.PAIR_DELTA_MAX
-    if candidates is None:
-        candidates = [(p, t, 0) for p, t in CANDIDATES]
-        if pairs_ok:
-            candidates += [(p, t, 1) for p, t in PAIR_CANDIDATES]
-        if level >= 2:
-            candidates += [(p, t, 2) for p, t in QUAD_CANDIDATES]
-    short = {1: engine.pair_short_radius(tiles, pix, phys.k) if pairs_ok else 0.0,
-             2: engine.quad_bounds(tiles, pix, phys.k)["short_radius_m"] if level >= 2 else 0.0}
-    def timed(view, cfg, n):
-        run_cfg = dict(cfg, pair_short_radius_m=short.get(cfg["pairs"], 0.0))
-        engine.run_split(view, pix, phys, table, launch=run_cfg, fresnel=fresnel,
-                         amp_real=amp_real, fresnel_radius=fresnel_radius)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(n):
-            engine.run_split(view, pix, phys, table, launch=run_cfg, fresnel=fresnel,
-                             amp_real=amp_real, fresnel_radius=fresnel_radius)
-        e1.record()
-        e1.synchronize()
-        return e0.elapsed_time(e1) / n
+@dataclass
+class Setup:
+    """One tile size's tiles and what its geometry allows: grouping
+    ``level`` (0 none, 1 pairs, 2 quads) with ``info`` from
+    engine.pixel_grouping, and whether the |d|^2 term is kept (``fresnel``)
+    beyond ``fresnel_radius`` [m]."""
+    tiles: object
+    level: int
+    info: dict = field(default_factory=dict)
+    fresnel: int = 0
+    fresnel_radius: float = 0.0
 
-    results = []
-    for cand in candidates:
-        pix_pt, nt = cand[0], cand[1]
-        pr = int(cand[2]) if len(cand) > 2 else 0
-        if pr > level or (pr == 1 and not pairs_ok):
-            continue
-        cfg = dict(pix_per_thread=pix_pt, threads=nt, slices=0, pairs=pr)
-        try:
-            results.append((timed(probe, cfg, reps), cfg))
-        except Exception:   # a shape that does not fit the SM is skipped
-            continue
-    if not results:
-        return dict(DEFAULT), []
-    # Run-off: the first pass's leaders are within ~2 % of each other and the
-    # short probe's noise is of that size, so the best FINALISTS are timed
-    # again, interleaved over ROUNDS rounds, on a probe FINAL_SCALE times
-    # larger; the smallest time wins.
+
+def candidates_for(level, pairs_ok):
+    out = [(p, t, 0) for p, t in CANDIDATES]
+    if pairs_ok:
+        out += [(p, t, 1) for p, t in PAIR_CANDIDATES]
+    if level >= 2:
+        out += [(p, t, 2) for p, t in QUAD_CANDIDATES]
+    return out
+
+
+def _runoff(results, timed_big, level):
+    """Time the FINALISTS best again, interleaved, and pick the winner."""
     ranked = sorted(results, key=lambda r: r[0])
     finalists = [cfg for _, cfg in ranked[:FINALISTS]]
-    if len(finalists) > 1:
-        big = engine.TilesView(tiles, min(tiles.n_tiles, FINAL_SCALE * PROBE_TILES))
-        best_t = {i: float("inf") for i in range(len(finalists))}
-        for _ in range(ROUNDS):
-            for i, cfg in enumerate(finalists):
-                best_t[i] = min(best_t[i], timed(big, cfg, 1))
-        best = pick(finalists, [best_t[i] for i in range(len(finalists))], level)
-        results = results + [(best_t[i] / FINAL_SCALE, dict(cfg, runoff=True))
-                             for i, cfg in enumerate(finalists)]
-    else:
-        best = finalists[0]
-    key = _key(pix.n, tiles, level)
+    if len(finalists) < 2:
+        return finalists[0], results
+    best_t = [float("inf")] * len(finalists)
+    for _ in range(ROUNDS):
+        for i, cfg in enumerate(finalists):
+            best_t[i] = min(best_t[i], timed_big(cfg))
+    best = pick(finalists, best_t, level)
+    return best, results + [(best_t[i] / FINAL_SCALE, dict(cfg, runoff=True))
+                            for i, cfg in enumerate(finalists)]
+
+
+def _events(fn, n):
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(n):
+        fn()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / n
+
+
+def tune(setups, pix, phys, table, amp_real=None, reps=3, kind="exposure", candidates=None):
+    """Time every candidate of every tile size on a probe; cache and return
+    (winner launch dict with ``tile_atoms``, [(ms, cfg), ...]).
+
+    ``setups``: {atoms per tile: Setup} (one entry tunes the launch shape
+    only). The probes hold the same number of atoms for every tile size.
+    """
+    results = []
+    views = {}
+    top_level = max(s.level for s in setups.values())
+    for T, su in sorted(setups.items()):
+        tiles = su.tiles
+        if not tiles.n_tiles:
+            continue
+        ar = tiles.amp_is_real() if amp_real is None else bool(amp_real)
+        n_probe = max(1, PROBE_ATOMS // int(T))
+        views[T] = (engine.TilesView(tiles, min(tiles.n_tiles, n_probe)),
+                    engine.TilesView(tiles, min(tiles.n_tiles, FINAL_SCALE * n_probe)), ar, su)
+        pairs_ok = bool(su.info.get("pairs_ok", su.level >= 1))
+        cands = candidates if candidates is not None else candidates_for(su.level, pairs_ok)
+        for cand in cands:
+            pr = int(cand[2]) if len(cand) > 2 else 0
+            if pr > su.level or (pr == 1 and not pairs_ok):
+                continue
+            cfg = dict(pix_per_thread=int(cand[0]), threads=int(cand[1]), slices=0, pairs=pr,
+                       tile_atoms=int(T))
+            try:
+                results.append((_time_exposure(views[T][0], views[T], pix, phys, table, cfg, reps), cfg))
+            except Exception:   # a shape that does not fit the SM is skipped
+                continue
+    if not results:
+        return dict(DEFAULT, tile_atoms=DEFAULT_TILE_ATOMS), []
+
+    def big(cfg):
+        v = views[cfg["tile_atoms"]]
+        return _time_exposure(v[1], v, pix, phys, table, cfg, 1)
+    best, results = _runoff(results, big, top_level)
+    key = _key(pix.n, kind)
     _mem[key] = best
     _store(key, best)
     return dict(best), results
+
+
+def _time_exposure(view, entry, pix, phys, table, cfg, n):
+    _, _, amp_real, su = entry
+    run = engine.grouping_launch({k: v for k, v in cfg.items() if k != "tile_atoms"}, su.level,
+                                 su.tiles, pix, phys.k, su.info)
+    return _events(lambda: engine.run_split(view, pix, phys, table, launch=run, fresnel=su.fresnel,
+                                            amp_real=amp_real, fresnel_radius=su.fresnel_radius), n)
+
+
+def tune_scan(scan, setups, reps=2, candidates=None):
+    """Tune a BatchedScan: candidates timed on a probe scan of its first
+    SCAN_PROBE_FRAMES frames (all their ROI shapes) against the first tiles
+    holding PROBE_ATOMS atoms. ``setups`` as in ``tune`` for the scan's own
+    atoms. Returns (winner with ``tile_atoms``, results); cached per device
+    and total scan pixels."""
+    probe = scan.probe(min(len(scan.frames), SCAN_PROBE_FRAMES))
+    results = []
+    top_level = max(s.level for s in setups.values())
+    plans = {}
+    for T, su in sorted(setups.items()):
+        if not su.tiles.n_tiles:
+            continue
+        n_probe = max(1, PROBE_ATOMS // int(T))
+        plans[T] = (engine.TilesView(su.tiles, min(su.tiles.n_tiles, n_probe)),
+                    engine.TilesView(su.tiles, min(su.tiles.n_tiles, FINAL_SCALE * n_probe)), su)
+        pairs_ok = bool(su.info.get("pairs_ok", su.level >= 1))
+        cands = candidates if candidates is not None else candidates_for(su.level, pairs_ok)
+        for cand in cands:
+            pr = int(cand[2]) if len(cand) > 2 else 0
+            if pr > su.level or (pr == 1 and not pairs_ok):
+                continue
+            cfg = dict(pix_per_thread=int(cand[0]), threads=int(cand[1]), slices=0, pairs=pr,
+                       tile_atoms=int(T))
+            try:
+                results.append((_time_scan(probe, plans[T][0], su, cfg, reps), cfg))
+            except Exception:
+                continue
+    if not results:
+        return dict(DEFAULT, tile_atoms=DEFAULT_TILE_ATOMS), []
+
+    def big(cfg):
+        p = plans[cfg["tile_atoms"]]
+        return _time_scan(probe, p[1], p[2], cfg, 1)
+    best, results = _runoff(results, big, top_level)
+    key = _key(int(scan.frame_pixels.sum()), "scan")
+    _mem[key] = best
+    _store(key, best)
+    return dict(best), results
+
+
+def _time_scan(probe, view, su, cfg, n):
+    probe.replan(view, su, {k: v for k, v in cfg.items() if k != "tile_atoms"})
+    return _events(probe.run, n)

@@ -50,7 +50,7 @@ class beam:
         # (the reference's _kernel_phase_tol_rad, Beam.py:1404-1406).
         self._use_fast_kernel = True
         self._kernel_phase_tol_rad = 1e-6
-        self._kernel_tile_atoms = 1024
+        self._kernel_tile_atoms = None      # None: autotuned (1024 untuned)
         self._kernel_launch = None          # None: autotuned
         self._debye_waller = None           # element -> B [A^2]; None = no factor
         self.tables = tables or ScatteringTables()
@@ -416,35 +416,58 @@ class beam:
                              memory_splits=max(self.last_run.get("memory_splits", 0), _depth + 1))
         return out
 
-    def _scatter_once(self, atoms, pix, phys, out=None, accumulate=False, launch=None):
-        if self._use_fast_kernel and atoms.n > 0:
-            tiles = engine.Tiles(atoms, self.k, self._kernel_tile_atoms, device=atoms.pos.device)
-            third, fresnel, tol, diag = self.split_budget(tiles, pix.r0_min())
-            excursion = 2.0 * diag["tile_radius_m"] / max(pix.r0_min(), 1e-30)
+    def split_setup(self, tiles, pix, phys=None):
+        """What the FP32 split form may do with these tiles and pixels: an
+        ``autotune.Setup`` (grouping level, |d|^2 term), or None when the
+        geometry leaves the split form's error budget (then the FP64 sum
+        runs, as the reference's fast kernel declines to its general kernel,
+        Beam.py:1376-1441). Returns (setup or None, diagnostics)."""
+        from .autotune import Setup
+        third, fresnel, tol, diag = self.split_budget(tiles, pix.r0_min())
+        excursion = 2.0 * diag["tile_radius_m"] / max(pix.r0_min(), 1e-30)
+        analyser = int(phys.analyser) if phys is not None else 0
+        if phys is not None:
             ana_err = self.analyser_budget(tiles, pix.r0_min(), phys)
             if ana_err > 1e-5:
-                self.last_run = dict(path="plain_f64", analyser_err=ana_err,
-                                     declined="Darwin analyser varies too fast across a tile", **diag)
-                return engine.run_plain(atoms, pix, phys, out=out, accumulate=accumulate)
-            if third <= tol and excursion < 1e-6:
-                # one sin/cos per pixel pair or 2x2 quad where the geometry
-                # allows it; the quad's dropped phase shares the budget with
-                # the third-order terms
-                level, ginfo = engine.pixel_grouping(
-                    tiles, pix, self.k, tol - third,
-                    fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0,
-                    analyser=int(phys.analyser))
-                cfg = dict(launch or self._kernel_launch or tuned_launch(pix.n, tiles, level))
-                cfg = engine.grouping_launch(cfg, level, tiles, pix, self.k, ginfo)
+                return None, dict(diag, analyser_err=ana_err,
+                                  declined="Darwin analyser varies too fast across a tile")
+        if not (third <= tol and excursion < 1e-6):
+            return None, dict(diag, declined="split-phase error budget")
+        # one sin/cos per pixel pair or 2x2 quad where the geometry allows
+        # it; the quad's dropped phase shares the budget with the
+        # third-order terms
+        level, ginfo = engine.pixel_grouping(tiles, pix, self.k, tol - third,
+                                             fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0,
+                                             analyser=analyser)
+        return Setup(tiles, level, ginfo, int(fresnel), diag["fresnel_radius_m"]), diag
+
+    def tile_atoms_for(self, n_pix, kind="exposure"):
+        """Atoms per tile: ``_kernel_tile_atoms`` when set, else the
+        autotuner's cached choice for this detector size (1024 untuned)."""
+        if self._kernel_tile_atoms:
+            return int(self._kernel_tile_atoms)
+        from . import autotune
+        return autotune.tile_atoms(n_pix, kind)
+
+    def _scatter_once(self, atoms, pix, phys, out=None, accumulate=False, launch=None):
+        if self._use_fast_kernel and atoms.n > 0:
+            tiles = engine.Tiles(atoms, self.k, self.tile_atoms_for(pix.n), device=atoms.pos.device)
+            su, diag = self.split_setup(tiles, pix, phys)
+            if su is not None:
+                src = "explicit" if launch else ("beam" if self._kernel_launch else "tuned")
+                cfg = dict(launch or self._kernel_launch or
+                           tuned_launch(pix.n, su.level, tiles.tile_atoms))
+                cfg = engine.grouping_launch(cfg, su.level, tiles, pix, self.k, su.info)
                 if phys.analyser:
                     cfg = engine.analyser_launch(cfg)
                 res = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg,
-                                       fresnel=int(fresnel), out=out, accumulate=accumulate,
-                                       fresnel_radius=diag["fresnel_radius_m"])
-                self.last_run = dict(path="split_f32", n_tiles=tiles.n_tiles, fresnel=fresnel,
-                                     launch=dict(cfg), **ginfo, **diag)
+                                       fresnel=su.fresnel, out=out, accumulate=accumulate,
+                                       fresnel_radius=su.fresnel_radius)
+                self.last_run = dict(path="split_f32", n_tiles=tiles.n_tiles,
+                                     tile_atoms=tiles.tile_atoms, fresnel=bool(su.fresnel),
+                                     launch=dict(cfg), launch_source=src, **su.info, **diag)
                 return res
-            self.last_run = dict(path="plain_f64", declined="split-phase error budget", **diag)
+            self.last_run = dict(path="plain_f64", **diag)
         else:
             self.last_run = dict(path="plain_f64")
         return engine.run_plain(atoms, pix, phys, out=out, accumulate=accumulate)
@@ -561,9 +584,9 @@ class beam:
         return E
 
 
-def tuned_launch(n_pix, tiles, level=0):
-    """Launch shape for the split kernel: the autotuner's cached winner, or
-    the default when none is cached (``level``: 0 no pixel sharing, 1 pairs,
-    2 quads allowed)."""
+def tuned_launch(n_pix, level=0, tile_atoms=None):
+    """Launch shape for the split kernel: the autotuner's cached winner for
+    this detector size and tile size, or the default when none is cached
+    (``level``: 0 no pixel sharing, 1 pairs, 2 quads allowed)."""
     from . import autotune
-    return autotune.lookup(n_pix, tiles, level)
+    return autotune.lookup(n_pix, level, "exposure", tile_atoms)

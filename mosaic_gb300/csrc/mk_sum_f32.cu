@@ -425,8 +425,10 @@ extern "C" int mk_kin_split_f32(const mk_tiles *tiles, const mk_species *spc,
 // ------------------------------------------------------ allocation-free entry
 // Scratch of mk_kin_split_f32_noalloc: one fixed array in every GPU that
 // loads this library, held until the process exits. Its device address is
-// looked up once per device (host code cannot use the symbol itself: on the
-// host it names a shadow object, not device memory).
+// looked up on the first call on each device (with that device current) and
+// kept: host code cannot use the symbol itself, which on the host names a
+// shadow object, not device memory. A cudaDeviceReset invalidates the kept
+// address (the header says so).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MK_NOALLOC_SCRATCH_BYTES];
 
 static std::mutex g_noalloc_mu;
@@ -483,13 +485,20 @@ extern "C" int mk_kin_split_f32_noalloc(const mk_tiles *tiles, const mk_species 
     long long n_items, n_partial;
     rc = mk_single_plan(tiles, phys, px, launch, &F, &n_items, &n_partial);
     if (rc != MK_OK) return rc;
-    if (n_partial > max_partial) {   // fewer slices: the partial fields must fit the array
-        mk_launch capped = *launch;
+    // Fewer slices when the partial fields would not fit the array; the plan
+    // and the launch then both use the capped shape.
+    mk_launch capped = *launch;
+    const mk_launch *eff = launch;
+    if (n_partial > max_partial) {
         capped.slices = (int)std::max<long long>(1, max_partial / np64);
-        rc = mk_single_plan(tiles, phys, px, &capped, &F, &n_items, &n_partial);
+        eff = &capped;
+        rc = mk_single_plan(tiles, phys, px, eff, &F, &n_items, &n_partial);
         if (rc != MK_OK) return rc;
+        MK_REQUIRE(n_partial <= max_partial,
+                   "mk_kin_split_f32_noalloc: %lld partial entries exceed the fixed scratch",
+                   n_partial);
     }
-    return mk_run_split(tiles, spc, phys, px, np64, 1, F, nullptr, n_items, n_partial, launch, out,
+    return mk_run_split(tiles, spc, phys, px, np64, 1, F, nullptr, n_items, n_partial, eff, out,
                         nullptr, accumulate, scratch, MK_NOALLOC_SCRATCH_BYTES, st);
 }
 

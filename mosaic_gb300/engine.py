@@ -194,7 +194,9 @@ class Pixels:
         its pixels (the quad's difference across it is then 0). Returns the
         largest norms of the row difference (b - a) + (d - c), the cross-row
         difference (c - a) + (d - b), the mixed difference (a - b) + (d - c)
-        and the diagonals d - a, c - b."""
+        and the diagonals d - a, c - b (computed once per Pixels object)."""
+        if getattr(self, "_quad_steps", None) is not None:
+            return dict(self._quad_steps)
         x = self.xyz
         u = x / torch.linalg.vector_norm(x, dim=1, keepdim=True)
         # frames of one shape at once (a scan has few distinct ROI shapes);
@@ -222,7 +224,8 @@ class Pixels:
                                       nrm((a - b) + (d - c)),
                                       torch.maximum(nrm(d - a), nrm(c - b))]))
         row, col, mixed, diag = torch.stack(parts).amax(0).tolist()
-        return dict(row=row, col=col, mixed=mixed, diag=diag)
+        self._quad_steps = dict(row=row, col=col, mixed=mixed, diag=diag)
+        return dict(self._quad_steps)
 
 
 @dataclass

@@ -61,11 +61,16 @@ class BatchedScan:
         frames: list of Frame.
         apply_polarization, spherical_decay, remove_forward: as in
             ``atomic_scattering_kinematic``.
-        launch: split-kernel launch shape (None: autotuned or default).
+        launch: split-kernel launch shape (None: the beam's ``_kernel_launch``,
+            else the autotuner's cached choice for this scan size, else tuned
+            now on a probe of the first frames when ``tune``, else the
+            default).
+        staged: an earlier BatchedScan of the same sample whose atoms and
+            tiles this one reuses.
     """
 
     def __init__(self, beam, sample, frames, apply_polarization=False, spherical_decay=False,
-                 remove_forward=False, launch=None, device="cuda", staged=None):
+                 remove_forward=False, launch=None, device="cuda", staged=None, tune=True):
         self.L = engine._require_cuda()
         self.beam = beam
         self.frames = list(frames)
@@ -73,6 +78,29 @@ class BatchedScan:
             raise ValueError("a scan needs at least one frame")
         beam._require_forward_beam()
         dev = torch.device(device)
+        self._dev = dev
+        self._flags = dict(apply_polarization=apply_polarization, spherical_decay=spherical_decay,
+                           remove_forward=remove_forward)
+        pol = beam._polarization_state()
+        e_lab = np.array(pol[1:4], dtype=np.float64)
+        b_lab = np.array([1.0, 0.0, 0.0])
+        xyz, fr, bdirs, pols = [], [], [], []
+        for f in self.frames:
+            R = np.asarray(f.rotation, dtype=np.float64)
+            t = np.asarray(f.translation, dtype=np.float64)
+            P = np.asarray(f.pixels, dtype=np.float64)
+            xyz.append((R.T @ (P - t[:, None])) / 1e10)
+            b = R.T @ b_lab
+            fr.append((int(f.shape[0]), int(f.shape[1]), b))
+            bdirs.append(b)
+            pols.append(R.T @ e_lab)
+        self.frame_pixels = np.array([int(s[0]) * int(s[1]) for s in fr], dtype=np.int32)
+        self.frame_rows = np.array([int(s[0]) for s in fr], dtype=np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.frame_pixels)]).astype(np.int64)
+        n_total = int(self.offsets[-1])
+        self._bd = np.ascontiguousarray(np.array(bdirs, dtype=np.float64))
+        self._pe = np.ascontiguousarray(np.array(pols, dtype=np.float64))
+        self._staged = staged is not None
         if staged is not None:
             # reuse the atoms and tiles of an earlier scan of the same sample
             self._rmax = staged._rmax
@@ -88,65 +116,104 @@ class BatchedScan:
             # atoms in the sample frame, incident amplitude 1
             self.atoms = engine.atoms_lab(pos, idx, np.eye(3), np.zeros(3), table, device=dev)
             self.table = table
-            self.tiles = engine.Tiles(self.atoms, beam.k, beam._kernel_tile_atoms, device=dev)
-        pol = beam._polarization_state()
-        e_lab = np.array(pol[1:4], dtype=np.float64)
-        b_lab = np.array([1.0, 0.0, 0.0])
-        xyz, fr, bdirs, pols = [], [], [], []
-        for f in self.frames:
-            R = np.asarray(f.rotation, dtype=np.float64)
-            t = np.asarray(f.translation, dtype=np.float64)
-            P = np.asarray(f.pixels, dtype=np.float64)
-            xyz.append((R.T @ (P - t[:, None])) / 1e10)
-            b = R.T @ b_lab
-            fr.append((int(f.shape[0]), int(f.shape[1]), b))
-            bdirs.append(b)
-            pols.append(R.T @ e_lab)
-        self.frame_pixels = np.array([int(s[0]) * int(s[1]) for s in fr], dtype=np.int32)
-        self.offsets = np.concatenate([[0], np.cumsum(self.frame_pixels)]).astype(np.int64)
-        n_total = int(self.offsets[-1])
+            self.tiles = engine.Tiles(self.atoms, beam.k, beam.tile_atoms_for(n_total, "scan"),
+                                      device=dev)
         self.phys = beam.physics(apply_polarization, spherical_decay, remove_forward, pol=pol)
         self.pix = engine.Pixels(np.concatenate(xyz, axis=1), n_total, 1, self.phys, device=dev,
                                  frames=fr)
-        third, fresnel, tol, diag = beam.split_budget(self.tiles, self.pix.r0_min())
-        if third > tol:
+        su = self._setup(self.tiles)
+        self.tune_results = []
+        if launch:
+            cfg, src = dict(launch), "explicit"
+        elif beam._kernel_launch:
+            cfg, src = dict(beam._kernel_launch), "beam"
+        else:
+            from . import autotune
+            best = autotune.cached(n_total, "scan")
+            src = "cached" if best else "default"
+            if best is None and tune and len(self.frames) > 1:
+                best, self.tune_results = autotune.tune_scan(self, self._setups(su))
+                src = "tuned"
+            if best and not self._staged and \
+                    int(best.get("tile_atoms", self.tiles.tile_atoms)) != self.tiles.tile_atoms:
+                tiles = engine.Tiles(self.atoms, beam.k, int(best["tile_atoms"]), device=dev)
+                try:
+                    su, self.tiles = self._setup(tiles), tiles
+                except _lib.DeclineError:
+                    pass
+            cfg = (autotune.lookup(n_total, su.level, "scan", self.tiles.tile_atoms) if best
+                   else engine.default_launch(su.level))
+        self.launch_source = src
+        self.out = torch.zeros((n_total, 2), dtype=torch.float64, device=dev)
+        self.sums = torch.zeros(len(self.frames), dtype=torch.float64, device=dev)
+        self.ws, self.ws_bytes = None, 0
+        self.replan(self.tiles, su, cfg)
+        self.terms = float(self.atoms.n) * n_total
+
+    def _setup(self, tiles):
+        """The split form's set-up for these tiles (raises when the scan's
+        geometry leaves its error budget)."""
+        su, diag = self.beam.split_setup(tiles, self.pix)
+        if su is None:
             raise _lib.DeclineError(_lib.MK_EDECLINE,
                                     f"scan geometry outside the split-phase error budget "
-                                    f"({third:.2e} rad > {tol:.0e})")
-        self.diag = diag
-        # one sin/cos per pixel pair or 2x2 quad where every frame allows it
-        level, ginfo = engine.pixel_grouping(self.tiles, self.pix, beam.k, tol - third,
-                                             fresnel_rad=diag["fresnel_rad"] if fresnel else 0.0)
-        self.diag.update(ginfo)
-        cfg = engine.default_launch(level)
-        cfg.update(launch or beam._kernel_launch or {})
-        cfg = engine.grouping_launch(cfg, level, self.tiles, self.pix, beam.k, ginfo)
-        short_r = cfg["pair_short_radius_m"]
+                                    f"({diag.get('declined', '')}; third-order "
+                                    f"{diag['third_order_rad']:.2e} rad)")
+        self.diag = dict(diag, **su.info)
+        return su
+
+    def _setups(self, su):
+        """{atoms per tile: Setup} the tuner tries: the scan's own tiles and,
+        unless they are shared with another scan, the other tile sizes."""
+        from . import autotune
+        out = {self.tiles.tile_atoms: su}
+        if self._staged:
+            return out
+        for T in autotune.TILE_SIZES:
+            if T in out:
+                continue
+            t = engine.Tiles(self.atoms, self.beam.k, T, device=self._dev)
+            s2, _ = self.beam.split_setup(t, self.pix)
+            if s2 is not None:
+                out[T] = s2
+        self.diag = dict(self.diag)
+        return out
+
+    def probe(self, n_frames, launch=None):
+        """A scan of this scan's first ``n_frames`` frames over the same
+        staged atoms (the autotuner's probe; also a cheap warm-up of a
+        launch shape before a long scan is captured)."""
+        return BatchedScan(self.beam, None, self.frames[:n_frames], staged=self, tune=False,
+                           launch=launch or engine.default_launch(0), device=self._dev,
+                           **self._flags)
+
+    def replan(self, tiles, su, cfg):
+        """Plan the launch for ``tiles`` (this scan's, or a view of them) with
+        launch dict ``cfg`` (clamped to what ``su`` allows)."""
+        cfg = engine.grouping_launch(cfg, su.level, tiles, self.pix, self.beam.k, su.info)
         self.cfg = cfg
+        self.setup = su
+        self.tiles_run = tiles
         self.launch = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]),
-                               int(fresnel), int(self.tiles.amp_is_real()),
-                               float(diag["fresnel_radius_m"]), int(cfg["pairs"]), short_r,
+                               int(su.fresnel), int(tiles.amp_is_real()), float(su.fresnel_radius),
+                               int(cfg["pairs"]), float(cfg["pair_short_radius_m"]),
                                float(cfg.get("sin_direct_max_rad", 0.0) or 0.0))
         nf = len(self.frames)
         desc = (MkFrameDesc * nf)()
         n_items, n_part = ctypes.c_longlong(0), ctypes.c_longlong(0)
-        bd = np.ascontiguousarray(np.array(bdirs, dtype=np.float64))
-        pe = np.ascontiguousarray(np.array(pols, dtype=np.float64))
-        self.frame_rows = np.array([int(s[0]) for s in fr], dtype=np.int32)
         check(self.L.mk_scan_plan(nf, self.frame_pixels.ctypes.data, self.frame_rows.ctypes.data,
-                                  bd.ctypes.data, pe.ctypes.data,
-                                  ctypes.byref(self.tiles.abi), ctypes.byref(self.launch),
+                                  self._bd.ctypes.data, self._pe.ctypes.data,
+                                  ctypes.byref(tiles.abi), ctypes.byref(self.launch),
                                   ctypes.cast(desc, ctypes.c_void_p), ctypes.byref(n_items),
                                   ctypes.byref(n_part)))
         self.n_items, self.n_partial = int(n_items.value), int(n_part.value)
         raw = np.frombuffer(bytes(desc), dtype=np.uint8).copy()
-        self.frames_dev = torch.as_tensor(raw).to(dev)
-        self.ws_bytes = int(self.L.mk_scan_workspace_size(self.n_partial))
-        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
-        self.out = torch.zeros((n_total, 2), dtype=torch.float64, device=dev)
-        self.sums = torch.zeros(nf, dtype=torch.float64, device=dev)
+        self.frames_dev = torch.as_tensor(raw).to(self._dev)
+        need = int(self.L.mk_scan_workspace_size(self.n_partial))
+        if self.ws is None or self.ws_bytes < need:
+            self.ws = torch.empty(need, dtype=torch.uint8, device=self._dev)
+            self.ws_bytes = need
         self._graph = None
-        self.terms = float(self.atoms.n) * n_total
 
     def _check_uniform_beam(self, pos):
         B = self.beam
@@ -169,7 +236,7 @@ class BatchedScan:
     def run(self, stream=None):
         """Launch the whole scan (asynchronous); returns (fields, sums) on device."""
         sp = self.table.abi()
-        check(self.L.mk_kin_scan_f32(ctypes.byref(self.tiles.abi), ctypes.byref(sp),
+        check(self.L.mk_kin_scan_f32(ctypes.byref(self.tiles_run.abi), ctypes.byref(sp),
                                      ctypes.byref(self.phys), ctypes.byref(self.pix.abi),
                                      len(self.frames), self.frames_dev.data_ptr(), self.n_items,
                                      self.n_partial, ctypes.byref(self.launch), self.out.data_ptr(),
@@ -177,14 +244,18 @@ class BatchedScan:
                                      engine._stream_handle(stream)))
         return self.out, self.sums
 
-    def capture(self):
-        """Capture run() in a CUDA graph (frames > 1); replay() then re-runs it."""
+    def capture(self, warm=True):
+        """Capture run() in a CUDA graph (frames > 1); replay() then re-runs it.
+        ``warm`` runs the scan once outside the capture first (the kernels'
+        first-use set-up); a caller that has already run a scan with the same
+        launch shape (a short one, e.g.) may skip it."""
         if len(self.frames) < 2:
             raise ValueError("graph capture needs at least two frames")
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(s):
-            self.run(s)                 # warm-up outside the capture
+        if warm:
+            with torch.cuda.stream(s):
+                self.run(s)             # warm-up outside the capture
         torch.cuda.current_stream().wait_stream(s)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):

@@ -304,6 +304,22 @@ def nacl_screw_8m_px128():
     return w
 
 
+def spread_pixels(det_shape, n=32):
+    """Pixel indices (iz * Ny + iy) spread over the whole detector for
+    accuracy checks: an n x n grid of rows and columns from edge to edge
+    (the four corners included), plus the midpoints of the four edges and
+    the centre pixel. n = 32 gives 1,029 pixels."""
+    ny, nz = int(det_shape[0]), int(det_shape[1])
+    ys = np.unique(np.rint(np.linspace(0, ny - 1, min(n, ny))).astype(np.int64))
+    zs = np.unique(np.rint(np.linspace(0, nz - 1, min(n, nz))).astype(np.int64))
+    iz, iy = np.meshgrid(zs, ys, indexing="ij")
+    pts = set(zip(iz.ravel().tolist(), iy.ravel().tolist()))
+    my, mz = ny // 2, nz // 2
+    pts |= {(0, my), (nz - 1, my), (mz, 0), (mz, ny - 1), (mz, my)}
+    pts = sorted(pts)
+    return np.array([z * ny + y for z, y in pts], dtype=np.int64)
+
+
 CONFIGS = {"fcc_cu_32k": fcc_cu_32k, "nacl_screw_8m": nacl_screw_8m, "nacl_screw_2m": nacl_screw_2m,
            "nacl_screw_8m_px128": nacl_screw_8m_px128,
            "cu_polycrystal_18m": cu_polycrystal_18m, "cu_bumps_scan_4m": cu_bumps_scan_4m,

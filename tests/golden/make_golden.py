@@ -308,7 +308,9 @@ def depth_ein(B):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout> [--only-depth]")
+    ref = sys.argv[1]
     if len(sys.argv) > 2 and sys.argv[2] == "--only-depth":
         sys.path[:0] = [os.path.join(HERE, "_shim"), ref]
         import Beam  # noqa: E402

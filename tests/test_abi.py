@@ -106,3 +106,10 @@ def test_scan_plan_checks_quad_rows_before_any_cuda_call():
     launch.pairs = 3
     assert plan(ctypes.cast(bad, ctypes.c_void_p)) == _lib.MK_EINVAL
     assert b"pairs must be" in L.mk_last_error()
+
+
+def test_noalloc_scratch_size_matches_the_header():
+    src = open(HEADER).read()
+    m = re.search(r"#define\s+MK_NOALLOC_SCRATCH_BYTES\s+\((\d+)u\s*<<\s*(\d+)\)", src)
+    assert m, "MK_NOALLOC_SCRATCH_BYTES not found"
+    assert int(m.group(1)) << int(m.group(2)) == _lib.MK_NOALLOC_SCRATCH_BYTES

@@ -19,46 +19,18 @@ from mosaic_gb300.beam import beam as Beam
 from mosaic_gb300.sample import ChunkedSample
 
 import oracle
-from helpers import atoms_from_arrays, field, rel_intensity, rel_max, table_from_rows
+from helpers import (atoms_from_arrays, field, kernel_case, oracle_case, rel_intensity, rel_max,
+                     run_case, table_from_rows)
 
 pytestmark = pytest.mark.gpu
-
-
-def _kernel_case(d, i):
-    p = f"c{i}_"
-    ny, nz, rf, ap, dc, k, pdeg, ex, ey, ez = d[p + "meta"]
-    return dict(pos=d[p + "pos_m"], wk=d[p + "wk"], f0z=d[p + "f0z"], anom=d[p + "anom"],
-                amp=d[p + "amp"], cxyz=d[p + "cxyz"], ny=int(ny), nz=int(nz), rf=int(rf),
-                ap=int(ap), dc=int(dc), k=float(k), pol=(pdeg, ex, ey, ez),
-                cffi=d[p + "out_cffi"], numpy=d[p + "out_numpy"])
-
-
-def _run_case(c, device, fast, tile_atoms=128):
-    table, idx = table_from_rows(c["wk"], c["f0z"], c["anom"])
-    atoms = atoms_from_arrays(c["pos"], idx, c["amp"], table, device)
-    phys = engine.physics(c["k"], (1, 0, 0), c["ap"], c["pol"], c["dc"], c["rf"])
-    pix = engine.Pixels(c["cxyz"], c["ny"], c["nz"], phys, device=device)
-    if fast:
-        tiles = engine.Tiles(atoms, c["k"], tile_atoms, device=device)
-        out = engine.run_split(tiles, pix, phys, table, fresnel=1)
-    else:
-        out = engine.run_plain(atoms, pix, phys)
-    return field(out)
-
-
-def _oracle_case(c):
-    a = c["anom"]
-    return oracle.scatter_f64(c["pos"], c["wk"], c["f0z"], a.real, a.imag, c["amp"].real,
-                              c["amp"].imag, *c["cxyz"], c["k"], c["ny"], c["nz"], c["rf"],
-                              c["ap"], c["pol"], c["dc"])
 
 
 def test_plain_f64_matches_oracle_and_reference(cuda, golden):
     d = golden("kernel_cases.npz")
     for i in range(int(d["n"])):
-        c = _kernel_case(d, i)
-        got = _run_case(c, cuda, fast=False)
-        ref = _oracle_case(c)
+        c = kernel_case(d, i)
+        got = run_case(c, cuda, fast=False)
+        ref = oracle_case(c)
         assert rel_max(got, ref) <= 1e-12, (i, rel_max(got, ref))
         assert rel_max(got, c["numpy"]) <= 2e-7, (i, rel_max(got, c["numpy"]))
         assert rel_max(got, c["cffi"]) <= 1e-5, (i, rel_max(got, c["cffi"]))
@@ -68,9 +40,9 @@ def test_plain_f64_matches_oracle_and_reference(cuda, golden):
 def test_split_f32_matches_oracle(cuda, golden, tile_atoms):
     d = golden("kernel_cases.npz")
     for i in range(int(d["n"])):
-        c = _kernel_case(d, i)
-        got = _run_case(c, cuda, fast=True, tile_atoms=tile_atoms)
-        ref = _oracle_case(c)
+        c = kernel_case(d, i)
+        got = run_case(c, cuda, fast=True, tile_atoms=tile_atoms)
+        ref = oracle_case(c)
         assert rel_intensity(got, ref) <= 1e-4, (i, rel_intensity(got, ref))
         assert rel_max(got, ref) <= 1e-4, (i, rel_max(got, ref))
 
@@ -82,7 +54,7 @@ def test_split_pairs_match_oracle(cuda, golden, pix_pt):
     d = golden("kernel_cases.npz")
     used = 0
     for i in range(int(d["n"])):
-        c = _kernel_case(d, i)
+        c = kernel_case(d, i)
         table, idx = table_from_rows(c["wk"], c["f0z"], c["anom"])
         atoms = atoms_from_arrays(c["pos"], idx, c["amp"], table, cuda)
         phys = engine.physics(c["k"], (1, 0, 0), c["ap"], c["pol"], c["dc"], c["rf"])
@@ -94,7 +66,7 @@ def test_split_pairs_match_oracle(cuda, golden, pix_pt):
         base = dict(pix_per_thread=pix_pt, threads=128, slices=0)
         got = field(engine.run_split(tiles, pix, phys, table, fresnel=1, launch=dict(base, pairs=1)))
         one = field(engine.run_split(tiles, pix, phys, table, fresnel=1, launch=base))
-        ref = _oracle_case(c)
+        ref = oracle_case(c)
         assert rel_intensity(got, ref) <= 1e-4, (i, rel_intensity(got, ref))
         assert rel_max(got, ref) <= 1e-4, (i, rel_max(got, ref))
         assert rel_max(got, one) <= 2e-5, (i, rel_max(got, one))

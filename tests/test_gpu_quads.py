@@ -11,8 +11,8 @@ from mosaic_gb300.sample import ChunkedSample
 from mosaic_gb300.scan import BatchedScan, frames_from_motors
 
 import oracle
-from helpers import atoms_from_arrays, field, rel_intensity, rel_max, table_from_rows
-from test_gpu_parity import _kernel_case, _oracle_case
+from helpers import (atoms_from_arrays, field, kernel_case, oracle_case, rel_intensity, rel_max,
+                     table_from_rows)
 
 pytestmark = pytest.mark.gpu
 
@@ -24,7 +24,7 @@ def test_split_quads_match_oracle(cuda, golden, pix_pt, threads):
     d = golden("kernel_cases.npz")
     used = 0
     for i in range(int(d["n"])):
-        c = _kernel_case(d, i)
+        c = kernel_case(d, i)
         table, idx = table_from_rows(c["wk"], c["f0z"], c["anom"])
         atoms = atoms_from_arrays(c["pos"], idx, c["amp"], table, cuda)
         phys = engine.physics(c["k"], (1, 0, 0), c["ap"], c["pol"], c["dc"], c["rf"])
@@ -38,7 +38,7 @@ def test_split_quads_match_oracle(cuda, golden, pix_pt, threads):
         base = dict(pix_per_thread=pix_pt, threads=threads, slices=0)
         got = field(engine.run_split(tiles, pix, phys, table, fresnel=1, launch=dict(base, pairs=2)))
         one = field(engine.run_split(tiles, pix, phys, table, fresnel=1, launch=base))
-        ref = _oracle_case(c)
+        ref = oracle_case(c)
         assert rel_intensity(got, ref) <= 1e-4, (i, rel_intensity(got, ref))
         assert rel_max(got, ref) <= 1e-4, (i, rel_max(got, ref))
         assert rel_max(got, one) <= 2e-5, (i, rel_max(got, one))
@@ -54,7 +54,7 @@ def test_quads_direct_sincos_argument(cuda, golden):
     d = golden("kernel_cases.npz")
     used = 0
     for i in range(int(d["n"])):
-        c = _kernel_case(d, i)
+        c = kernel_case(d, i)
         if c["ny"] % 2 or c["nz"] % 2:
             continue
         table, idx = table_from_rows(c["wk"], c["f0z"], c["anom"])
@@ -67,7 +67,7 @@ def test_quads_direct_sincos_argument(cuda, golden):
         run = lambda lim: field(engine.run_split(tiles, pix, phys, table, fresnel=0,
                                                  launch=dict(base, sin_direct_max_rad=lim)))
         always, default, never = run(1e4), run(0.0), run(-1.0)
-        ref = _oracle_case(c)
+        ref = oracle_case(c)
         for got in (always, default, never):
             assert rel_intensity(got, ref) <= 1e-4, (i, rel_intensity(got, ref))
         assert rel_max(always, never) <= 2e-5, (i, rel_max(always, never))
