@@ -57,9 +57,19 @@ MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR = 1, 10
 # short cos/sin polynomials of u and v 6, the four products with the phasor 4,
 # eight accumulators 8, sin/cos argument scaling 1, per-atom coefficients 2)
 MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD = 0.5, 9
+# 2x4 pixel-octet form (two quads sharing their half differences): per octet
+# and atom 47 FP32 lane operations on tiles that pass the phase straight to
+# the sin/cos (three dot products 9, the two quad phases 2, the four sin/cos
+# argument scalings 2, u^2 and v^2 2, short polynomials 6, 2 x 4 products 8,
+# 2 x 8 accumulators 16, per-atom coefficients 2) and 51 with the mod-1
+# reduction (4 more); ~87 % of the headline's tiles take the first: ~6 per
+# term, 0.5 MUFU
+MUFU_PER_TERM_OCT, FP32_PER_TERM_OCT = 0.5, 6
 FORMS = {0: ("one sin/cos per term", MUFU_PER_TERM, FP32_PER_TERM),
          1: ("pixel pairs (one sin/cos per two terms)", MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR),
-         2: ("2x2 pixel quads (one sin/cos per four terms)", MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD)}
+         2: ("2x2 pixel quads (one sin/cos per four terms)", MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD),
+         3: ("2x4 pixel octets (two quads sharing their half differences; one sin/cos per four "
+             "terms)", MUFU_PER_TERM_OCT, FP32_PER_TERM_OCT)}
 
 
 def _dist():
@@ -412,6 +422,8 @@ def run_ours(args):
             su.level = 0
         elif args.no_quads:
             su.level = min(su.level, 1 if su.info["pairs_ok"] else 0)
+        elif args.no_octets:
+            su.level = min(su.level, 2)
         setups[T] = su
     if not setups:
         raise RuntimeError(f"{args.config}: the split form declines this geometry")
@@ -630,10 +642,13 @@ def main():
                     help="one sin/cos per term (the pixel-pair and quad forms off)")
     ap.add_argument("--launch", default="",
                     help="fixed launch shape 'pixels_per_thread,threads,mode' (mode 0 one sin/cos "
-                         "per term, 1 pairs, 2 quads; clamped to what the geometry allows) "
+                         "per term, 1 pairs, 2 quads, 3 octets; clamped to what the geometry "
+                         "allows) "
                          "instead of the autotuner's")
     ap.add_argument("--no-quads", action="store_true",
-                    help="at most one sin/cos per pixel pair (the 2x2 quad form off)")
+                    help="at most one sin/cos per pixel pair (the 2x2 quad and octet forms off)")
+    ap.add_argument("--no-octets", action="store_true",
+                    help="at most the 2x2 quad form (the 2x4 octet form off)")
     ap.add_argument("--scan-frames", type=int, default=724,
                     help="frames of the batched-scan leg (0: skip; the configuration has 724)")
     ap.add_argument("--profile", action="store_true",

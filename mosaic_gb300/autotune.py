@@ -5,7 +5,8 @@ mode); the slice count is then chosen inside the library to fill whole
 waves of the GPU. Tile sizes 512, 1024 and 2048 are tried where the caller
 passes the atoms (the tiles are rebuilt for each size); pair candidates
 (one sin/cos shared by two neighbouring pixels) and quad candidates (one by
-a 2x2 block) only where that tile size's geometry allows them. Each
+a 2x2 block) and octet candidates (two quads sharing their half
+differences) only where that tile size's geometry allows them. Each
 candidate is timed with CUDA events on a probe -- the first tiles holding
 ``PROBE_ATOMS`` atoms against every pixel, the same per-term work as the
 full problem -- the three fastest again, interleaved, on a probe four times
@@ -32,6 +33,7 @@ from . import engine
 CANDIDATES = [(4, 128), (4, 256), (2, 256), (8, 128), (2, 128), (8, 64), (4, 64), (1, 256)]
 PAIR_CANDIDATES = [(4, 128), (4, 256), (8, 128), (2, 256), (8, 64)]
 QUAD_CANDIDATES = [(4, 128), (4, 256), (8, 128), (8, 64), (4, 64)]
+OCTET_CANDIDATES = [(8, 128), (8, 256), (8, 64)]
 TILE_SIZES = (512, 1024, 2048)
 DEFAULT_TILE_ATOMS = 1024
 DEFAULT = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
@@ -139,7 +141,7 @@ def pick(finalists, times, level):
 @dataclass
 class Setup:
     """One tile size's tiles and what its geometry allows: grouping
-    ``level`` (0 none, 1 pairs, 2 quads) with ``info`` from
+    ``level`` (0 none, 1 pairs, 2 quads, 3 octets) with ``info`` from
     engine.pixel_grouping, and whether the |d|^2 term is kept (``fresnel``)
     beyond ``fresnel_radius`` [m]."""
     tiles: object
@@ -155,6 +157,8 @@ def candidates_for(level, pairs_ok):
         out += [(p, t, 1) for p, t in PAIR_CANDIDATES]
     if level >= 2:
         out += [(p, t, 2) for p, t in QUAD_CANDIDATES]
+    if level >= 3:
+        out += [(p, t, 3) for p, t in OCTET_CANDIDATES]
     return out
 
 

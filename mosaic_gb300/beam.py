@@ -20,6 +20,7 @@ There is no CPU path: ``use_gpu=False`` and a missing GPU raise.
 from __future__ import annotations
 
 import hashlib
+import os
 import warnings
 
 import numpy as np
@@ -52,6 +53,11 @@ class beam:
         self._kernel_phase_tol_rad = 1e-6
         self._kernel_tile_atoms = None      # None: autotuned (1024 untuned)
         self._kernel_launch = None          # None: autotuned
+        # tune tile size and launch shape on the first use of a detector size
+        # (as the reference tunes its fast kernel on first use, Beam.py:8871-8940);
+        # MOSAIC_GB300_AUTOTUNE=0 uses the cached choice or the defaults only
+        self._autotune = os.environ.get("MOSAIC_GB300_AUTOTUNE", "1") != "0"
+        self.last_tune = []
         self._debye_waller = None           # element -> B [A^2]; None = no factor
         self.tables = tables or ScatteringTables()
         self.last_run = {}
@@ -449,14 +455,46 @@ class beam:
         from . import autotune
         return autotune.tile_atoms(n_pix, kind)
 
+    def choose_split(self, atoms, pix, phys, launch=None):
+        """Tiles, set-up and launch shape of the FP32 split sum for these
+        atoms and pixels: an explicit ``launch`` or ``_kernel_launch`` (tile
+        size ``_kernel_tile_atoms`` or the cached one), else the autotuner's
+        cached choice for this detector size, else -- when ``_autotune`` --
+        tuned now over tile sizes and launch shapes (the result is cached),
+        else the defaults. Returns (setup or None when the geometry declines
+        the split form, launch dict, where it came from, diagnostics)."""
+        from . import autotune
+        explicit = launch or self._kernel_launch
+        if not explicit and not phys.analyser and self._autotune and \
+                autotune.cached(pix.n) is None:
+            sizes = ([int(self._kernel_tile_atoms)] if self._kernel_tile_atoms
+                     else list(autotune.TILE_SIZES))
+            setups, diags = {}, {}
+            for T in sizes:
+                su, diag = self.split_setup(engine.Tiles(atoms, self.k, T, device=atoms.pos.device),
+                                            pix, phys)
+                diags[T] = diag
+                if su is not None:
+                    setups[T] = su
+            if not setups:
+                return None, None, "declined", diags[sizes[0]]
+            best, self.last_tune = autotune.tune(setups, pix, phys, atoms.table)
+            T = int(best.pop("tile_atoms"))
+            return setups[T], best, "tuned", diags[T]
+        tiles = engine.Tiles(atoms, self.k, self.tile_atoms_for(pix.n), device=atoms.pos.device)
+        su, diag = self.split_setup(tiles, pix, phys)
+        if su is None:
+            return None, None, "declined", diag
+        if explicit:
+            return su, dict(explicit), "explicit" if launch else "beam", diag
+        src = "cached" if autotune.cached(pix.n) is not None else "default"
+        return su, tuned_launch(pix.n, su.level, tiles.tile_atoms), src, diag
+
     def _scatter_once(self, atoms, pix, phys, out=None, accumulate=False, launch=None):
         if self._use_fast_kernel and atoms.n > 0:
-            tiles = engine.Tiles(atoms, self.k, self.tile_atoms_for(pix.n), device=atoms.pos.device)
-            su, diag = self.split_setup(tiles, pix, phys)
+            su, cfg, src, diag = self.choose_split(atoms, pix, phys, launch)
             if su is not None:
-                src = "explicit" if launch else ("beam" if self._kernel_launch else "tuned")
-                cfg = dict(launch or self._kernel_launch or
-                           tuned_launch(pix.n, su.level, tiles.tile_atoms))
+                tiles = su.tiles
                 cfg = engine.grouping_launch(cfg, su.level, tiles, pix, self.k, su.info)
                 if phys.analyser:
                     cfg = engine.analyser_launch(cfg)

@@ -488,17 +488,118 @@ __device__ __forceinline__ void mk_tile_terms_quad(
     }
 }
 
-// PM (pixel mode): 0 one sin/cos a term, 1 pixel pairs, 2 pixel quads.
+// 2x4 pixel octets: two 2x2 quads side by side in a pair of detector rows
+// (a b a' b' in the upper row, c d c' d' below) share one pair of half
+// differences u, v -- the means of the two quads' -- and take their quad
+// phases from the octet's mean phase sigma_c: the quad centres sit one pixel
+// step either side of the octet centre, and a pixel step is 2u, so
+//   2 pi sigma_0 = 2 pi sigma_c - 2 u,   2 pi sigma_1 = 2 pi sigma_c + 2 u,
+// and inside quad j the quad form applies unchanged. Dropped beyond the quad
+// form: the change of the row and column steps across the octet (the
+// octet's departure from a plane in w), which the host bounds from the
+// FP64 pixel directions against its phase budget. Per atom pair: three dot
+// products (9), the two quad phases (2), two sin/cos, u^2 and v^2 (2), the
+// polynomials (6), 2 x 4 products with the phasors and 2 x 8 accumulators:
+// ~45 FP32 lane operations per 8 terms (two quads: ~60).
+// acc[j][0..7] = K, R, S, Q (re, im) of quad j, f32x2 over atoms 2q, 2q+1.
+template <bool FR, bool CPLX, bool SHORT, bool RAD>
+__device__ __forceinline__ void mk_tile_terms_oct(
+    const float4 *__restrict__ P, const float4 *__restrict__ E, int T, mk_f2 sx, mk_f2 sy, mk_f2 sz,
+    mk_f2 ux, mk_f2 uy, mk_f2 uz, mk_f2 vx, mk_f2 vy, mk_f2 vz, mk_f2 hq, mk_f2 bx, mk_f2 by,
+    mk_f2 bz, mk_f2 (&acc)[2][8])
+{
+    const mk_f2 magic = f2_splat(MK_ROUND_MAGIC), two_pi = f2_splat(TWO_PI_F);
+    const mk_f2 one = f2_splat(1.f), m_one = f2_splat(-1.f);
+    const mk_f2 two = f2_splat(2.f), m_two = f2_splat(-2.f);
+    const mk_f2 k2 = f2_splat(-0.5f), k3 = f2_splat(-1.f / 6.f);
+    const mk_f2 k4 = f2_splat(1.f / 24.f), k5 = f2_splat(1.f / 120.f), k6 = f2_splat(-1.f / 720.f);
+    const ulonglong2 *P2 = reinterpret_cast<const ulonglong2 *>(P);
+    const ulonglong2 *E2 = reinterpret_cast<const ulonglong2 *>(E);
+#pragma unroll (kPairUnroll)
+    for (int q = 0; q < T / 2; ++q) {
+        const ulonglong2 A = P2[2 * q], B = P2[2 * q + 1], M = E2[q];
+        const mk_f2 X = A.x, Y = A.y, Z = B.x, W = B.y, ER = M.x, EI = M.y;
+        const mk_f2 e0 = CPLX ? one : ER;
+        const mk_f2 c2 = f2_mul(e0, k2), s2 = f2_mul(e0, k3);
+        mk_f2 c4 = 0ull, s4 = 0ull, c6 = 0ull;
+        if (!SHORT) {
+            c4 = f2_mul(e0, k4);
+            s4 = f2_mul(e0, k5);
+            c6 = f2_mul(e0, k6);
+        }
+        mk_f2 sig = f2_fma(Z, sz, f2_fma(Y, sy, f2_mul(X, sx)));
+        if (FR) {
+            const mk_f2 db = f2_fma(Z, bz, f2_fma(Y, by, f2_mul(X, bx)));
+            const mk_f2 sp = f2_sub(db, sig);
+            sig = f2_fma(f2_fma(f2_mul(sp, m_one), sp, W), hq, sig);
+        }
+        const mk_f2 du = f2_fma(Z, uz, f2_fma(Y, uy, f2_mul(X, ux)));
+        const mk_f2 dv = f2_fma(Z, vz, f2_fma(Y, vy, f2_mul(X, vx)));
+        const mk_f2 rc = RAD ? sig : f2_mul(f2_sub(sig, f2_sub(f2_add(sig, magic), magic)), two_pi);
+        const float2 r0 = f2_unpack(f2_fma(du, m_two, rc));
+        const float2 r1 = f2_unpack(f2_fma(du, two, rc));
+        float sa, ca, sb, cb, sc_, cc, sd, cd;
+        __sincosf(r0.x, &sa, &ca);
+        __sincosf(r0.y, &sb, &cb);
+        __sincosf(r1.x, &sc_, &cc);
+        __sincosf(r1.y, &sd, &cd);
+        mk_f2 ec[2] = {f2_pack(ca, cb), f2_pack(cc, cd)};
+        mk_f2 es[2] = {f2_pack(sa, sb), f2_pack(sc_, sd)};
+        if (CPLX) {
+            const mk_f2 EIn = f2_mul(EI, m_one);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const mk_f2 c = ec[j];
+                ec[j] = f2_fma(ER, c, f2_mul(EIn, es[j]));
+                es[j] = f2_fma(ER, es[j], f2_mul(EI, c));
+            }
+        }
+        const mk_f2 u2 = f2_mul(du, du), v2 = f2_mul(dv, dv);
+        mk_f2 cu, su, cv, sv;
+        if (SHORT) {
+            cu = f2_fma(u2, c2, e0);
+            su = f2_mul(du, f2_fma(u2, s2, e0));
+            cv = f2_fma(v2, k2, one);
+            sv = f2_mul(dv, f2_fma(v2, k3, one));
+        } else {
+            cu = f2_fma(u2, f2_fma(u2, f2_fma(u2, c6, c4), c2), e0);
+            su = f2_mul(du, f2_fma(u2, f2_fma(u2, s4, s2), e0));
+            cv = f2_fma(v2, f2_fma(v2, f2_fma(v2, k6, k4), k2), one);
+            sv = f2_mul(dv, f2_fma(v2, f2_fma(v2, k5, k3), one));
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const mk_f2 xc = f2_mul(ec[j], cu), yc = f2_mul(es[j], cu);
+            const mk_f2 xs = f2_mul(ec[j], su), ys = f2_mul(es[j], su);
+            acc[j][0] = f2_fma(xc, cv, acc[j][0]);
+            acc[j][1] = f2_fma(yc, cv, acc[j][1]);
+            acc[j][2] = f2_fma(xc, sv, acc[j][2]);
+            acc[j][3] = f2_fma(yc, sv, acc[j][3]);
+            acc[j][4] = f2_fma(xs, cv, acc[j][4]);
+            acc[j][5] = f2_fma(ys, cv, acc[j][5]);
+            acc[j][6] = f2_fma(xs, sv, acc[j][6]);
+            acc[j][7] = f2_fma(ys, sv, acc[j][7]);
+        }
+    }
+}
+
+// PM (pixel mode): 0 one sin/cos a term, 1 pixel pairs, 2 pixel quads, 3
+// pixel octets (2x4: two quads sharing their half differences).
 // Blocks per SM the register allocation is held to: the 8-pixel quad kernels
 // (their per-pixel state lives in shared memory) aim at MK_QUAD8_WARPS warps
 // per SM, the rest are free.
 #ifndef MK_QUAD8_WARPS
 #define MK_QUAD8_WARPS 12
 #endif
+#ifndef MK_OCT_WARPS
+#define MK_OCT_WARPS 12
+#endif
 template <int NT, int PIX, int PM, bool ANA>
 constexpr int mk_min_blocks()
 {
-    return (PM == 2 && PIX == 8 && !ANA && MK_QUAD8_WARPS * 32 / NT > 1) ? MK_QUAD8_WARPS * 32 / NT : 1;
+    return (PM == 2 && PIX == 8 && !ANA && MK_QUAD8_WARPS * 32 / NT > 1) ? MK_QUAD8_WARPS * 32 / NT
+           : (PM == 3 && MK_OCT_WARPS * 32 / NT > 1)                  ? MK_OCT_WARPS * 32 / NT
+                                                                       : 1;
 }
 
 template <int NT, int PIX, bool FRESNEL, bool CPLX, int PM, bool ANA>
@@ -516,7 +617,7 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
     // with it and w rebuilt in the fold they fit three 128-thread blocks per
     // SM (152 registers) instead of two (234); measured +2 % on the 8.19M-atom
     // step, while the 4-pixel kernels (126 registers already) lost 1.4 %.
-    constexpr bool KS = (PM == 2 && PIX == 8);
+    constexpr bool KS = ((PM == 2 || PM == 3) && PIX == 8);
     float4 *s_kahan = reinterpret_cast<float4 *>(s_amp + 2 * T);
     const int tid = threadIdx.x;
     const uint32_t tile_bytes = (uint32_t)T * (uint32_t)(sizeof(float4) + sizeof(float2));
@@ -570,6 +671,31 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
         }
         // pixels this thread writes (a quad's repeated edge pixel is not)
         unsigned keep = (1u << PIX) - 1u;
+        if constexpr (PM == 3) {
+            // octet of the thread: rows 2 gz, 2 gz + 1, columns 4 gy .. 4 gy + 3;
+            // pixels 0..3 = quad (a, b, c, d) at columns 4 gy, 4 gy + 1, pixels
+            // 4..7 the quad at 4 gy + 2, 4 gy + 3. The planner admits only
+            // frames of whole octets (row % 4 == 0, an even row count); past
+            // the last octet the pixels get n_pix (loads clamp, stores skip).
+            static_assert(PIX == 8, "octets are 8 pixels a thread");
+            const int row = max(F.row, 1), rows = F.n_pix / row;
+            const int gpr = row >> 2, n_oct = gpr * (rows >> 1);
+            const int gi = pb * NT + tid;
+            if (gi < n_oct) {
+                const int gz = gi / gpr, gy = gi - gz * gpr;
+                const int a0 = 2 * gz * row + 4 * gy, c0 = a0 + row;
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    pix[4 * j] = a0 + 2 * j;
+                    pix[4 * j + 1] = a0 + 2 * j + 1;
+                    pix[4 * j + 2] = c0 + 2 * j;
+                    pix[4 * j + 3] = c0 + 2 * j + 1;
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < PIX; ++p) pix[p] = F.n_pix;
+            }
+        }
         if constexpr (PM == 2) {
             // quad j of the thread: pixels 4j..4j+3 = a, b (row 2 qz) and c, d
             // (row 2 qz + 1) at columns 2 qy, 2 qy + 1. An odd last column or
@@ -711,6 +837,88 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                 else
                     mk_tile_terms_ana<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
                                                         agx, agy, agz, ath, ag0, ag1, csr, csi);
+            } else if constexpr (PM == 3) {
+                // octet vectors: mean w of the 8 pixels, and the two quads'
+                // mean half-difference vectors (pixels 0..3 and 4..7 are
+                // quads a b c d)
+                const float hpi4 = 0.785398163397448f;   // (pi/2) / 2 quads
+                float msx = 0.f, msy = 0.f, msz = 0.f, mh = 0.f;
+#pragma unroll
+                for (int p = 0; p < 8; ++p) {
+                    msx += wx[p]; msy += wy[p]; msz += wz[p]; mh += hq[p];
+                }
+                const float ax = hpi4 * (((wx[1] - wx[0]) + (wx[3] - wx[2])) + ((wx[5] - wx[4]) + (wx[7] - wx[6])));
+                const float ay = hpi4 * (((wy[1] - wy[0]) + (wy[3] - wy[2])) + ((wy[5] - wy[4]) + (wy[7] - wy[6])));
+                const float az = hpi4 * (((wz[1] - wz[0]) + (wz[3] - wz[2])) + ((wz[5] - wz[4]) + (wz[7] - wz[6])));
+                const float cx = hpi4 * (((wx[2] - wx[0]) + (wx[3] - wx[1])) + ((wx[6] - wx[4]) + (wx[7] - wx[5])));
+                const float cy = hpi4 * (((wy[2] - wy[0]) + (wy[3] - wy[1])) + ((wy[6] - wy[4]) + (wy[7] - wy[5])));
+                const float cz = hpi4 * (((wz[2] - wz[0]) + (wz[3] - wz[1])) + ((wz[6] - wz[4]) + (wz[7] - wz[5])));
+                msx *= 0.125f; msy *= 0.125f; msz *= 0.125f; mh *= 0.125f;
+                mk_f2 acc[2][8];
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) acc[j][m] = 0ull;
+                const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
+                const bool short_tile = (float)o.w <= A.pair_short_r;
+                // direct sin/cos argument (warp-uniform): the quad phases
+                // reach kappa r (2 pi |s| + 2 |u|)
+                bool rad = false;
+                if (!fr_tile && short_tile) {
+                    const float bound = (TWO_PI_F * sqrtf(fmaf(msz, msz, fmaf(msy, msy, msx * msx))) +
+                                         2.f * sqrtf(fmaf(az, az, fmaf(ay, ay, ax * ax)))) *
+                                        A.kappa * (float)o.w;
+                    rad = __all_sync(0xffffffffu, bound <= A.sin_direct);
+                }
+                const mk_f2 ux = f2_splat(ax), uy = f2_splat(ay), uz = f2_splat(az);
+                const mk_f2 vx = f2_splat(cx), vy = f2_splat(cy), vz = f2_splat(cz);
+                const mk_f2 hp = f2_splat(mh);
+                if (rad) {
+                    const mk_f2 sx = f2_splat(msx * TWO_PI_F), sy = f2_splat(msy * TWO_PI_F),
+                                sz = f2_splat(msz * TWO_PI_F);
+                    mk_tile_terms_oct<false, CPLX, true, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx, vy,
+                                                               vz, hp, bx, by, bz, acc);
+                } else {
+                    const mk_f2 sx = f2_splat(msx), sy = f2_splat(msy), sz = f2_splat(msz);
+                    if (fr_tile) {
+                        if (short_tile)
+                            mk_tile_terms_oct<true, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                                       vx, vy, vz, hp, bx, by, bz, acc);
+                        else
+                            mk_tile_terms_oct<true, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy,
+                                                                        uz, vx, vy, vz, hp, bx, by, bz,
+                                                                        acc);
+                    } else {
+                        if (short_tile)
+                            mk_tile_terms_oct<false, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy,
+                                                                        uz, vx, vy, vz, hp, bx, by, bz,
+                                                                        acc);
+                        else
+                            mk_tile_terms_oct<false, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy,
+                                                                         uz, vx, vy, vz, hp, bx, by,
+                                                                         bz, acc);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    float h[8];
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) {
+                        const float2 t2 = f2_unpack(acc[j][m]);   // halves: even, odd atoms
+                        h[m] = t2.x + t2.y;
+                    }
+                    const float Kr = h[0], Ki = h[1], Rr = h[2], Ri = h[3];
+                    const float Sr = h[4], Si = h[5], Qr = h[6], Qi = h[7];
+                    // A(s, t) = K - s t Q + i t R + i s S
+                    csr[4 * j] = (Kr - Qr) + (Ri + Si);       // a (-, -)
+                    csi[4 * j] = (Ki - Qi) - (Rr + Sr);
+                    csr[4 * j + 1] = (Kr + Qr) + (Ri - Si);   // b (+, -)
+                    csi[4 * j + 1] = (Ki + Qi) - (Rr - Sr);
+                    csr[4 * j + 2] = (Kr + Qr) - (Ri - Si);   // c (-, +)
+                    csi[4 * j + 2] = (Ki + Qi) + (Rr - Sr);
+                    csr[4 * j + 3] = (Kr - Qr) - (Ri + Si);   // d (+, +)
+                    csi[4 * j + 3] = (Ki - Qi) + (Rr + Sr);
+                }
             } else if constexpr (PM == 2) {
                 constexpr int NQ = PIX / 4;
                 mk_f2 sx[NQ], sy[NQ], sz[NQ], ux[NQ], uy[NQ], uz[NQ], vx[NQ], vy[NQ], vz[NQ],
@@ -957,6 +1165,9 @@ mk_split_fn mk_pick_nt256(int pix, bool fresnel, bool cplx, bool pair, bool ana)
 // analyser 128/256 threads); defined in mk_split_quad.cu, mk_split_quad8.cu
 // and mk_split_quad_ana.cu.
 mk_split_fn mk_pick_quad(int nt, int pix, bool fresnel, bool cplx, bool ana);
+// Pixel-octet instances (64/128/256 threads, 8 pixels a thread, no
+// analyser); defined in mk_split_oct.cu.
+mk_split_fn mk_pick_oct(int nt, int pix, bool fresnel, bool cplx, bool ana);
 
 #define MK_PIX_CASES(NT_)                                                  \
     switch (pix) {                                                         \

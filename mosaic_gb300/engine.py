@@ -228,6 +228,53 @@ class Pixels:
         return dict(self._quad_steps)
 
 
+    def octets_fit(self):
+        """True when every frame is whole 2x4 octets: rows of a multiple of 4
+        pixels and an even number of rows."""
+        return all(ny % 4 == 0 and nz % 2 == 0 for ny, nz in self.shapes)
+
+    def octet_steps(self):
+        """Departure from a plane of the FP64 unit vectors u to the pixels
+        over the 2x4 octets of every frame (rows 2i, 2i+1, columns 4j..4j+3),
+        as the octet kernels model them: the mean of the 8 u plus the mean
+        row step times the column offset (-1.5..1.5) plus the mean column
+        step times the row offset (-0.5, 0.5). Returns the largest norm of
+        that residual (``plane``), the largest |u - mean| (``extent``) and
+        the largest mean row / column step (``step``); None when a frame is
+        not whole octets. Computed once per Pixels object."""
+        if getattr(self, "_octet_steps", None) is not None:
+            return dict(self._octet_steps)
+        if not self.octets_fit():
+            return None
+        x = self.xyz
+        u = x / torch.linalg.vector_norm(x, dim=1, keepdim=True)
+        groups = {}
+        for (off, m), shp in zip(self.spans, self.shapes):
+            groups.setdefault(shp, []).append(off)
+        parts = []
+        mo = (torch.arange(4, device=u.device, dtype=u.dtype) - 1.5).view(1, 1, 1, 4, 1)
+        to = (torch.arange(2, device=u.device, dtype=u.dtype) - 0.5).view(1, 2, 1, 1, 1)
+        for (ny, nz), offs in groups.items():
+            m = ny * nz
+            if len(offs) == 1:
+                U = u[offs[0]:offs[0] + m]
+            else:
+                idx = (torch.as_tensor(offs, device=u.device)[:, None] +
+                       torch.arange(m, device=u.device)[None, :])
+                U = u[idx.reshape(-1)]
+            U = U.reshape(-1, 2, ny // 4, 4, 3)          # (row pairs, 2, octets, 4, 3)
+            mean = U.mean(dim=(1, 3), keepdim=True)
+            g = (U[:, :, :, 1:] - U[:, :, :, :-1]).mean(dim=(1, 3), keepdim=True)
+            h = (U[:, 1:] - U[:, :1]).mean(dim=(1, 3), keepdim=True)
+            res = U - (mean + mo * g + to * h)
+            nrm = lambda t: torch.linalg.vector_norm(t, dim=-1).amax()
+            parts.append(torch.stack([nrm(res), nrm(U - mean),
+                                      torch.maximum(nrm(g), nrm(h))]))
+        plane, extent, step = torch.stack(parts).amax(0).tolist()
+        self._octet_steps = dict(plane=plane, extent=extent, step=step)
+        return dict(self._octet_steps)
+
+
 @dataclass
 class Atoms:
     """Atoms on the device in the frame of the pixels."""
@@ -399,9 +446,10 @@ DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
 
 def default_launch(level=0):
     """Untuned launch shape for a pixel-sharing level (0 none, 1 pairs, 2
-    quads): quads run two per thread (8 pixels; measured 1.6-2 % above one
-    on the 8.19M-atom exposure and the 128^2 scan frames)."""
-    return dict(DEFAULT_LAUNCH, pairs=int(level), pix_per_thread=8 if int(level) == 2 else 4)
+    quads, 3 octets): quads run two per thread (8 pixels; measured 1.6-2 %
+    above one on the 8.19M-atom exposure and the 128^2 scan frames), octets
+    are 8 pixels a thread."""
+    return dict(DEFAULT_LAUNCH, pairs=int(level), pix_per_thread=8 if int(level) >= 2 else 4)
 PAIR_DELTA_MAX = 0.5     # rad: the long pair polynomials are then exact to ~2e-6 per term
 PAIR_SHORT_DELTA = 0.07  # rad: the short ones to 1e-6 (the kernel's MK_PAIR_SHORT_DELTA)
 
@@ -459,16 +507,44 @@ def quad_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
                 cross=cross, **st)
 
 
+def octet_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
+    """Error bound [rad] of the 2x4 pixel-octet form over all tiles, or None
+    when a frame is not whole octets.
+
+    The octet drops, beyond the quad form, the departure of w over its 8
+    pixels from a plane (mean, mean row step, mean column step): the kernel
+    takes both quads' half differences from the octet's mean steps and their
+    phases from the octet's mean phase. That residual of the FP64 pixel
+    directions (``Pixels.octet_steps``), widened for the tile-origin term of
+    w, times k |D| <= k r bounds the phase error; the |d|^2 term, which the
+    octet evaluates once at its centre, adds 4 ``fresnel_rad`` x the octet's
+    extent |u - mean|."""
+    st = pix.octet_steps()
+    if st is None:
+        return None
+    if not tiles.n_tiles:
+        return dict(cross=0.0, **st)
+    r0 = max(pix.r0_min(), 1e-300)
+    o_ratio = tiles.max_origin_norm() / r0
+    grow = 1.0 + 2.0 * o_ratio
+    plane = st["plane"] * grow + 12.0 * o_ratio * st["step"] ** 2
+    cross = float(k) * tiles.max_radius() * plane * 1.05 + 4.0 * float(fresnel_rad) * st["extent"]
+    return dict(cross=cross, **st)
+
+
 def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=False):
     """Widest legal sharing of one sin/cos between neighbouring pixels:
-    (level, info) with level 2 quads, 1 pairs, 0 none, and info["pairs_ok"]
-    whether pairs alone are legal. Pairs need ``pair_delta`` <=
-    PAIR_DELTA_MAX (a pair across a row end, with an odd row length, breaks
-    it); quads need their half differences within it and their dropped phase
-    within ``budget_rad``, on any detector shape. ``analyser`` (0 off, 1
-    top-hat, 2 Darwin): the analyser kernels have quads for the top-hat
-    (tiles the acceptance edge cuts take the per-atom loop) and no pairs; a
-    Darwin analyser expands per atom on every tile, so it shares nothing."""
+    (level, info) with level 3 octets, 2 quads, 1 pairs, 0 none, and
+    info["pairs_ok"] whether pairs alone are legal. Pairs need ``pair_delta``
+    <= PAIR_DELTA_MAX (a pair across a row end, with an odd row length,
+    breaks it); quads need their half differences within it and their
+    dropped phase within ``budget_rad``, on any detector shape; octets (2x4:
+    two quads sharing their half differences) need frames of whole octets
+    and their dropped phase within the budget as well. ``analyser`` (0 off,
+    1 top-hat, 2 Darwin): the analyser kernels have quads for the top-hat
+    (tiles the acceptance edge cuts take the per-atom loop) and no pairs or
+    octets; a Darwin analyser expands per atom on every tile, so it shares
+    nothing."""
     analyser = int(analyser)
     info = dict(pair_delta_rad=pair_delta(tiles, pix, k))
     info["pairs_ok"] = (not analyser) and info["pair_delta_rad"] <= PAIR_DELTA_MAX
@@ -478,6 +554,12 @@ def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=
     info.update(quad_delta_rad=q["delta"], quad_cross_rad=q["cross"],
                 quad_short_radius_m=q["short_radius_m"])
     if q["delta"] <= PAIR_DELTA_MAX and q["cross"] <= budget_rad:
+        if not analyser:
+            ob = octet_bounds(tiles, pix, k, fresnel_rad)
+            if ob is not None:
+                info["octet_cross_rad"] = ob["cross"]
+                if ob["cross"] <= budget_rad:
+                    return 3, info
         return 2, info
     return (1 if info["pairs_ok"] else 0), info
 
@@ -487,6 +569,8 @@ def analyser_launch(cfg):
     and 4/8 pixels, else one sin/cos per term with ANALYSER_LAUNCHES."""
     cfg = dict(cfg)
     nt, ppt = int(cfg.get("threads", 128)), int(cfg.get("pix_per_thread", 4))
+    if int(cfg.get("pairs", 0) or 0) == 3:
+        cfg["pairs"] = 2
     if int(cfg.get("pairs", 0) or 0) == 2:
         if nt not in (128, 256) or ppt not in (4, 8):
             cfg.update(threads=128, pix_per_thread=8)
@@ -504,12 +588,14 @@ def grouping_launch(cfg, level, tiles, pix, k, info):
     pairs_ok = bool(info.get("pairs_ok", level >= 1))
     mode = min(int(cfg.get("pairs", 0) or 0), int(level))
     ppt = int(cfg.get("pix_per_thread", 4))
+    if mode == 3 and ppt != 8:
+        mode = 2
     if mode == 2 and ppt not in (4, 8):
         mode = 1
     if mode == 1 and (ppt % 2 or not pairs_ok):
         mode = 0
     cfg["pairs"] = mode
-    if mode == 2:
+    if mode >= 2:
         cfg["pair_short_radius_m"] = info["quad_short_radius_m"]
     elif mode == 1:
         cfg["pair_short_radius_m"] = pair_short_radius(tiles, pix, k)
@@ -533,7 +619,7 @@ def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None,
     if pairs:
         short_r = cfg.get("pair_short_radius_m")
         if short_r is None:
-            short_r = (quad_bounds(tiles, pix, phys.k)["short_radius_m"] if pairs == 2
+            short_r = (quad_bounds(tiles, pix, phys.k)["short_radius_m"] if pairs >= 2
                        else pair_short_radius(tiles, pix, phys.k))
     ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
                   int(tiles.amp_is_real() if amp_real is None else bool(amp_real)),

@@ -63,14 +63,14 @@ class BatchedScan:
             ``atomic_scattering_kinematic``.
         launch: split-kernel launch shape (None: the beam's ``_kernel_launch``,
             else the autotuner's cached choice for this scan size, else tuned
-            now on a probe of the first frames when ``tune``, else the
-            default).
+            now on a probe of the first frames when ``tune`` (default: the
+            beam's ``_autotune``), else the default).
         staged: an earlier BatchedScan of the same sample whose atoms and
             tiles this one reuses.
     """
 
     def __init__(self, beam, sample, frames, apply_polarization=False, spherical_decay=False,
-                 remove_forward=False, launch=None, device="cuda", staged=None, tune=True):
+                 remove_forward=False, launch=None, device="cuda", staged=None, tune=None):
         self.L = engine._require_cuda()
         self.beam = beam
         self.frames = list(frames)
@@ -124,13 +124,15 @@ class BatchedScan:
         su = self._setup(self.tiles)
         self.tune_results = []
         if launch:
-            cfg, src = dict(launch), "explicit"
+            cfg, src = dict(engine.default_launch(su.level), **launch), "explicit"
         elif beam._kernel_launch:
-            cfg, src = dict(beam._kernel_launch), "beam"
+            cfg, src = dict(engine.default_launch(su.level), **beam._kernel_launch), "beam"
         else:
             from . import autotune
             best = autotune.cached(n_total, "scan")
             src = "cached" if best else "default"
+            if tune is None:
+                tune = beam._autotune
             if best is None and tune and len(self.frames) > 1:
                 best, self.tune_results = autotune.tune_scan(self, self._setups(su))
                 src = "tuned"

@@ -399,7 +399,9 @@ class SurrogateScan:
                                         [self.roi] * len(sub))
             if len(frames) == 1:           # a one-frame batch still goes through the scan path
                 frames = frames * 2
-            scan = BatchedScan(self.beam, self.sample, frames, staged=self._staged, **self.kw)
+            # no tuning inside the timed scan: the cached launch shape or the default
+            scan = BatchedScan(self.beam, self.sample, frames, staged=self._staged, tune=False,
+                               **self.kw)
             self._staged = self._staged or scan
             out, _ = scan.run()
             outs.append((out * out).sum(1).reshape(len(frames), -1)[: len(sub)].float())

@@ -10,6 +10,11 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
 def pytest_configure(config):
+    # Hermetic launch shapes: no tuning on first use (tests pin the shapes they
+    # check; the tuner has its own tests) and a cache of the session's own.
+    import tempfile
+    os.environ.setdefault("MOSAIC_GB300_AUTOTUNE", "0")
+    os.environ.setdefault("MOSAIC_GB300_CACHE", tempfile.mkdtemp(prefix="mosaic_gb300_tune_"))
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")
     config.addinivalue_line("markers", "slow: full-size configuration (seconds to minutes)")
 

@@ -83,8 +83,9 @@ def test_struct_layouts_match_the_header(tmp_path):
 
 
 def test_scan_plan_checks_quad_rows_before_any_cuda_call():
-    """Pixel quads need every frame's row length, and whole rows: both are
-    argument errors from mk_scan_plan, raised before it touches the GPU."""
+    """Pixel quads need every frame's row length, and whole rows; octets
+    need whole 2x4 octets; an unknown pixel mode is refused: all argument
+    errors from mk_scan_plan, raised before it touches the GPU."""
     L = _lib.load()
     tiles = _lib.MkTiles(4, 128, None, None, None, None)
     launch = _lib.MkLaunch(8, 128, 0, 1, 1, 0.0, 2, 0.0, 0.0)
@@ -104,6 +105,12 @@ def test_scan_plan_checks_quad_rows_before_any_cuda_call():
     assert plan(ctypes.cast(bad, ctypes.c_void_p)) == _lib.MK_EINVAL
     assert b"whole rows" in L.mk_last_error()
     launch.pairs = 3
+    assert plan(ctypes.cast(bad, ctypes.c_void_p)) == _lib.MK_EINVAL
+    assert b"whole rows" in L.mk_last_error()
+    odd = (ctypes.c_int * 2)(4, 6)          # 16 = 4 x 4 octets, but 12 = 2 rows of 6
+    assert plan(ctypes.cast(odd, ctypes.c_void_p)) == _lib.MK_EINVAL
+    assert b"octets" in L.mk_last_error()
+    launch.pairs = 4
     assert plan(ctypes.cast(bad, ctypes.c_void_p)) == _lib.MK_EINVAL
     assert b"pairs must be" in L.mk_last_error()
 

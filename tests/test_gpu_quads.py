@@ -174,7 +174,8 @@ def test_scan_quads_match_pairs_and_single_exposures(cuda):
     every frame matches the pair form and FP64 single exposures."""
     w, frames = _scan_frames([16, 64, 24, 8, 40, 32])
     B = w.beam
-    quad = BatchedScan(B, w.sample, frames, **w.sc_kwargs)
+    quad = BatchedScan(B, w.sample, frames, launch=dict(pix_per_thread=8, threads=128, pairs=2),
+                       **w.sc_kwargs)
     assert quad.cfg["pairs"] == 2, quad.cfg
     quad.run()
     pair = BatchedScan(B, w.sample, frames, launch=dict(pairs=1), **w.sc_kwargs)

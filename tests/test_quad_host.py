@@ -25,6 +25,8 @@ def _flat_pixels(ny, nz, pitch, dist, y0=0.0, z0=0.0, frames=None):
     st = types.SimpleNamespace(xyz=torch.tensor(np.concatenate(xyz)), spans=spans, shapes=shapes)
     st.n = off
     st.quad_steps = lambda: engine.Pixels.quad_steps(st)
+    st.octets_fit = lambda: engine.Pixels.octets_fit(st)
+    st.octet_steps = lambda: engine.Pixels.octet_steps(st)
     u = st.xyz / torch.linalg.vector_norm(st.xyz, dim=1, keepdim=True)
     st.u = torch.cat([u.float(), torch.zeros(off, 1)], 1)
     st.pair_step = lambda: engine.Pixels.pair_step(st)
@@ -144,3 +146,48 @@ def test_analyser_launch_shapes():
     assert (q["threads"], q["pix_per_thread"]) == (256, 4)
     q = engine.analyser_launch(dict(pix_per_thread=8, threads=128, pairs=0))
     assert (q["threads"], q["pix_per_thread"]) in engine.ANALYSER_LAUNCHES
+
+
+def test_octet_bounds_of_a_flat_detector():
+    """The octet's departure from a plane is the row curvature of the pixel
+    directions, ~(p/R)^2 / 2 near the axis; frames that are not whole
+    octets have none; small tiles admit octets, large ones only quads."""
+    k = 2 * np.pi / 1.2398e-10
+    p, R = 55e-6, 1.0
+    pix = _flat_pixels(16, 16, p, R)
+    st = pix.octet_steps()
+    assert 0.3 * (p / R) ** 2 < st["plane"] < 1.0 * (p / R) ** 2
+    assert st["step"] == pytest.approx(p / R, rel=1e-3)
+    assert st["extent"] == pytest.approx(np.hypot(1.5, 0.5) * p / R, rel=1e-2)
+    for shape in ((15, 16), (16, 15), (18, 16), (2, 2)):
+        assert _flat_pixels(*shape, p, R).octet_steps() is None, shape
+    multi = _flat_pixels(0, 0, p, R, frames=[(8, 4), (16, 16), (4, 2)])
+    assert multi.octet_steps()["plane"] == pytest.approx(st["plane"], rel=0.5)
+    assert _flat_pixels(0, 0, p, R, frames=[(8, 4), (6, 2)]).octet_steps() is None
+    small, big = _tiles(2e-9, 6e-8), _tiles(4.6e-8, 6e-8)
+    lv, info = engine.pixel_grouping(small, pix, k, 1e-6)
+    assert lv == 3 and info["octet_cross_rad"] < 1e-6
+    assert info["octet_cross_rad"] > info["quad_cross_rad"]
+    lv, info = engine.pixel_grouping(big, pix, k, 1e-6)
+    assert lv == 2 and info["octet_cross_rad"] > 1e-6
+    assert engine.pixel_grouping(small, _flat_pixels(18, 16, p, R), k, 1e-6)[0] == 2
+    assert engine.pixel_grouping(small, pix, k, 1e-6, analyser=1)[0] == 2
+    # the |d|^2 term's change across the octet counts against the budget
+    c0 = engine.octet_bounds(small, pix, k)["cross"]
+    c1 = engine.octet_bounds(small, pix, k, fresnel_rad=1e-3)["cross"]
+    assert c1 == pytest.approx(c0 + 4e-3 * st["extent"], rel=1e-9)
+
+
+def test_octet_launch_clamps():
+    k = 2 * np.pi / 1.2398e-10
+    pix = _flat_pixels(16, 16, 55e-6, 1.0)
+    small = _tiles(2e-9, 6e-8)
+    lv, info = engine.pixel_grouping(small, pix, k, 1e-6)
+    assert lv == 3
+    g = lambda cfg, level=lv: engine.grouping_launch(cfg, level, small, pix, k, info)
+    cfg = g(dict(pix_per_thread=8, threads=128, pairs=3))
+    assert cfg["pairs"] == 3 and cfg["pair_short_radius_m"] == info["quad_short_radius_m"]
+    assert g(dict(pix_per_thread=4, threads=128, pairs=3))["pairs"] == 2
+    assert g(dict(pix_per_thread=8, threads=128, pairs=3), 2)["pairs"] == 2
+    assert engine.default_launch(3) == dict(pix_per_thread=8, threads=128, slices=0, pairs=3)
+    assert engine.analyser_launch(dict(pix_per_thread=8, threads=128, pairs=3))["pairs"] == 2

@@ -66,3 +66,53 @@ def test_quads_are_neighbours():
         assert divmod(c, ny) in ((ra + 1, ca), (ra, ca))
         rd, cd = divmod(d, ny)
         assert (rd - ra, cd - ca) in ((1, 1), (0, 1), (1, 0), (0, 0))
+
+
+def octet_pixels(n_pix, row, nt, pix_blocks):
+    """(loads, stores) of the octet kernels' mapping (mk_split.cuh, PM == 3):
+    thread gi = pb * nt + tid owns rows 2 gz, 2 gz + 1 and columns
+    4 gy .. 4 gy + 3 (pixels 0..3 the left quad a b c d, 4..7 the right one);
+    past the last octet the pixels are n_pix (loads clamp, stores skip)."""
+    rows = n_pix // row
+    gpr = row >> 2
+    n_oct = gpr * (rows >> 1)
+    loads, stores = [], []
+    for pb in range(pix_blocks):
+        for tid in range(nt):
+            gi = pb * nt + tid
+            if gi >= n_oct:
+                loads += [n_pix - 1] * 8
+                continue
+            gz, gy = divmod(gi, gpr)
+            a0 = 2 * gz * row + 4 * gy
+            c0 = a0 + row
+            pix = []
+            for j in range(2):
+                pix += [a0 + 2 * j, a0 + 2 * j + 1, c0 + 2 * j, c0 + 2 * j + 1]
+            loads += pix
+            stores += pix
+    return np.array(loads), np.array(stores)
+
+
+OCTET_SHAPES = [(4, 2), (8, 2), (4, 6), (16, 16), (64, 64), (128, 128), (20, 14), (512, 2), (4, 512)]
+
+
+@pytest.mark.parametrize("nt", [64, 128, 256])
+def test_octets_store_every_pixel_once(nt):
+    for ny, nz in OCTET_SHAPES:
+        n_pix = ny * nz
+        pb = (n_pix + nt * 8 - 1) // (nt * 8)      # mk_scan_plan: whole octets, 8 pixels a thread
+        loads, stores = octet_pixels(n_pix, ny, nt, pb)
+        assert loads.min() >= 0 and loads.max() < n_pix, (ny, nz)
+        assert len(stores) == n_pix and np.array_equal(np.sort(stores), np.arange(n_pix)), (ny, nz)
+
+
+def test_octets_are_two_side_by_side_quads():
+    ny, nz = 20, 6
+    loads, _ = octet_pixels(ny * nz, ny, 64, 1)
+    for o in loads.reshape(-1, 8)[: (ny // 4) * (nz // 2)]:
+        r, c = divmod(int(o[0]), ny)
+        assert r % 2 == 0 and c % 4 == 0
+        want = [(r, c), (r, c + 1), (r + 1, c), (r + 1, c + 1),
+                (r, c + 2), (r, c + 3), (r + 1, c + 2), (r + 1, c + 3)]
+        assert [divmod(int(p), ny) for p in o] == want
