@@ -147,14 +147,21 @@ typedef struct {
                              difference (pi/2) D.(w_a + w_d - w_b - w_c) is dropped: the caller
                              checks the half differences as for pairs and the dropped term
                              against its phase budget (pix_per_thread 4 or 8; an odd last
-                             column or row repeats its pixels inside the quad) */
+                             column or row repeats its pixels inside the quad).
+                             3: 2x4 pixel octets (see octet_radius_m) */
     double pair_short_radius_m; /* with pairs or quads: tiles up to this radius keep the half
                              differences below 0.07 rad and use the short polynomials
                              (0: none does) */
-    double sin_direct_max_rad; /* with quads: tiles without the |d|^2 term whose in-tile phase
-                             bound stays below this [rad] pass the phase to the MUFU sin/cos
-                             without the mod-1 reduction (its error grows ~1e-7 |x|);
-                             0: the library default, 100 rad; < 0: never */
+    double sin_direct_max_rad; /* with quads or octets: tiles without the |d|^2 term whose
+                             in-tile phase bound stays below this [rad] pass the phase to the
+                             MUFU sin/cos without the mod-1 reduction (its error grows
+                             ~1e-7 |x|); 0: the library default, 100 rad; < 0: never */
+    double octet_radius_m; /* with octets (pairs 3: two quads side by side in a 2x4 block share
+                             their half differences, pix_per_thread 8, frames of whole octets):
+                             tiles up to this radius [m] take the octet form, wider ones the
+                             quad form; the caller bounds the octet's dropped phase (the
+                             departure of w from a plane over the 8 pixels, times k r) for
+                             that radius; <= 0: every tile takes the quad form */
 } mk_launch;
 
 /* --- library ---------------------------------------------------------- */
@@ -319,6 +326,22 @@ int mk_prop_pad(const float *field, int ny, int nz, float *padded, int ny2, int 
  * removed; k_axis = k for a forward beam. Phase formed in FP64. */
 int mk_prop_mul(float *spectrum, int ny2, int nz2, double dy, double dz, double k, double z,
                 double k_axis, double k_perp_y, double k_perp_z, void *stream);
+/* The spectral step with the multiply fused into the transform: on the
+ * (nz2, ny2) field already transformed along z (columns, FFT order), each
+ * row is transformed along y in shared memory, multiplied by the same
+ * propagator as mk_prop_mul (formed in FP32 as the reference's
+ * prop_mul_kernel does, Beam.py:4763-4830, with the constant phases
+ * z (k - k_axis) and -z k_axis reduced mod 2 pi in FP64) and transformed
+ * back along y, unnormalised, in place. The caller's inverse column
+ * transform then completes the inverse 2-D transform; the crop applies
+ * 1 / (ny2 nz2). Replaces the row passes of the forward and inverse 2-D
+ * FFTs and prop_mul_kernel's separate pass over the spectrum. ny2 a power
+ * of two in [2, 8192]; workspace of mk_prop_rows_workspace_size bytes
+ * (twiddle and wavenumber tables), 16-byte aligned. */
+size_t mk_prop_rows_workspace_size(int ny2, int nz2);
+int mk_prop_rows(float *spectrum, int ny2, int nz2, double dy, double dz, double k, double z,
+                 double k_axis, double k_perp_y, double k_perp_z, void *workspace, size_t ws_bytes,
+                 void *stream);
 /* Centre crop (nz, ny) at (z0, y0) of the inverse transform times `scale`,
  * fused with |A|^2: writes field (complex64) and/or intensity (float32). */
 int mk_prop_crop_abs2(const float *grid, int ny2, int nz2, int y0, int z0, int ny, int nz,

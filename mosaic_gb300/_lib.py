@@ -147,7 +147,8 @@ class MkLaunch(ctypes.Structure):
     _fields_ = [("pix_per_thread", ctypes.c_int), ("threads", ctypes.c_int),
                 ("slices", ctypes.c_int), ("fresnel", ctypes.c_int), ("amp_real", ctypes.c_int),
                 ("fresnel_radius_m", ctypes.c_double), ("pairs", ctypes.c_int),
-                ("pair_short_radius_m", ctypes.c_double), ("sin_direct_max_rad", ctypes.c_double)]
+                ("pair_short_radius_m", ctypes.c_double), ("sin_direct_max_rad", ctypes.c_double),
+                ("octet_radius_m", ctypes.c_double)]
 
 
 # name -> (restype, argtypes)
@@ -202,6 +203,10 @@ SIGNATURES = {
     "mk_prop_mul": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, _vp]),
+    "mk_prop_rows": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, _vp, ctypes.c_size_t, _vp]),
+    "mk_prop_rows_workspace_size": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "mk_prop_crop_abs2": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_float, _vp, _vp, _vp]),
     "mk_split_plan": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkPixels),

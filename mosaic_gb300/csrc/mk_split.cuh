@@ -58,6 +58,7 @@ struct MkSplitArgs {
     float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
     float pair_short_r; // pair/quad kernels: tiles up to this radius [m] use the short polynomials
     float sin_direct;   // quad kernels: in-tile phase bound [rad] below which the reduction is skipped
+    float oct_r;        // octet kernels: tiles up to this radius [m] take the octet form, the rest quads
     // analyser (ANA kernels, single exposures): kind 1 top-hat / 2 Darwin,
     // beam direction and analyser axis in FP64, 4 sin^2(alpha/2), half-width
     int analyser;
@@ -602,6 +603,194 @@ constexpr int mk_min_blocks()
                                                                        : 1;
 }
 
+// The 2x2 pixel-quad form for one tile: NQ quads of the thread (pixels
+// 4j..4j+3 = a, b, c, d), each with its own mean, half differences and
+// sin/cos; the quad kernels run it on every tile and the octet kernels on
+// tiles too wide for the octet form.
+template <int NQ, bool CPLX>
+__device__ __forceinline__ void mk_quads_tile(const MkSplitArgs &A, const mk_frame_desc &F,
+                                              const double4 &o, bool fr_tile,
+                                              const float4 *__restrict__ P,
+                                              const float4 *__restrict__ E, int T,
+                                              const float (&wx)[4 * NQ], const float (&wy)[4 * NQ],
+                                              const float (&wz)[4 * NQ], const float (&hq)[4 * NQ],
+                                              float (&csr)[4 * NQ], float (&csi)[4 * NQ])
+{
+    mk_f2 sx[NQ], sy[NQ], sz[NQ], ux[NQ], uy[NQ], uz[NQ], vx[NQ], vy[NQ], vz[NQ],
+        hp[NQ];
+    mk_f2 acc[NQ][8];
+#pragma unroll
+    for (int j = 0; j < NQ; ++j) {
+        const int a = 4 * j, b = a + 1, c = a + 2, d = a + 3;
+        const float hpi = 1.57079632679490f;
+        sx[j] = f2_splat(0.25f * ((wx[a] + wx[b]) + (wx[c] + wx[d])));
+        sy[j] = f2_splat(0.25f * ((wy[a] + wy[b]) + (wy[c] + wy[d])));
+        sz[j] = f2_splat(0.25f * ((wz[a] + wz[b]) + (wz[c] + wz[d])));
+        ux[j] = f2_splat(hpi * ((wx[b] - wx[a]) + (wx[d] - wx[c])));
+        uy[j] = f2_splat(hpi * ((wy[b] - wy[a]) + (wy[d] - wy[c])));
+        uz[j] = f2_splat(hpi * ((wz[b] - wz[a]) + (wz[d] - wz[c])));
+        vx[j] = f2_splat(hpi * ((wx[c] - wx[a]) + (wx[d] - wx[b])));
+        vy[j] = f2_splat(hpi * ((wy[c] - wy[a]) + (wy[d] - wy[b])));
+        vz[j] = f2_splat(hpi * ((wz[c] - wz[a]) + (wz[d] - wz[b])));
+        hp[j] = f2_splat(0.25f * ((hq[a] + hq[b]) + (hq[c] + hq[d])));
+#pragma unroll
+        for (int m = 0; m < 8; ++m) acc[j][m] = 0ull;
+    }
+    const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
+    const bool short_tile = (float)o.w <= A.pair_short_r;
+    // direct sin/cos argument: warp-uniform, from the bound
+    // 2 pi |w_mean| kappa r of every quad of the warp
+    bool rad = false;
+    if (!fr_tile && short_tile) {
+        float wmax = 0.f;
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) {
+            const float2 a = f2_unpack(sx[j]), b = f2_unpack(sy[j]), c = f2_unpack(sz[j]);
+            wmax = fmaxf(wmax, fmaf(c.x, c.x, fmaf(b.x, b.x, a.x * a.x)));
+        }
+        const float bound = TWO_PI_F * sqrtf(wmax) * A.kappa * (float)o.w;
+        rad = __all_sync(0xffffffffu, bound <= A.sin_direct);
+    }
+    if (rad) {
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) {
+            sx[j] = f2_mul(sx[j], f2_splat(TWO_PI_F));
+            sy[j] = f2_mul(sy[j], f2_splat(TWO_PI_F));
+            sz[j] = f2_mul(sz[j], f2_splat(TWO_PI_F));
+        }
+        mk_tile_terms_quad<NQ, false, CPLX, true, true>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                        vx, vy, vz, hp, bx, by, bz, acc);
+    } else if (fr_tile) {
+        if (short_tile)
+            mk_tile_terms_quad<NQ, true, CPLX, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx,
+                                                     vy, vz, hp, bx, by, bz, acc);
+        else
+            mk_tile_terms_quad<NQ, true, CPLX, false>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                      vx, vy, vz, hp, bx, by, bz, acc);
+    } else {
+        if (short_tile)
+            mk_tile_terms_quad<NQ, false, CPLX, true>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                      vx, vy, vz, hp, bx, by, bz, acc);
+        else
+            mk_tile_terms_quad<NQ, false, CPLX, false>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                       vx, vy, vz, hp, bx, by, bz, acc);
+    }
+#pragma unroll
+    for (int j = 0; j < NQ; ++j) {
+        float h[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const float2 t2 = f2_unpack(acc[j][m]);   // halves: even, odd atoms
+            h[m] = t2.x + t2.y;
+        }
+        const float Kr = h[0], Ki = h[1], Rr = h[2], Ri = h[3];
+        const float Sr = h[4], Si = h[5], Qr = h[6], Qi = h[7];
+        // A(s, t) = K - s t Q + i t R + i s S
+        csr[4 * j] = (Kr - Qr) + (Ri + Si);       // a (-, -)
+        csi[4 * j] = (Ki - Qi) - (Rr + Sr);
+        csr[4 * j + 1] = (Kr + Qr) + (Ri - Si);   // b (+, -)
+        csi[4 * j + 1] = (Ki + Qi) - (Rr - Sr);
+        csr[4 * j + 2] = (Kr + Qr) - (Ri - Si);   // c (-, +)
+        csi[4 * j + 2] = (Ki + Qi) + (Rr - Sr);
+        csr[4 * j + 3] = (Kr - Qr) - (Ri + Si);   // d (+, +)
+        csi[4 * j + 3] = (Ki - Qi) + (Rr + Sr);
+    }
+}
+
+// The 2x4 pixel-octet form for one tile (pixels 0..3 and 4..7 are the
+// thread's two quads a, b, c, d, side by side).
+template <bool CPLX>
+__device__ __forceinline__ void mk_octet_tile(const MkSplitArgs &A, const mk_frame_desc &F,
+                                              const double4 &o, bool fr_tile,
+                                              const float4 *__restrict__ P,
+                                              const float4 *__restrict__ E, int T,
+                                              const float (&wx)[8], const float (&wy)[8],
+                                              const float (&wz)[8], const float (&hq)[8],
+                                              float (&csr)[8], float (&csi)[8])
+{
+    // octet vectors: mean w of the 8 pixels, and the two quads'
+    // mean half-difference vectors (pixels 0..3 and 4..7 are
+    // quads a b c d)
+    const float hpi4 = 0.785398163397448f;   // (pi/2) / 2 quads
+    float msx = 0.f, msy = 0.f, msz = 0.f, mh = 0.f;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        msx += wx[p]; msy += wy[p]; msz += wz[p]; mh += hq[p];
+    }
+    const float ax = hpi4 * (((wx[1] - wx[0]) + (wx[3] - wx[2])) + ((wx[5] - wx[4]) + (wx[7] - wx[6])));
+    const float ay = hpi4 * (((wy[1] - wy[0]) + (wy[3] - wy[2])) + ((wy[5] - wy[4]) + (wy[7] - wy[6])));
+    const float az = hpi4 * (((wz[1] - wz[0]) + (wz[3] - wz[2])) + ((wz[5] - wz[4]) + (wz[7] - wz[6])));
+    const float cx = hpi4 * (((wx[2] - wx[0]) + (wx[3] - wx[1])) + ((wx[6] - wx[4]) + (wx[7] - wx[5])));
+    const float cy = hpi4 * (((wy[2] - wy[0]) + (wy[3] - wy[1])) + ((wy[6] - wy[4]) + (wy[7] - wy[5])));
+    const float cz = hpi4 * (((wz[2] - wz[0]) + (wz[3] - wz[1])) + ((wz[6] - wz[4]) + (wz[7] - wz[5])));
+    msx *= 0.125f; msy *= 0.125f; msz *= 0.125f; mh *= 0.125f;
+    mk_f2 acc[2][8];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int m = 0; m < 8; ++m) acc[j][m] = 0ull;
+    const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
+    const bool short_tile = (float)o.w <= A.pair_short_r;
+    // direct sin/cos argument (warp-uniform): the quad phases
+    // reach kappa r (2 pi |s| + 2 |u|)
+    bool rad = false;
+    if (!fr_tile && short_tile) {
+        const float bound = (TWO_PI_F * sqrtf(fmaf(msz, msz, fmaf(msy, msy, msx * msx))) +
+                             2.f * sqrtf(fmaf(az, az, fmaf(ay, ay, ax * ax)))) *
+                            A.kappa * (float)o.w;
+        rad = __all_sync(0xffffffffu, bound <= A.sin_direct);
+    }
+    const mk_f2 ux = f2_splat(ax), uy = f2_splat(ay), uz = f2_splat(az);
+    const mk_f2 vx = f2_splat(cx), vy = f2_splat(cy), vz = f2_splat(cz);
+    const mk_f2 hp = f2_splat(mh);
+    if (rad) {
+        const mk_f2 sx = f2_splat(msx * TWO_PI_F), sy = f2_splat(msy * TWO_PI_F),
+                    sz = f2_splat(msz * TWO_PI_F);
+        mk_tile_terms_oct<false, CPLX, true, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx, vy,
+                                                   vz, hp, bx, by, bz, acc);
+    } else {
+        const mk_f2 sx = f2_splat(msx), sy = f2_splat(msy), sz = f2_splat(msz);
+        if (fr_tile) {
+            if (short_tile)
+                mk_tile_terms_oct<true, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                           vx, vy, vz, hp, bx, by, bz, acc);
+            else
+                mk_tile_terms_oct<true, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy,
+                                                            uz, vx, vy, vz, hp, bx, by, bz,
+                                                            acc);
+        } else {
+            if (short_tile)
+                mk_tile_terms_oct<false, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy,
+                                                            uz, vx, vy, vz, hp, bx, by, bz,
+                                                            acc);
+            else
+                mk_tile_terms_oct<false, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy,
+                                                             uz, vx, vy, vz, hp, bx, by,
+                                                             bz, acc);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        float h[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const float2 t2 = f2_unpack(acc[j][m]);   // halves: even, odd atoms
+            h[m] = t2.x + t2.y;
+        }
+        const float Kr = h[0], Ki = h[1], Rr = h[2], Ri = h[3];
+        const float Sr = h[4], Si = h[5], Qr = h[6], Qi = h[7];
+        // A(s, t) = K - s t Q + i t R + i s S
+        csr[4 * j] = (Kr - Qr) + (Ri + Si);       // a (-, -)
+        csi[4 * j] = (Ki - Qi) - (Rr + Sr);
+        csr[4 * j + 1] = (Kr + Qr) + (Ri - Si);   // b (+, -)
+        csi[4 * j + 1] = (Ki + Qi) - (Rr - Sr);
+        csr[4 * j + 2] = (Kr + Qr) - (Ri - Si);   // c (-, +)
+        csi[4 * j + 2] = (Ki + Qi) + (Rr - Sr);
+        csr[4 * j + 3] = (Kr - Qr) - (Ri + Si);   // d (+, +)
+        csi[4 * j + 3] = (Ki - Qi) + (Rr + Sr);
+    }
+}
+
 template <int NT, int PIX, bool FRESNEL, bool CPLX, int PM, bool ANA>
 __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
     mk_split_kernel(const __grid_constant__ MkSplitArgs A)
@@ -838,168 +1027,14 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                     mk_tile_terms_ana<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
                                                         agx, agy, agz, ath, ag0, ag1, csr, csi);
             } else if constexpr (PM == 3) {
-                // octet vectors: mean w of the 8 pixels, and the two quads'
-                // mean half-difference vectors (pixels 0..3 and 4..7 are
-                // quads a b c d)
-                const float hpi4 = 0.785398163397448f;   // (pi/2) / 2 quads
-                float msx = 0.f, msy = 0.f, msz = 0.f, mh = 0.f;
-#pragma unroll
-                for (int p = 0; p < 8; ++p) {
-                    msx += wx[p]; msy += wy[p]; msz += wz[p]; mh += hq[p];
-                }
-                const float ax = hpi4 * (((wx[1] - wx[0]) + (wx[3] - wx[2])) + ((wx[5] - wx[4]) + (wx[7] - wx[6])));
-                const float ay = hpi4 * (((wy[1] - wy[0]) + (wy[3] - wy[2])) + ((wy[5] - wy[4]) + (wy[7] - wy[6])));
-                const float az = hpi4 * (((wz[1] - wz[0]) + (wz[3] - wz[2])) + ((wz[5] - wz[4]) + (wz[7] - wz[6])));
-                const float cx = hpi4 * (((wx[2] - wx[0]) + (wx[3] - wx[1])) + ((wx[6] - wx[4]) + (wx[7] - wx[5])));
-                const float cy = hpi4 * (((wy[2] - wy[0]) + (wy[3] - wy[1])) + ((wy[6] - wy[4]) + (wy[7] - wy[5])));
-                const float cz = hpi4 * (((wz[2] - wz[0]) + (wz[3] - wz[1])) + ((wz[6] - wz[4]) + (wz[7] - wz[5])));
-                msx *= 0.125f; msy *= 0.125f; msz *= 0.125f; mh *= 0.125f;
-                mk_f2 acc[2][8];
-#pragma unroll
-                for (int j = 0; j < 2; ++j)
-#pragma unroll
-                    for (int m = 0; m < 8; ++m) acc[j][m] = 0ull;
-                const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
-                const bool short_tile = (float)o.w <= A.pair_short_r;
-                // direct sin/cos argument (warp-uniform): the quad phases
-                // reach kappa r (2 pi |s| + 2 |u|)
-                bool rad = false;
-                if (!fr_tile && short_tile) {
-                    const float bound = (TWO_PI_F * sqrtf(fmaf(msz, msz, fmaf(msy, msy, msx * msx))) +
-                                         2.f * sqrtf(fmaf(az, az, fmaf(ay, ay, ax * ax)))) *
-                                        A.kappa * (float)o.w;
-                    rad = __all_sync(0xffffffffu, bound <= A.sin_direct);
-                }
-                const mk_f2 ux = f2_splat(ax), uy = f2_splat(ay), uz = f2_splat(az);
-                const mk_f2 vx = f2_splat(cx), vy = f2_splat(cy), vz = f2_splat(cz);
-                const mk_f2 hp = f2_splat(mh);
-                if (rad) {
-                    const mk_f2 sx = f2_splat(msx * TWO_PI_F), sy = f2_splat(msy * TWO_PI_F),
-                                sz = f2_splat(msz * TWO_PI_F);
-                    mk_tile_terms_oct<false, CPLX, true, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx, vy,
-                                                               vz, hp, bx, by, bz, acc);
-                } else {
-                    const mk_f2 sx = f2_splat(msx), sy = f2_splat(msy), sz = f2_splat(msz);
-                    if (fr_tile) {
-                        if (short_tile)
-                            mk_tile_terms_oct<true, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy, uz,
-                                                                       vx, vy, vz, hp, bx, by, bz, acc);
-                        else
-                            mk_tile_terms_oct<true, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy,
-                                                                        uz, vx, vy, vz, hp, bx, by, bz,
-                                                                        acc);
-                    } else {
-                        if (short_tile)
-                            mk_tile_terms_oct<false, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy,
-                                                                        uz, vx, vy, vz, hp, bx, by, bz,
-                                                                        acc);
-                        else
-                            mk_tile_terms_oct<false, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy,
-                                                                         uz, vx, vy, vz, hp, bx, by,
-                                                                         bz, acc);
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    float h[8];
-#pragma unroll
-                    for (int m = 0; m < 8; ++m) {
-                        const float2 t2 = f2_unpack(acc[j][m]);   // halves: even, odd atoms
-                        h[m] = t2.x + t2.y;
-                    }
-                    const float Kr = h[0], Ki = h[1], Rr = h[2], Ri = h[3];
-                    const float Sr = h[4], Si = h[5], Qr = h[6], Qi = h[7];
-                    // A(s, t) = K - s t Q + i t R + i s S
-                    csr[4 * j] = (Kr - Qr) + (Ri + Si);       // a (-, -)
-                    csi[4 * j] = (Ki - Qi) - (Rr + Sr);
-                    csr[4 * j + 1] = (Kr + Qr) + (Ri - Si);   // b (+, -)
-                    csi[4 * j + 1] = (Ki + Qi) - (Rr - Sr);
-                    csr[4 * j + 2] = (Kr + Qr) - (Ri - Si);   // c (-, +)
-                    csi[4 * j + 2] = (Ki + Qi) + (Rr - Sr);
-                    csr[4 * j + 3] = (Kr - Qr) - (Ri + Si);   // d (+, +)
-                    csi[4 * j + 3] = (Ki - Qi) + (Rr + Sr);
-                }
+                // tiles wider than the octet form's radius (the host bounds its
+                // dropped phase per radius): the thread's two quads on their own
+                if ((float)o.w > A.oct_r)
+                    mk_quads_tile<2, CPLX>(A, F, o, fr_tile, P, E, T, wx, wy, wz, hq, csr, csi);
+                else
+                    mk_octet_tile<CPLX>(A, F, o, fr_tile, P, E, T, wx, wy, wz, hq, csr, csi);
             } else if constexpr (PM == 2) {
-                constexpr int NQ = PIX / 4;
-                mk_f2 sx[NQ], sy[NQ], sz[NQ], ux[NQ], uy[NQ], uz[NQ], vx[NQ], vy[NQ], vz[NQ],
-                    hp[NQ];
-                mk_f2 acc[NQ][8];
-#pragma unroll
-                for (int j = 0; j < NQ; ++j) {
-                    const int a = 4 * j, b = a + 1, c = a + 2, d = a + 3;
-                    const float hpi = 1.57079632679490f;
-                    sx[j] = f2_splat(0.25f * ((wx[a] + wx[b]) + (wx[c] + wx[d])));
-                    sy[j] = f2_splat(0.25f * ((wy[a] + wy[b]) + (wy[c] + wy[d])));
-                    sz[j] = f2_splat(0.25f * ((wz[a] + wz[b]) + (wz[c] + wz[d])));
-                    ux[j] = f2_splat(hpi * ((wx[b] - wx[a]) + (wx[d] - wx[c])));
-                    uy[j] = f2_splat(hpi * ((wy[b] - wy[a]) + (wy[d] - wy[c])));
-                    uz[j] = f2_splat(hpi * ((wz[b] - wz[a]) + (wz[d] - wz[c])));
-                    vx[j] = f2_splat(hpi * ((wx[c] - wx[a]) + (wx[d] - wx[b])));
-                    vy[j] = f2_splat(hpi * ((wy[c] - wy[a]) + (wy[d] - wy[b])));
-                    vz[j] = f2_splat(hpi * ((wz[c] - wz[a]) + (wz[d] - wz[b])));
-                    hp[j] = f2_splat(0.25f * ((hq[a] + hq[b]) + (hq[c] + hq[d])));
-#pragma unroll
-                    for (int m = 0; m < 8; ++m) acc[j][m] = 0ull;
-                }
-                const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
-                const bool short_tile = (float)o.w <= A.pair_short_r;
-                // direct sin/cos argument: warp-uniform, from the bound
-                // 2 pi |w_mean| kappa r of every quad of the warp
-                bool rad = false;
-                if (!fr_tile && short_tile) {
-                    float wmax = 0.f;
-#pragma unroll
-                    for (int j = 0; j < NQ; ++j) {
-                        const float2 a = f2_unpack(sx[j]), b = f2_unpack(sy[j]), c = f2_unpack(sz[j]);
-                        wmax = fmaxf(wmax, fmaf(c.x, c.x, fmaf(b.x, b.x, a.x * a.x)));
-                    }
-                    const float bound = TWO_PI_F * sqrtf(wmax) * A.kappa * (float)o.w;
-                    rad = __all_sync(0xffffffffu, bound <= A.sin_direct);
-                }
-                if (rad) {
-#pragma unroll
-                    for (int j = 0; j < NQ; ++j) {
-                        sx[j] = f2_mul(sx[j], f2_splat(TWO_PI_F));
-                        sy[j] = f2_mul(sy[j], f2_splat(TWO_PI_F));
-                        sz[j] = f2_mul(sz[j], f2_splat(TWO_PI_F));
-                    }
-                    mk_tile_terms_quad<NQ, false, CPLX, true, true>(P, E, T, sx, sy, sz, ux, uy, uz,
-                                                                    vx, vy, vz, hp, bx, by, bz, acc);
-                } else if (fr_tile) {
-                    if (short_tile)
-                        mk_tile_terms_quad<NQ, true, CPLX, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx,
-                                                                 vy, vz, hp, bx, by, bz, acc);
-                    else
-                        mk_tile_terms_quad<NQ, true, CPLX, false>(P, E, T, sx, sy, sz, ux, uy, uz,
-                                                                  vx, vy, vz, hp, bx, by, bz, acc);
-                } else {
-                    if (short_tile)
-                        mk_tile_terms_quad<NQ, false, CPLX, true>(P, E, T, sx, sy, sz, ux, uy, uz,
-                                                                  vx, vy, vz, hp, bx, by, bz, acc);
-                    else
-                        mk_tile_terms_quad<NQ, false, CPLX, false>(P, E, T, sx, sy, sz, ux, uy, uz,
-                                                                   vx, vy, vz, hp, bx, by, bz, acc);
-                }
-#pragma unroll
-                for (int j = 0; j < NQ; ++j) {
-                    float h[8];
-#pragma unroll
-                    for (int m = 0; m < 8; ++m) {
-                        const float2 t2 = f2_unpack(acc[j][m]);   // halves: even, odd atoms
-                        h[m] = t2.x + t2.y;
-                    }
-                    const float Kr = h[0], Ki = h[1], Rr = h[2], Ri = h[3];
-                    const float Sr = h[4], Si = h[5], Qr = h[6], Qi = h[7];
-                    // A(s, t) = K - s t Q + i t R + i s S
-                    csr[4 * j] = (Kr - Qr) + (Ri + Si);       // a (-, -)
-                    csi[4 * j] = (Ki - Qi) - (Rr + Sr);
-                    csr[4 * j + 1] = (Kr + Qr) + (Ri - Si);   // b (+, -)
-                    csi[4 * j + 1] = (Ki + Qi) - (Rr - Sr);
-                    csr[4 * j + 2] = (Kr + Qr) - (Ri - Si);   // c (-, +)
-                    csi[4 * j + 2] = (Ki + Qi) + (Rr - Sr);
-                    csr[4 * j + 3] = (Kr - Qr) - (Ri + Si);   // d (+, +)
-                    csi[4 * j + 3] = (Ki - Qi) + (Rr + Sr);
-                }
+                mk_quads_tile<PIX / 4, CPLX>(A, F, o, fr_tile, P, E, T, wx, wy, wz, hq, csr, csi);
             } else if constexpr (PM == 1) {
                 constexpr int NP = PIX / 2;
                 mk_f2 sx[NP], sy[NP], sz[NP], dx[NP], dy[NP], dz[NP], hp[NP];

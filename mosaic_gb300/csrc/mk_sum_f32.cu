@@ -355,6 +355,7 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
     A.pdeg = (float)phys->pol_deg;
     A.fres_r = launch->fresnel_radius_m > 0.0 ? (float)launch->fresnel_radius_m : 0.f;
     A.pair_short_r = launch->pair_short_radius_m > 0.0 ? (float)launch->pair_short_radius_m : -1.f;
+    A.oct_r = launch->octet_radius_m > 0.0 ? (float)launch->octet_radius_m : -1.f;
     A.sin_direct = launch->sin_direct_max_rad == 0.0 ? MK_SIN_DIRECT_MAX
                    : launch->sin_direct_max_rad < 0.0 ? -1.f : (float)launch->sin_direct_max_rad;
     if (ana) {

@@ -507,29 +507,45 @@ def quad_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
                 cross=cross, **st)
 
 
-def octet_bounds(tiles, pix: Pixels, k, fresnel_rad=0.0):
-    """Error bound [rad] of the 2x4 pixel-octet form over all tiles, or None
-    when a frame is not whole octets.
+OCTET_MIN_TILE_FRACTION = 0.5   # octets only where at least half the tiles take them
+
+
+def octet_bounds(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0):
+    """Largest tile radius [m] whose 2x4 pixel-octet form stays within the
+    phase budget, or None when a frame is not whole octets.
 
     The octet drops, beyond the quad form, the departure of w over its 8
     pixels from a plane (mean, mean row step, mean column step): the kernel
     takes both quads' half differences from the octet's mean steps and their
     phases from the octet's mean phase. That residual of the FP64 pixel
     directions (``Pixels.octet_steps``), widened for the tile-origin term of
-    w, times k |D| <= k r bounds the phase error; the |d|^2 term, which the
-    octet evaluates once at its centre, adds 4 ``fresnel_rad`` x the octet's
-    extent |u - mean|."""
+    w, times k |D| <= k r bounds the phase error of a tile of radius r; the
+    |d|^2 term, which the octet evaluates once at its centre, adds
+    4 ``fresnel_rad`` x the octet's extent |u - mean|. Tiles wider than the
+    returned radius take the quad form inside the octet kernel. Returns
+    dict(radius_m, cross (the bound at min(radius, widest tile)), plane,
+    extent, step)."""
     st = pix.octet_steps()
     if st is None:
         return None
-    if not tiles.n_tiles:
-        return dict(cross=0.0, **st)
     r0 = max(pix.r0_min(), 1e-300)
-    o_ratio = tiles.max_origin_norm() / r0
+    o_ratio = tiles.max_origin_norm() / r0 if tiles.n_tiles else 0.0
     grow = 1.0 + 2.0 * o_ratio
     plane = st["plane"] * grow + 12.0 * o_ratio * st["step"] ** 2
-    cross = float(k) * tiles.max_radius() * plane * 1.05 + 4.0 * float(fresnel_rad) * st["extent"]
-    return dict(cross=cross, **st)
+    rate = float(k) * plane * 1.05                      # rad per metre of tile radius
+    fixed = 4.0 * float(fresnel_rad) * st["extent"]
+    room = float(budget_rad) - fixed
+    radius = room / rate if (room > 0.0 and rate > 0.0) else (1.0 if room > 0.0 else 0.0)
+    r_eff = min(radius, tiles.max_radius()) if tiles.n_tiles else 0.0
+    return dict(radius_m=radius, cross=rate * r_eff + fixed, **st)
+
+
+def tile_fraction_within(tiles, radius_m):
+    """Fraction of the tiles whose radius is at most ``radius_m``."""
+    if not tiles.n_tiles:
+        return 1.0
+    r = tiles.origin[: tiles.n_tiles, 3]
+    return float((r <= float(radius_m)).double().mean())
 
 
 def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=False):
@@ -540,7 +556,9 @@ def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=
     breaks it); quads need their half differences within it and their
     dropped phase within ``budget_rad``, on any detector shape; octets (2x4:
     two quads sharing their half differences) need frames of whole octets
-    and their dropped phase within the budget as well. ``analyser`` (0 off,
+    and at least OCTET_MIN_TILE_FRACTION of the tiles narrow enough for
+    their dropped phase to fit the budget (``octet_bounds``; the wider tiles
+    take the quad form). ``analyser`` (0 off,
     1 top-hat, 2 Darwin): the analyser kernels have quads for the top-hat
     (tiles the acceptance edge cuts take the per-atom loop) and no pairs or
     octets; a Darwin analyser expands per atom on every tile, so it shares
@@ -555,10 +573,12 @@ def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=
                 quad_short_radius_m=q["short_radius_m"])
     if q["delta"] <= PAIR_DELTA_MAX and q["cross"] <= budget_rad:
         if not analyser:
-            ob = octet_bounds(tiles, pix, k, fresnel_rad)
-            if ob is not None:
-                info["octet_cross_rad"] = ob["cross"]
-                if ob["cross"] <= budget_rad:
+            ob = octet_bounds(tiles, pix, k, budget_rad, fresnel_rad)
+            if ob is not None and ob["radius_m"] > 0.0:
+                frac = tile_fraction_within(tiles, ob["radius_m"])
+                info.update(octet_cross_rad=ob["cross"], octet_radius_m=ob["radius_m"],
+                            octet_tile_fraction=frac)
+                if frac >= OCTET_MIN_TILE_FRACTION:
                     return 3, info
         return 2, info
     return (1 if info["pairs_ok"] else 0), info
@@ -595,6 +615,7 @@ def grouping_launch(cfg, level, tiles, pix, k, info):
     if mode == 1 and (ppt % 2 or not pairs_ok):
         mode = 0
     cfg["pairs"] = mode
+    cfg["octet_radius_m"] = float(info.get("octet_radius_m", 0.0)) if mode == 3 else 0.0
     if mode >= 2:
         cfg["pair_short_radius_m"] = info["quad_short_radius_m"]
     elif mode == 1:
@@ -624,7 +645,8 @@ def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None,
     ln = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]), int(fresnel),
                   int(tiles.amp_is_real() if amp_real is None else bool(amp_real)),
                   float(fresnel_radius), int(pairs), short_r,
-                  float(cfg.get("sin_direct_max_rad", 0.0) or 0.0))
+                  float(cfg.get("sin_direct_max_rad", 0.0) or 0.0),
+                  float(cfg.get("octet_radius_m", 0.0) or 0.0))
     wsb = ctypes.c_size_t(0)
     check(L.mk_split_plan(ctypes.byref(tiles.abi), ctypes.byref(pix.abi), ctypes.byref(ln),
                           ctypes.byref(wsb)))

@@ -5,9 +5,14 @@ Follows the reference's ``_angular_spectrum_propagate_gpu`` and
 to a power-of-two grid sized for the distance, transformed, multiplied by the
 exact free-space transfer function with the carrier removed, transformed
 back and centre-cropped; distances the padded grid cannot sample without
-aliasing are split into equal alias-free steps. Here the pad, the multiply
-and the crop (fused with |A|^2) are libmosaic_kin kernels; the FFTs are
-cuFFT through torch.fft.
+aliasing are split into equal alias-free steps. Here the 2-D transform is
+split by dimension: the column (z) transforms are cuFFT through torch.fft,
+and one libmosaic_kin kernel (``mk_prop_rows``) does the row transform, the
+transfer-function multiply and the inverse row transform per row in shared
+memory, so the spectrum makes one round trip through HBM between the column
+transforms instead of three. The pad and the crop (fused with |A|^2) are
+libmosaic_kin kernels too. ``fused=False`` runs the unfused sequence
+(cuFFT 2-D transforms around ``mk_prop_mul``, FP64 phase) instead.
 
 ``FreeSpaceStack`` is a minimal optics stack with the reference's
 ``apply_stack`` interface holding free-space segments only (the reference's
@@ -75,7 +80,7 @@ def _as_device_c64(field, device):
 
 def propagate(field, dy, dz, z, wavelength, step_max=None, pad_factor=1.0, padding_mode="edge",
               pad_constant=0.0, k_axis=None, k_perp_y=0.0, k_perp_z=0.0, intensity=False,
-              device="cuda"):
+              device="cuda", fused=True):
     """Propagate a (Nz, Ny) field over z [m]. Returns the complex64 field on
     the device, or (field, |field|^2) with ``intensity``."""
     L = engine._require_cuda()
@@ -100,10 +105,18 @@ def propagate(field, dy, dz, z, wavelength, step_max=None, pad_factor=1.0, paddi
         c = complex(pad_constant)
         check(L.mk_prop_pad(E.data_ptr(), Ny, Nz, P.data_ptr(), Ny2, Nz2, y0, z0, mode,
                             c.real, c.imag, sh))
-        F = torch.fft.fft2(P)
-        check(L.mk_prop_mul(F.data_ptr(), Ny2, Nz2, float(dy), float(dz), k, dz_step, kga,
-                            float(k_perp_y), float(k_perp_z), sh))
-        G = torch.fft.ifft2(F, norm="forward")        # unnormalised; 1/N in the crop
+        if fused:
+            F = torch.fft.fft(P, dim=0)                # columns (z)
+            ws_n = int(L.mk_prop_rows_workspace_size(Ny2, Nz2))
+            ws = torch.empty(ws_n, dtype=torch.uint8, device=E.device)
+            check(L.mk_prop_rows(F.data_ptr(), Ny2, Nz2, float(dy), float(dz), k, dz_step, kga,
+                                 float(k_perp_y), float(k_perp_z), ws.data_ptr(), ws_n, sh))
+            G = torch.fft.ifft(F, dim=0, norm="forward")   # unnormalised; 1/N in the crop
+        else:
+            F = torch.fft.fft2(P)
+            check(L.mk_prop_mul(F.data_ptr(), Ny2, Nz2, float(dy), float(dz), k, dz_step, kga,
+                                float(k_perp_y), float(k_perp_z), sh))
+            G = torch.fft.ifft2(F, norm="forward")        # unnormalised; 1/N in the crop
         out = torch.empty((Nz, Ny), dtype=torch.complex64, device=E.device)
         if intensity and last:
             I = torch.empty((Nz, Ny), dtype=torch.float32, device=E.device)

@@ -199,7 +199,8 @@ class BatchedScan:
         self.launch = MkLaunch(int(cfg["pix_per_thread"]), int(cfg["threads"]), int(cfg["slices"]),
                                int(su.fresnel), int(tiles.amp_is_real()), float(su.fresnel_radius),
                                int(cfg["pairs"]), float(cfg["pair_short_radius_m"]),
-                               float(cfg.get("sin_direct_max_rad", 0.0) or 0.0))
+                               float(cfg.get("sin_direct_max_rad", 0.0) or 0.0),
+                               float(cfg.get("octet_radius_m", 0.0) or 0.0))
         nf = len(self.frames)
         desc = (MkFrameDesc * nf)()
         n_items, n_part = ctypes.c_longlong(0), ctypes.c_longlong(0)

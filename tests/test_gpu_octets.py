@@ -31,7 +31,7 @@ def _cu_ni_case():
     return w, pos, spc
 
 
-def _det(shape, pitch, theta_deg, dist=2.0e9):
+def _det(shape, pitch, theta_deg, dist=1.0e10):
     D = Detector()
     D.create_detector(shape, (pitch, pitch))
     D.position_detector_absolute(dist, 2.0 * theta_deg, 0.0)
@@ -49,9 +49,11 @@ def _oracle(B, pos, spc, D, stage):
 @pytest.mark.parametrize("shape,threads,complex_beam", [((24, 20), 128, False), ((16, 16), 64, True),
                                                          ((32, 6), 256, False), ((4, 2), 128, False)])
 def test_octets_match_oracle_and_other_forms(cuda, shape, threads, complex_beam):
-    """A Cu/Ni crystal at its (111) reflection, 0.2 m, through the entry
+    """A Cu/Ni crystal at its (111) reflection, 1 m, through the entry
     point: octets on detectors of whole octets (the smallest one a single
-    octet), with a complex incident wavefield too."""
+    octet), with a complex incident wavefield too. (At 0.2 m the octet's
+    dropped phase exceeds the 1e-6 rad budget for tiles of this size and the
+    host keeps quads.)"""
     w, pos, spc = _cu_ni_case()
     sample = ChunkedSample([(pos, spc)])
     B = workloads._beam(10000.0, 200.0, pol_perp_rate=1.0)
@@ -70,6 +72,7 @@ def test_octets_match_oracle_and_other_forms(cuda, shape, threads, complex_beam)
         assert B.last_run["launch"]["pairs"] == cfg["pairs"], (name, B.last_run)
         if name == "oct":
             assert B.last_run["octet_cross_rad"] <= 1e-6, B.last_run
+            assert B.last_run["octet_tile_fraction"] == 1.0, B.last_run
     ref = _oracle(B, pos, spc, D, stage)
     assert rel_intensity(out["oct"], ref) <= 1e-4, rel_intensity(out["oct"], ref)
     assert rel_max(out["oct"], ref) <= 1e-4, rel_max(out["oct"], ref)
@@ -94,7 +97,8 @@ def test_octets_direct_sincos_argument(cuda):
     short_r = info["quad_short_radius_m"]
 
     def run(lim):
-        cfg = dict(OCT, sin_direct_max_rad=lim, pair_short_radius_m=short_r)
+        cfg = dict(OCT, sin_direct_max_rad=lim, pair_short_radius_m=short_r,
+                   octet_radius_m=info["octet_radius_m"])
         o = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg, fresnel=0)
         engine.sync()
         return o.cpu().numpy()
@@ -106,6 +110,43 @@ def test_octets_direct_sincos_argument(cuda):
         assert rel_intensity(c(got), ref) <= 1e-4, rel_intensity(c(got), ref)
     assert rel_max(always, never) <= 2e-5, rel_max(always, never)
     assert rel_max(default, never) <= 2e-5, rel_max(default, never)
+
+
+def test_octets_with_wide_tiles_taking_quads(cuda):
+    """The octet kernel switches to the quad form per tile: with the octet
+    radius at the median tile radius half the tiles take each form, and the
+    result equals both the all-octet and the all-quad runs (within the
+    forms' budget) and the oracle."""
+    w, pos, spc = _cu_ni_case()
+    B = workloads._beam(10000.0, 200.0, pol_perp_rate=1.0)
+    stage = StaticStage(w.stage.rotation, w.stage.translation)
+    D = _det((24, 20), 5.5e5, w.meta["theta_deg"])
+    phys = B.physics(apply_polarization=True, spherical_decay=True)
+    atoms = B.stage_atoms(ChunkedSample([(pos, spc)]), stage, device=cuda)
+    tiles = engine.Tiles(atoms, B.k, 128, device=cuda)
+    pix = engine.Pixels(np.asarray(D.pixel_coordinates, np.float64) / 1e10, *D.shape, phys,
+                        device=cuda)
+    level, info = engine.pixel_grouping(tiles, pix, B.k, 1e-6)
+    assert level == 3, info
+    radii = tiles.origin[: tiles.n_tiles, 3].cpu().numpy()
+    assert tiles.n_tiles >= 8 and radii.max() <= info["octet_radius_m"]
+    med = float(np.median(radii))
+    assert 0.2 < float((radii <= med).mean()) < 0.8
+
+    def run(cfg):
+        cfg = dict(cfg, pair_short_radius_m=info["quad_short_radius_m"])
+        o = engine.run_split(tiles, pix, phys, atoms.table, launch=cfg, fresnel=0)
+        engine.sync()
+        a = o.cpu().numpy()
+        return (a[:, 0] + 1j * a[:, 1]).reshape(D.shape[1], D.shape[0])
+
+    mixed = run(dict(OCT, octet_radius_m=med))
+    all_oct = run(dict(OCT, octet_radius_m=info["octet_radius_m"]))
+    all_quad = run(dict(OCT, octet_radius_m=0.0))
+    quads = run(QUAD)
+    assert rel_max(all_quad, quads) <= 1e-6         # the same quad arithmetic per tile
+    assert rel_max(mixed, all_oct) <= 2e-5 and rel_max(mixed, quads) <= 2e-5
+    assert rel_intensity(mixed, _oracle(B, pos, spc, D, stage)) <= 1e-4
 
 
 def test_octets_near_the_bound(cuda):

@@ -34,9 +34,13 @@ def _flat_pixels(ny, nz, pitch, dist, y0=0.0, z0=0.0, frames=None):
     return st
 
 
-def _tiles(radius, origin=0.0):
-    return types.SimpleNamespace(n_tiles=4, max_radius=lambda: radius,
-                                 max_origin_norm=lambda: origin)
+def _tiles(radius, origin=0.0, radii=None):
+    """Stub tiles: four of ``radius`` (or the given radii)."""
+    radii = [radius] * 4 if radii is None else list(radii)
+    org = torch.zeros((len(radii), 4), dtype=torch.float64)
+    org[:, 3] = torch.tensor(radii, dtype=torch.float64)
+    return types.SimpleNamespace(n_tiles=len(radii), max_radius=lambda: max(radii),
+                                 max_origin_norm=lambda: origin, origin=org)
 
 
 def test_quad_steps_of_a_flat_detector():
@@ -166,16 +170,30 @@ def test_octet_bounds_of_a_flat_detector():
     assert _flat_pixels(0, 0, p, R, frames=[(8, 4), (6, 2)]).octet_steps() is None
     small, big = _tiles(2e-9, 6e-8), _tiles(4.6e-8, 6e-8)
     lv, info = engine.pixel_grouping(small, pix, k, 1e-6)
-    assert lv == 3 and info["octet_cross_rad"] < 1e-6
+    assert lv == 3 and info["octet_cross_rad"] < 1e-6 and info["octet_tile_fraction"] == 1.0
     assert info["octet_cross_rad"] > info["quad_cross_rad"]
+    assert small.max_radius() < info["octet_radius_m"] < big.max_radius()
+    # every tile too wide: quads; a few wide tiles among narrow ones: octets
+    # (the wide ones take the quad form inside the octet kernel)
     lv, info = engine.pixel_grouping(big, pix, k, 1e-6)
-    assert lv == 2 and info["octet_cross_rad"] > 1e-6
+    assert lv == 2 and info["octet_tile_fraction"] == 0.0
+    mixed = _tiles(0, 6e-8, radii=[2e-9] * 7 + [4.6e-8])
+    lv, info = engine.pixel_grouping(mixed, pix, k, 1e-6)
+    assert lv == 3 and info["octet_tile_fraction"] == pytest.approx(7 / 8)
+    cfg = engine.grouping_launch(dict(pix_per_thread=8, threads=128, pairs=3), lv, mixed, pix, k,
+                                 info)
+    assert cfg["octet_radius_m"] == info["octet_radius_m"]
     assert engine.pixel_grouping(small, _flat_pixels(18, 16, p, R), k, 1e-6)[0] == 2
     assert engine.pixel_grouping(small, pix, k, 1e-6, analyser=1)[0] == 2
+    # the radius shrinks linearly with the budget
+    r1 = engine.octet_bounds(small, pix, k, 1e-6)["radius_m"]
+    r2 = engine.octet_bounds(small, pix, k, 2e-6)["radius_m"]
+    assert r2 == pytest.approx(2 * r1, rel=1e-9)
     # the |d|^2 term's change across the octet counts against the budget
-    c0 = engine.octet_bounds(small, pix, k)["cross"]
-    c1 = engine.octet_bounds(small, pix, k, fresnel_rad=1e-3)["cross"]
+    c0 = engine.octet_bounds(small, pix, k, 1e-6)["cross"]
+    c1 = engine.octet_bounds(small, pix, k, 1e-6, fresnel_rad=1e-3)["cross"]
     assert c1 == pytest.approx(c0 + 4e-3 * st["extent"], rel=1e-9)
+    assert engine.octet_bounds(small, pix, k, 1e-6, fresnel_rad=1.0)["radius_m"] == 0.0
 
 
 def test_octet_launch_clamps():
@@ -187,6 +205,8 @@ def test_octet_launch_clamps():
     g = lambda cfg, level=lv: engine.grouping_launch(cfg, level, small, pix, k, info)
     cfg = g(dict(pix_per_thread=8, threads=128, pairs=3))
     assert cfg["pairs"] == 3 and cfg["pair_short_radius_m"] == info["quad_short_radius_m"]
+    assert cfg["octet_radius_m"] == info["octet_radius_m"] > 0
+    assert g(dict(pix_per_thread=8, threads=128, pairs=2))["octet_radius_m"] == 0.0
     assert g(dict(pix_per_thread=4, threads=128, pairs=3))["pairs"] == 2
     assert g(dict(pix_per_thread=8, threads=128, pairs=3), 2)["pairs"] == 2
     assert engine.default_launch(3) == dict(pix_per_thread=8, threads=128, slices=0, pairs=3)
