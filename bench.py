@@ -23,9 +23,10 @@ plain kernel on a pixel subset (speed and error reference), the batched scan
 surrogate-assisted 101 x 101 theta x chi scan (frames/s against the exact
 batched scan) and the CPU baseline.
 
---impl reference times the reference algorithm's CPU implementation on the
-host cores (the C restatement in oracle/, all threads) on a bounded sample
-of the same workload, rank 0 only.
+--impl reference times the reference's CPU implementation on the host cores
+(its own compute_scattering_cffi compiled from source into oracle/_ref, or,
+where that source is absent, the oracle's C restatement of it; all threads)
+on a bounded sample of the same workload, rank 0 only.
 """
 from __future__ import annotations
 
@@ -195,11 +196,15 @@ def _central_subset(det_shape, m):
 
 
 def cpu_baseline(w, chunks=4, m=32, threads=None, reps=1):
-    """The oracle (C, FP64, reference algorithm) on host cores: `chunks` sample
-    chunks x a central m x m pixel subset."""
+    """The reference CPU path on host cores: ``chunks`` sample chunks x a
+    central m x m pixel subset, all threads. It runs the reference's own
+    kernel (compute_scattering_cffi, compiled from its source into
+    oracle/_ref by oracle/ref_build.py) where that is built, else the
+    oracle's FP64 C restatement of it."""
     import oracle
     B = w.beam
     threads = threads or os.cpu_count() or 1
+    kernel = "reference" if oracle.ref_lib() is not None else "oracle"
     sel = _central_subset(w.detector.shape, m)
     coords = np.asarray(w.detector.pixel_coordinates)[:, sel]
     ch = []
@@ -212,7 +217,8 @@ def cpu_baseline(w, chunks=4, m=32, threads=None, reps=1):
             f0z, B.tables.f1f2, B._beam_E0_map, B._beam_grid(), B._polarization_state())
     kw = dict(apply_polarization=w.sc_kwargs.get("apply_polarization", False),
               spherical_decay=w.sc_kwargs.get("spherical_decay", False),
-              remove_forward=w.sc_kwargs.get("remove_forward", False), n_threads=threads)
+              remove_forward=w.sc_kwargs.get("remove_forward", False), n_threads=threads,
+              kernel=kernel)
     best = None
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -220,11 +226,13 @@ def cpu_baseline(w, chunks=4, m=32, threads=None, reps=1):
         dt = time.perf_counter() - t0
         best = dt if best is None else min(best, dt)
     terms = float(n_atoms) * m * m
+    what = ("the reference's own compute_scattering_cffi (compiled from its source, gcc -O3), "
+            "atom slices on a thread pool summed in order as interact_beam_cpu does"
+            if kernel == "reference" else "FP64 C restatement of the reference CPU kernel")
     return {"value": terms / best / 1e9, "unit": "Gatom*pixel/s", "cores": int(threads),
-            "kind": "port",
+            "kind": "reference" if kernel == "reference" else "port",
             "sample": f"{n_atoms} atoms ({len(ch)} of {w.sample.chunk_total} chunks) x central "
-                      f"{m}x{m} pixels, FP64 C restatement of the reference CPU kernel, "
-                      f"{threads} threads, {best:.2f} s"}
+                      f"{m}x{m} pixels, {what}, {threads} threads, {best:.2f} s"}
 
 
 def probe_pipes(dev):
@@ -363,7 +371,7 @@ def run_reference(args):
                        "sample": "one chunk x central 16x16 pixels per step (terms/s is linear in atoms "
                                  "and pixels)"},
             "cpu_baseline": {"value": val, "unit": "Gatom*pixel/s", "cores": threads,
-                             "kind": "port", "sample": steps[-1]["sample"]},
+                             "kind": steps[-1]["kind"], "sample": steps[-1]["sample"]},
             "e2e": {"value": val, "unit": "Gatom*pixel/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

@@ -327,19 +327,20 @@ int mk_prop_pad(const float *field, int ny, int nz, float *padded, int ny2, int 
 int mk_prop_mul(float *spectrum, int ny2, int nz2, double dy, double dz, double k, double z,
                 double k_axis, double k_perp_y, double k_perp_z, void *stream);
 /* The spectral step with the multiply fused into the transform: on the
- * (nz2, ny2) field already transformed along z (columns, FFT order), each
- * row is transformed along y in shared memory, multiplied by the same
+ * (nz2, ny2) field already transformed along y (rows, FFT order), each
+ * column is transformed along z in shared memory, multiplied by the same
  * propagator as mk_prop_mul (formed in FP32 as the reference's
  * prop_mul_kernel does, Beam.py:4763-4830, with the constant phases
  * z (k - k_axis) and -z k_axis reduced mod 2 pi in FP64) and transformed
- * back along y, unnormalised, in place. The caller's inverse column
- * transform then completes the inverse 2-D transform; the crop applies
- * 1 / (ny2 nz2). Replaces the row passes of the forward and inverse 2-D
- * FFTs and prop_mul_kernel's separate pass over the spectrum. ny2 a power
- * of two in [2, 8192]; workspace of mk_prop_rows_workspace_size bytes
- * (twiddle and wavenumber tables), 16-byte aligned. */
-size_t mk_prop_rows_workspace_size(int ny2, int nz2);
-int mk_prop_rows(float *spectrum, int ny2, int nz2, double dy, double dz, double k, double z,
+ * back along z, unnormalised, in place. The caller's inverse row transform
+ * then completes the inverse 2-D transform; the crop applies
+ * 1 / (ny2 nz2). Replaces the column passes of the forward and inverse 2-D
+ * FFTs and prop_mul_kernel's separate pass over the spectrum. nz2 a power
+ * of two in [2, 8192], ny2 a power of two; workspace of
+ * mk_prop_cols_workspace_size bytes (twiddle and wavenumber tables),
+ * 16-byte aligned. */
+size_t mk_prop_cols_workspace_size(int ny2, int nz2);
+int mk_prop_cols(float *spectrum, int ny2, int nz2, double dy, double dz, double k, double z,
                  double k_axis, double k_perp_y, double k_perp_z, void *workspace, size_t ws_bytes,
                  void *stream);
 /* Centre crop (nz, ny) at (z0, y0) of the inverse transform times `scale`,

@@ -203,10 +203,10 @@ SIGNATURES = {
     "mk_prop_mul": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, _vp]),
-    "mk_prop_rows": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+    "mk_prop_cols": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, _vp, ctypes.c_size_t, _vp]),
-    "mk_prop_rows_workspace_size": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    "mk_prop_cols_workspace_size": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "mk_prop_crop_abs2": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_float, _vp, _vp, _vp]),
     "mk_split_plan": (ctypes.c_int, [ctypes.POINTER(MkTiles), ctypes.POINTER(MkPixels),

@@ -81,142 +81,138 @@ __global__ void mk_prop_crop_kernel(const float2 *__restrict__ G, int ny2, int n
     if (intensity) intensity[(size_t)y * ny + x] = v.x * v.x + v.y * v.y;
 }
 
-// ------------------------------------------------ fused spectral row pass
-// The 2-D transform separates into a transform along z (columns) and one
-// along y (rows), in either order. Taking the columns first and last,
-//   G = C^-1 R^-1 [H o (R C P)] = C^-1 (R^-1 H R) C P,
-// the row transform, the transfer-function multiply and the inverse row
-// transform are adjacent: one kernel does all three per row in shared
-// memory, so the spectrum is read and written once between the two column
-// transforms (cuFFT) instead of three times (row FFT, multiply, inverse row
-// FFT).
+// --------------------------------------------- fused spectral column pass
+// The 2-D transform separates into a transform along y (rows) and one along
+// z (columns), in either order. Taking the rows first and last,
+//   G = R^-1 C^-1 [H o (C R P)] = R^-1 (C^-1 H C) R P,
+// the column transform, the transfer-function multiply and the inverse
+// column transform are adjacent: one kernel does all three for a group of
+// W neighbouring columns in shared memory, so between the two row
+// transforms (cuFFT, contiguous rows) the spectrum is read and written once
+// instead of three times (column FFT, multiply, inverse column FFT).
 //
-// Row FFT: Stockham autosort passes of radix 8 (then 4 or 2 for the rest of
-// log2 N) between two shared-memory rows. Twiddles come from a table of exp(-2 pi i t / N) made in FP64
-// (mk_prop_twiddles). The transfer function is formed in FP32 as the
-// reference's prop_mul_kernel does (Beam.py:4763-4830), with the two large
-// constant phases, z (k - k_axis) and -z k_axis, reduced mod 2 pi in FP64 on
-// the host.
+// A block loads W columns (each row's W neighbours are one contiguous
+// segment of 8 W bytes) into shared memory as W lines of N points in
+// bit-reversed order (stride N + 1, which spreads a row's W points over
+// different banks), transforms every line in place by radix-2
+// decimation-in-time stages fused three at a time (a butterfly keeps its 8
+// points in registers through the three stages and writes them back where
+// it read them), applies H in natural order, bit-reverses the lines and
+// transforms them back the same way, and writes the columns back. Twiddles come from a table of exp(-2 pi i t / N)
+// made in FP64. The transfer function is formed in FP32 as the reference's
+// prop_mul_kernel does (Beam.py:4763-4830), with the two large constant
+// phases, z (k - k_axis) and -z k_axis, reduced mod 2 pi in FP64 on the
+// host.
 #define MK_FFT_NT 512
 #define MK_FFT_MAX 8192
+#define MK_FFT_PTS 16384          // W x N points a block holds
 
 __device__ __forceinline__ float2 mk_cmul(float2 a, float2 b)
 {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
-// In-register DFT of R = 2, 4, 8 points (natural order in and out); INV
-// uses exp(+i ...).
-template <int R, bool INV>
-__device__ __forceinline__ void mk_dft(float2 (&v)[R])
+// Bit reversal of the low `bits` bits of i.
+__device__ __forceinline__ int mk_bitrev(int i, int bits)
 {
-    if constexpr (R == 2) {
-        const float2 a = v[0], b = v[1];
-        v[0] = make_float2(a.x + b.x, a.y + b.y);
-        v[1] = make_float2(a.x - b.x, a.y - b.y);
-    } else if constexpr (R == 4) {
-        const float2 a0 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
-        const float2 a1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
-        const float2 b0 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
-        float2 b1 = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
-        // b1 * (-i) forward, * (+i) inverse
-        b1 = INV ? make_float2(-b1.y, b1.x) : make_float2(b1.y, -b1.x);
-        v[0] = make_float2(a0.x + b0.x, a0.y + b0.y);
-        v[2] = make_float2(a0.x - b0.x, a0.y - b0.y);
-        v[1] = make_float2(a1.x + b1.x, a1.y + b1.y);
-        v[3] = make_float2(a1.x - b1.x, a1.y - b1.y);
-    } else {
-        // 8 = 2 x 4: DFT-4 of the even and odd points, twiddle the odd ones
-        // by exp(-/+ 2 pi i m / 8), combine
-        float2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
-        mk_dft<4, INV>(e);
-        mk_dft<4, INV>(o);
-        const float h = 0.70710678118654752f;
-        const float sg = INV ? 1.f : -1.f;
-        o[1] = mk_cmul(o[1], make_float2(h, sg * h));
-        o[2] = INV ? make_float2(-o[2].y, o[2].x) : make_float2(o[2].y, -o[2].x);
-        o[3] = mk_cmul(o[3], make_float2(-h, sg * h));
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            v[m] = make_float2(e[m].x + o[m].x, e[m].y + o[m].y);
-            v[m + 4] = make_float2(e[m].x - o[m].x, e[m].y - o[m].y);
-        }
-    }
+    return (int)(__brev((unsigned)i) >> (32 - bits));
 }
 
-// One Stockham pass of radix R over a row of N points, from one shared-
-// memory buffer to the other; Ns = product of the radices before it.
-// Butterfly j reads points j + r N/R, twiddles them by
-// exp(-/+ 2 pi i r (j mod Ns) / (Ns R)) and writes its R outputs to
-// (j - j mod Ns) R + j mod Ns + r Ns.
-template <int R, bool INV>
-__device__ __forceinline__ void mk_fft_pass(const float2 *src, float2 *dst, int N, int Ns,
+// G consecutive in-place radix-2 decimation-in-time stages (half sizes m,
+// 2m, .., 2^(G-1) m) fused into one pass over W lines of N points in shared
+// memory (line c at s + c * ld; the lines were loaded in bit-reversed
+// order). A butterfly owns the R = 2^G points b + i + r m (b a multiple of
+// R m, i < m), keeps them in registers through the G stages and writes them
+// back where it read them, so the pass works in place. Stage h pairs points
+// a and a + 2^h (bit h of a clear) with the twiddle
+// exp(-/+ 2 pi i j / (2^(h+1) m)), j = i + (a mod 2^h) m.
+template <int G, bool INV>
+__device__ __forceinline__ void mk_dit_pass(float2 *s, int ld, int W, int N, int m,
                                             const float2 *__restrict__ tw)
 {
-    const int nb = N / R;
-    const int tstep = N / (Ns * R);
-    for (int j = threadIdx.x; j < nb; j += MK_FFT_NT) {
+    constexpr int R = 1 << G;
+    const int nb = N / R, total = W * nb;
+    for (int t = threadIdx.x; t < total; t += MK_FFT_NT) {
+        const int c = t / nb, q = t - c * nb;
+        const int i = q & (m - 1);
+        float2 *pts = s + c * ld + (q - i) * R + i;
         float2 v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
-        const int k = j & (Ns - 1);
-        if (Ns > 1) {
+        for (int r = 0; r < R; ++r) v[r] = pts[r * m];
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 w = __ldg(tw + r * k * tstep);
+        for (int h = 0; h < G; ++h) {
+            const int hs = m << h;
+            const int tstep = N / (2 * hs);
+#pragma unroll
+            for (int a = 0; a < R; ++a) {
+                if (a & (1 << h)) continue;
+                const int j = i + (a & ((1 << h) - 1)) * m;
+                float2 w = __ldg(tw + j * tstep);
                 if (INV) w.y = -w.y;
-                v[r] = mk_cmul(v[r], w);
+                const float2 x = v[a], y = mk_cmul(v[a + (1 << h)], w);
+                v[a] = make_float2(x.x + y.x, x.y + y.y);
+                v[a + (1 << h)] = make_float2(x.x - y.x, x.y - y.y);
             }
         }
-        mk_dft<R, INV>(v);
-        const int base = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) dst[base + r * Ns] = v[r];
+        for (int r = 0; r < R; ++r) pts[r * m] = v[r];
     }
     __syncthreads();
 }
 
-// FFT of the row in buf[0]; returns the buffer (0 or 1) holding the result.
+// FFT of W lines of N = 2^logn points loaded in bit-reversed order; the
+// result is in natural order, in place.
 template <bool INV>
-__device__ __forceinline__ int mk_fft_row(float2 *buf0, float2 *buf1, int N, int logn,
-                                          const float2 *__restrict__ tw)
+__device__ __forceinline__ void mk_fft_lines(float2 *s, int ld, int W, int N, int logn,
+                                             const float2 *__restrict__ tw)
 {
-    float2 *src = buf0, *dst = buf1;
-    int Ns = 1, left = logn, at = 0;
-    for (; left >= 3; left -= 3, Ns *= 8) {
-        mk_fft_pass<8, INV>(src, dst, N, Ns, tw);
-        float2 *t = src; src = dst; dst = t; at ^= 1;
-    }
-    if (left == 2) {
-        mk_fft_pass<4, INV>(src, dst, N, Ns, tw);
-        at ^= 1;
-    } else if (left == 1) {
-        mk_fft_pass<2, INV>(src, dst, N, Ns, tw);
-        at ^= 1;
-    }
-    return at;
+    int m = 1, left = logn;
+    for (; left >= 3; left -= 3, m <<= 3) mk_dit_pass<3, INV>(s, ld, W, N, m, tw);
+    if (left == 2) mk_dit_pass<2, INV>(s, ld, W, N, m, tw);
+    else if (left == 1) mk_dit_pass<1, INV>(s, ld, W, N, m, tw);
 }
 
-// F (nz2, ny2) column-transformed spectrum, in place: each row y-transformed,
-// multiplied by H(ky[x], kz[row]) and inverse y-transformed (unnormalised).
-// ky, kz: FP32 transverse wavenumbers (2 pi fftfreq + carrier offset) of
-// every column and row; c_prop = z (k - k_axis) mod 2 pi, c_evan =
-// -z k_axis mod 2 pi. Shared memory: two rows (ping-pong between passes).
+// In-place bit-reversal permutation of W lines (between the forward and the
+// inverse transform, whose input must again be bit-reversed).
+__device__ __forceinline__ void mk_bitrev_lines(float2 *s, int ld, int W, int N, int logn)
+{
+    for (int e = threadIdx.x; e < W * N; e += MK_FFT_NT) {
+        const int c = e / N, r = e - c * N;
+        const int q = mk_bitrev(r, logn);
+        if (q > r) {
+            float2 *line = s + c * ld;
+            const float2 t = line[r];
+            line[r] = line[q];
+            line[q] = t;
+        }
+    }
+    __syncthreads();
+}
+
+// F (nz2, ny2) row-transformed spectrum, in place: every column
+// z-transformed, multiplied by H(ky[col], kz[row]) and inverse
+// z-transformed (unnormalised). W columns a block; ky, kz: FP32 transverse
+// wavenumbers (2 pi fftfreq + carrier offset) of every column and row;
+// c_prop = z (k - k_axis) mod 2 pi, c_evan = -z k_axis mod 2 pi.
 __global__ void __launch_bounds__(MK_FFT_NT)
-    mk_prop_rows_kernel(float2 *__restrict__ F, int ny2, int logn, int nz2,
+    mk_prop_cols_kernel(float2 *__restrict__ F, int ny2, int nz2, int logn, int W,
                         const float2 *__restrict__ tw, const float *__restrict__ ky,
                         const float *__restrict__ kz, float k, float z, float c_prop, float c_evan)
 {
-    extern __shared__ __align__(16) float2 s_buf[];
-    float2 *b0 = s_buf, *b1 = s_buf + ny2;
-    for (int rowi = blockIdx.x; rowi < nz2; rowi += gridDim.x) {
-        float2 *g = F + (size_t)rowi * ny2;
-        for (int x = threadIdx.x; x < ny2; x += MK_FFT_NT) b0[x] = g[x];
+    extern __shared__ __align__(16) float2 s_lines[];
+    const int ld = nz2 + 1;
+    const int groups = ny2 / W, pts = W * nz2;
+    for (int g = blockIdx.x; g < groups; g += gridDim.x) {
+        const int c0 = g * W;
+        for (int e = threadIdx.x; e < pts; e += MK_FFT_NT) {
+            const int r = e / W, c = e - r * W;
+            s_lines[c * ld + mk_bitrev(r, logn)] = F[(size_t)r * ny2 + c0 + c];
+        }
         __syncthreads();
-        float2 *spec = mk_fft_row<false>(b0, b1, ny2, logn, tw) ? b1 : b0;
-        const float b = kz[rowi];
-        for (int x = threadIdx.x; x < ny2; x += MK_FFT_NT) {
-            const float a = ky[x];
+        mk_fft_lines<false>(s_lines, ld, W, nz2, logn, tw);
+        for (int e = threadIdx.x; e < pts; e += MK_FFT_NT) {
+            const int c = e / nz2, r = e - c * nz2;
+            const float a = ky[c0 + c], b = kz[r];
             const float kt2 = fmaf(a, a, b * b);
             const float kt = sqrtf(kt2);
             float ph, amp;
@@ -230,11 +226,16 @@ __global__ void __launch_bounds__(MK_FFT_NT)
             }
             float sn, cs;
             sincosf(ph, &sn, &cs);
-            b0[x] = mk_cmul(spec[x], make_float2(amp * cs, amp * sn));
+            float2 *p = s_lines + c * ld + r;
+            *p = mk_cmul(*p, make_float2(amp * cs, amp * sn));
         }
         __syncthreads();
-        const float2 *res = mk_fft_row<true>(b0, b1, ny2, logn, tw) ? b1 : b0;
-        for (int x = threadIdx.x; x < ny2; x += MK_FFT_NT) g[x] = res[x];
+        mk_bitrev_lines(s_lines, ld, W, nz2, logn);
+        mk_fft_lines<true>(s_lines, ld, W, nz2, logn, tw);
+        for (int e = threadIdx.x; e < pts; e += MK_FFT_NT) {
+            const int r = e / W, c = e - r * W;
+            F[(size_t)r * ny2 + c0 + c] = s_lines[c * ld + r];
+        }
         __syncthreads();
     }
 }
@@ -257,33 +258,46 @@ __global__ void mk_prop_freq_kernel(float *__restrict__ out, int n, double d, do
     out[i] = (float)(MK_TWO_PI * mk_fftfreq(i, n, d) + off);
 }
 
-extern "C" size_t mk_prop_rows_workspace_size(int ny2, int nz2)
+// Columns a block: W x nz2 <= MK_FFT_PTS, at most 16 and the row length.
+static int mk_prop_cols_width(int ny2, int nz2)
 {
-    if (ny2 <= 0 || nz2 <= 0) return 0;
-    return sizeof(float2) * (size_t)ny2 + sizeof(float) * ((size_t)ny2 + (size_t)nz2) + 256;
+    int W = MK_FFT_PTS / nz2;
+    W = std::min(W, 16);
+    W = std::min(W, ny2);
+    return std::max(W, 1);
 }
 
-extern "C" int mk_prop_rows(float *spectrum, int ny2, int nz2, double dy, double dz, double k,
+extern "C" size_t mk_prop_cols_workspace_size(int ny2, int nz2)
+{
+    if (ny2 <= 0 || nz2 <= 0) return 0;
+    return sizeof(float2) * (size_t)nz2 + sizeof(float) * ((size_t)ny2 + (size_t)nz2) + 256;
+}
+
+extern "C" int mk_prop_cols(float *spectrum, int ny2, int nz2, double dy, double dz, double k,
                             double z, double k_axis, double k_perp_y, double k_perp_z,
                             void *workspace, size_t ws_bytes, void *stream)
 {
     MK_REQUIRE(spectrum && ny2 > 0 && nz2 > 0 && dy > 0.0 && dz > 0.0 && k > 0.0,
-               "mk_prop_rows: bad arguments");
-    MK_REQUIRE((ny2 & (ny2 - 1)) == 0 && ny2 >= 2 && ny2 <= MK_FFT_MAX,
-               "mk_prop_rows: the row length %d must be a power of two in [2, %d]", ny2, MK_FFT_MAX);
-    const size_t need = mk_prop_rows_workspace_size(ny2, nz2);
+               "mk_prop_cols: bad arguments");
+    MK_REQUIRE((nz2 & (nz2 - 1)) == 0 && nz2 >= 2 && nz2 <= MK_FFT_MAX,
+               "mk_prop_cols: the column length %d must be a power of two in [2, %d]", nz2,
+               MK_FFT_MAX);
+    MK_REQUIRE((ny2 & (ny2 - 1)) == 0, "mk_prop_cols: the row length %d must be a power of two",
+               ny2);
+    const size_t need = mk_prop_cols_workspace_size(ny2, nz2);
     if (!workspace || ws_bytes < need) {
-        mk_set_error("mk_prop_rows: workspace %zu bytes, need %zu", ws_bytes, need);
+        mk_set_error("mk_prop_cols: workspace %zu bytes, need %zu", ws_bytes, need);
         return MK_ENOMEM;
     }
-    MK_REQUIRE(((uintptr_t)workspace & 15) == 0, "mk_prop_rows: workspace must be 16-byte aligned");
+    MK_REQUIRE(((uintptr_t)workspace & 15) == 0, "mk_prop_cols: workspace must be 16-byte aligned");
     int logn = 0;
-    while ((1 << logn) < ny2) ++logn;
+    while ((1 << logn) < nz2) ++logn;
+    const int W = mk_prop_cols_width(ny2, nz2);
     cudaStream_t st = mk_stream(stream);
     float2 *tw = reinterpret_cast<float2 *>(workspace);
-    float *ky = reinterpret_cast<float *>(tw + ny2);
+    float *ky = reinterpret_cast<float *>(tw + nz2);
     float *kz = ky + ny2;
-    mk_prop_twiddle_kernel<<<(ny2 + 255) / 256, 256, 0, st>>>(tw, ny2);
+    mk_prop_twiddle_kernel<<<(nz2 + 255) / 256, 256, 0, st>>>(tw, nz2);
     MK_CHECK_CUDA(cudaGetLastError());
     mk_prop_freq_kernel<<<(ny2 + 255) / 256, 256, 0, st>>>(ky, ny2, dy, k_perp_y);
     MK_CHECK_CUDA(cudaGetLastError());
@@ -291,18 +305,18 @@ extern "C" int mk_prop_rows(float *spectrum, int ny2, int nz2, double dy, double
     MK_CHECK_CUDA(cudaGetLastError());
     const double c_prop = fmod(z * (k - k_axis), MK_TWO_PI);
     const double c_evan = fmod(-z * k_axis, MK_TWO_PI);
-    const size_t smem = 2 * sizeof(float2) * (size_t)ny2;
-    MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)mk_prop_rows_kernel,
+    const size_t smem = sizeof(float2) * (size_t)W * (size_t)(nz2 + 1);
+    MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)mk_prop_cols_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, sms = 0, bps = 0;
     MK_CHECK_CUDA(cudaGetDevice(&dev));
     MK_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    MK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void *)mk_prop_rows_kernel,
+    MK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void *)mk_prop_cols_kernel,
                                                                 MK_FFT_NT, smem));
-    MK_REQUIRE(bps >= 1, "mk_prop_rows: a row of %d points does not fit on an SM", ny2);
-    const int grid = std::min(nz2, sms * bps);
-    mk_prop_rows_kernel<<<grid, MK_FFT_NT, smem, st>>>(reinterpret_cast<float2 *>(spectrum), ny2, logn,
-                                                      nz2, tw, ky, kz, (float)k, (float)z,
+    MK_REQUIRE(bps >= 1, "mk_prop_cols: %d columns of %d points do not fit on an SM", W, nz2);
+    const int grid = std::min(ny2 / W, sms * bps);
+    mk_prop_cols_kernel<<<grid, MK_FFT_NT, smem, st>>>(reinterpret_cast<float2 *>(spectrum), ny2, nz2,
+                                                      logn, W, tw, ky, kz, (float)k, (float)z,
                                                       (float)c_prop, (float)c_evan);
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;

@@ -6,11 +6,12 @@ to a power-of-two grid sized for the distance, transformed, multiplied by the
 exact free-space transfer function with the carrier removed, transformed
 back and centre-cropped; distances the padded grid cannot sample without
 aliasing are split into equal alias-free steps. Here the 2-D transform is
-split by dimension: the column (z) transforms are cuFFT through torch.fft,
-and one libmosaic_kin kernel (``mk_prop_rows``) does the row transform, the
-transfer-function multiply and the inverse row transform per row in shared
-memory, so the spectrum makes one round trip through HBM between the column
-transforms instead of three. The pad and the crop (fused with |A|^2) are
+split by dimension: the row (y) transforms, over contiguous rows, are cuFFT
+through torch.fft, and one libmosaic_kin kernel (``mk_prop_cols``) does the
+column transform, the transfer-function multiply and the inverse column
+transform for groups of neighbouring columns in shared memory, so the
+spectrum makes one round trip through HBM between the row transforms
+instead of three. The pad and the crop (fused with |A|^2) are
 libmosaic_kin kernels too. ``fused=False`` runs the unfused sequence
 (cuFFT 2-D transforms around ``mk_prop_mul``, FP64 phase) instead.
 
@@ -106,12 +107,12 @@ def propagate(field, dy, dz, z, wavelength, step_max=None, pad_factor=1.0, paddi
         check(L.mk_prop_pad(E.data_ptr(), Ny, Nz, P.data_ptr(), Ny2, Nz2, y0, z0, mode,
                             c.real, c.imag, sh))
         if fused:
-            F = torch.fft.fft(P, dim=0)                # columns (z)
-            ws_n = int(L.mk_prop_rows_workspace_size(Ny2, Nz2))
+            F = torch.fft.fft(P, dim=-1).contiguous()   # rows (y); already contiguous
+            ws_n = int(L.mk_prop_cols_workspace_size(Ny2, Nz2))
             ws = torch.empty(ws_n, dtype=torch.uint8, device=E.device)
-            check(L.mk_prop_rows(F.data_ptr(), Ny2, Nz2, float(dy), float(dz), k, dz_step, kga,
+            check(L.mk_prop_cols(F.data_ptr(), Ny2, Nz2, float(dy), float(dz), k, dz_step, kga,
                                  float(k_perp_y), float(k_perp_z), ws.data_ptr(), ws_n, sh))
-            G = torch.fft.ifft(F, dim=0, norm="forward")   # unnormalised; 1/N in the crop
+            G = torch.fft.ifft(F, dim=-1, norm="forward")   # unnormalised; 1/N in the crop
         else:
             F = torch.fft.fft2(P)
             check(L.mk_prop_mul(F.data_ptr(), Ny2, Nz2, float(dy), float(dz), k, dz_step, kga,

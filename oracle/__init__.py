@@ -10,6 +10,11 @@ Contents
   ``compute_scattering_cffi`` (MOSAIC ``Beam.py:663-816``), threaded over atom
   slices summed in slice order (``Beam.py:5941-5955``), plus the free-space
   propagator multiply (``Beam.py:4747-4834``).
+* ``scatter_ref`` -- the reference's OWN CPU kernel, ``compute_scattering_cffi``,
+  compiled from its source by ``oracle/ref_build.py`` into ``oracle/_ref/``
+  when a reference checkout (or its extracted source) is present: the
+  timed CPU baseline of the reference, threaded over atom slices summed in
+  slice order as ``interact_beam_cpu`` does (``Beam.py:5933-5955``).
 * ``ref_tables`` / ``ein_bilinear`` / ``polarization_state`` /
   ``interact_cpu`` below -- NumPy restatements of the reference host logic
   around that kernel (``Beam.py:31-47``, ``117-149``, ``503-615``, ``956-1045``,
@@ -39,7 +44,9 @@ Q_E = 1.602176634e-19
 
 
 def build(force: bool = False) -> str:
-    """Compile kin_oracle.c into oracle/_ref/libkin_oracle.so.
+    """Compile kin_oracle.c into oracle/_ref/libkin_oracle.so, and the
+    reference's own CPU kernel where its source is available
+    (oracle/ref_build.py).
 
     gcc -O3 with -ffp-contract=off: without contraction the x86 and Arm builds
     round every operation identically. The absolute phase k (x + r) is ~1e10 rad,
@@ -50,12 +57,98 @@ def build(force: bool = False) -> str:
     os.makedirs(os.path.dirname(_SO), exist_ok=True)
     if (not force and os.path.exists(_SO)
             and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
+        _build_ref()
         return _SO
     tmp = _SO + f".tmp{os.getpid()}"
     subprocess.check_call(["gcc", "-O3", "-ffp-contract=off", "-std=c11", "-shared", "-fPIC", "-pthread",
                            _SRC, "-o", tmp, "-lm"])
     os.replace(tmp, _SO)
+    _build_ref()
     return _SO
+
+
+def _build_ref():
+    """The reference's own kernels where their source is available: the CPU
+    kernel (gcc) and the GPU general kernel (nvcc, for the comparator)."""
+    from . import ref_build
+    for step in (ref_build.build, ref_build.build_gpu):
+        try:
+            step()
+        except (OSError, subprocess.CalledProcessError, ValueError, RuntimeError):
+            pass
+
+
+_ref_lib = None
+
+
+def ref_lib():
+    """The reference's own compute_scattering_cffi (ctypes), or None when it
+    could not be built here (no reference checkout and no extracted source)."""
+    global _ref_lib
+    if _ref_lib is None:
+        from . import ref_build
+        try:
+            so = ref_build.build()
+        except (OSError, subprocess.CalledProcessError, ValueError, RuntimeError):
+            so = None
+        if so is None:
+            return None
+        L = ctypes.CDLL(so)
+        dp = ctypes.POINTER(ctypes.c_double)
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.compute_scattering_cffi.restype = ctypes.c_int
+        L.compute_scattering_cffi.argtypes = [
+            ctypes.c_int, dp, fp, fp, ctypes.c_int, fp, fp, fp, fp, ctypes.c_int, ctypes.c_int,
+            dp, dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+            ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, fp]
+        _ref_lib = L
+    return _ref_lib
+
+
+def scatter_ref(pos_m, wk, f0z, anom_re, anom_im, amp_re, amp_im, cx, cy, cz, k, ny, nz,
+                remove_forward=False, apply_pol=False, pol=(0.0, 0.0, 1.0, 0.0), decay=False,
+                n_threads=None, slice_atoms=None):
+    """The reference's own CPU kernel on atom slices, ``n_threads`` at a time
+    (ctypes releases the GIL), each slice into its own float32 buffers and
+    the slices summed in order (Beam.py:5933-5955). Same arguments as
+    ``scatter_f64`` (no Debye-Waller factor or analyser: the reference's CPU
+    kernel has neither). Returns complex128 (ny*nz,)."""
+    from concurrent.futures import ThreadPoolExecutor
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("the reference CPU kernel is not built (oracle/ref_build.py)")
+    n = int(np.asarray(pos_m).shape[0])
+    P = int(ny) * int(nz)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    pos = f64(pos_m).reshape(n, 3)
+    wk = f32(wk).reshape(n, 11)
+    f0z, ar, ai, er, ei = (f32(v).reshape(n) for v in (f0z, anom_re, anom_im, amp_re, amp_im))
+    cx, cy, cz = (f64(v).reshape(P) for v in (cx, cy, cz))
+    nt = int(n_threads or os.cpu_count() or 1)
+    sl = int(slice_atoms or max(1000, -(-max(n, 1) // nt)))
+
+    def run(a0, a1):
+        o_r = np.zeros(P, np.float32)
+        o_i = np.zeros(P, np.float32)
+        rc = L.compute_scattering_cffi(
+            a1 - a0, _p(pos[a0:a1], ctypes.c_double), _p(wk[a0:a1], ctypes.c_float),
+            _p(f0z[a0:a1], ctypes.c_float), int(bool(remove_forward)),
+            _p(ar[a0:a1], ctypes.c_float), _p(ai[a0:a1], ctypes.c_float),
+            _p(er[a0:a1], ctypes.c_float), _p(ei[a0:a1], ctypes.c_float), int(ny), int(nz),
+            _p(cx, ctypes.c_double), _p(cy, ctypes.c_double), _p(cz, ctypes.c_double), float(k),
+            int(bool(apply_pol)), float(pol[0]), float(pol[1]), float(pol[2]), float(pol[3]),
+            int(bool(decay)), _p(o_r, ctypes.c_float), _p(o_i, ctypes.c_float))
+        if rc != 0:
+            raise MemoryError("reference CPU kernel could not allocate its work buffers")
+        return o_r.astype(np.float64) + 1j * o_i.astype(np.float64)
+
+    out = np.zeros(P, np.complex128)
+    bounds = [(a, min(a + sl, n)) for a in range(0, n, sl)]
+    with ThreadPoolExecutor(max_workers=max(1, min(nt, len(bounds)))) as ex:
+        for f in [ex.submit(run, a, b) for a, b in bounds]:
+            out += f.result()
+    return out
 
 
 def lib():
@@ -328,7 +421,7 @@ def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV
                  f0_rows, f0_zero, f1f2_tables, E0, beam_grid, pol_state,
                  remove_forward=False, apply_polarization=False,
                  spherical_decay=False, dw_b=None, n_threads=None, analyser=None,
-                 depth=False):
+                 depth=False, kernel="oracle"):
     """Restatement of ``interact_beam_cpu`` (Beam.py:5773-5956), returning
     complex128 (Nz, Ny). ``analyser`` (see ``scatter_f64``) adds the GPU
     general kernel's analyser factor, which the reference's CPU path does not
@@ -340,6 +433,9 @@ def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV
     beam_grid: (du, dv, uc, vc). f0_rows: element -> (11,) float32;
     f0_zero: element -> float; f1f2_tables: element -> (M,3) float32.
     dw_b: None or element -> B (A^2).
+    kernel: "oracle" (the FP64 C restatement) or "reference" (the
+    reference's own compute_scattering_cffi, ``scatter_ref``; no
+    Debye-Waller factor or analyser).
     """
     Ny, Nz = shape
     lam = H_PLANCK / Q_E * C_LIGHT / float(energy_eV)
@@ -402,6 +498,14 @@ def interact_cpu(chunks, pixel_coords_A, shape, rotation, translation, energy_eV
                 ai[m] = c.imag
             if dw_b is not None:
                 b[m] = float(dw_b.get(el, 0.0))
+        if kernel == "reference":
+            if dw_b is not None or analyser is not None:
+                raise ValueError("the reference CPU kernel has no Debye-Waller factor or analyser")
+            out += scatter_ref(lab.astype(np.float64) / 1e10, wk, f0z, ar, ai, amp.real,
+                               amp.imag, cx, cy, cz, k, Ny, Nz, remove_forward=remove_forward,
+                               apply_pol=apply_polarization, pol=pol_state, decay=spherical_decay,
+                               n_threads=n_threads)
+            continue
         out += scatter_f64(lab.astype(np.float64) / 1e10, wk, f0z, ar, ai,
                            amp.real, amp.imag, cx, cy, cz, k, Ny, Nz,
                            remove_forward=remove_forward, apply_pol=apply_polarization,

@@ -1,6 +1,7 @@
-"""The benchmark's reference arm (the oracle's C restatement of the reference
-CPU kernel on the host cores) runs without a GPU and prints one JSON line
-with the same metric as the GPU arm."""
+"""The benchmark's reference arm (the reference's own CPU kernel, compiled
+from its source into oracle/_ref, or where that source is absent the
+oracle's C restatement of it, on the host cores) runs without a GPU and
+prints one JSON line with the same metric as the GPU arm."""
 import json
 import os
 import subprocess
@@ -19,6 +20,8 @@ def test_reference_arm_prints_the_contract_line():
     import bench
     assert line["impl"] == "reference" and line["metric"] == bench.METRIC
     assert line["unit"] == "Gatom*pixel/s" and line["higher_is_better"] is True
-    assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
+    import oracle
+    kind = "reference" if oracle.ref_lib() is not None else "port"
+    assert line["value"] > 0 and line["cpu_baseline"]["kind"] == kind
     assert line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["config"]["workload"] == "fcc_cu_32k"

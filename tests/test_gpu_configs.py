@@ -35,15 +35,15 @@ def _check_spread(B, w, a32, kw, label):
 
 
 def test_nacl_screw_8m_fp32_vs_fp64_whole_detector(cuda):
-    """The headline configuration (8.19M atoms, 512^2 pixels, 2x2 pixel
-    quads): FP32 over the whole detector against FP64 at 1,029 pixels that
-    reach its corners and edges."""
+    """The headline configuration (8.19M atoms, 512^2 pixels, pixels sharing
+    sin/cos in 2x4 octets): FP32 over the whole detector against FP64 at
+    1,029 pixels that reach its corners and edges."""
     w = workloads.nacl_screw_8m()
     B = w.beam
     kw = w.sc_kwargs
     B._use_fast_kernel = True
     a32 = B.atomic_scattering_kinematic(w.sample, w.detector, w.stage, return_double=True, **kw)
-    assert B.last_run["path"] == "split_f32" and B.last_run["launch"]["pairs"] == 2, B.last_run
+    assert B.last_run["path"] == "split_f32" and B.last_run["launch"]["pairs"] >= 2, B.last_run
     _check_spread(B, w, a32, kw, "nacl_screw_8m")
     assert np.isfinite(a32).all()
 

@@ -64,13 +64,14 @@ def test_wavefield_propagation_entry_point_and_fused_intensity(cuda):
         B.wavefield_propagation(D, propagation.FreeSpaceStack([1.0]))
 
 
-@pytest.mark.parametrize("ny2,nz2", [(2, 4), (4, 8), (8, 16), (64, 32), (512, 16), (2048, 8),
-                                     (4096, 4), (8192, 64)])
-def test_fused_row_pass_matches_unfused_spectral_step(cuda, ny2, nz2):
-    """mk_prop_rows between the column transforms equals the unfused step
+@pytest.mark.parametrize("ny2,nz2", [(4, 2), (8, 4), (16, 8), (32, 64), (16, 512), (8, 2048),
+                                     (4, 4096), (64, 8192), (2, 8192), (1024, 1024)])
+def test_fused_column_pass_matches_unfused_spectral_step(cuda, ny2, nz2):
+    """mk_prop_cols between the row transforms equals the unfused step
     (2-D cuFFT, mk_prop_mul's FP64 multiply, inverse 2-D cuFFT) on random
-    grids for row lengths 2..8192 (every Stockham radix tail), within FP32
-    rounding of the transforms (relative 2e-6 of max |A|)."""
+    grids for column lengths 2..8192 (every stage-group tail, 1 to 16
+    columns a block), within FP32 rounding of the transforms (relative
+    2e-6 of max |A|, scaled with the transform length)."""
     from mosaic_gb300 import _lib, engine
     L = _lib.load()
     rng = np.random.default_rng(ny2 + nz2)
@@ -83,29 +84,32 @@ def test_fused_row_pass_matches_unfused_spectral_step(cuda, ny2, nz2):
     F = torch.fft.fft2(X)
     _lib.check(L.mk_prop_mul(F.data_ptr(), ny2, nz2, dy, dz, k, z, k, 0.0, 0.0, sh))
     ref = torch.fft.ifft2(F, norm="forward")
-    G = torch.fft.fft(X, dim=0).contiguous()
-    ws_n = int(L.mk_prop_rows_workspace_size(ny2, nz2))
+    G = torch.fft.fft(X, dim=-1)
+    assert G.is_contiguous()
+    ws_n = int(L.mk_prop_cols_workspace_size(ny2, nz2))
     ws = torch.empty(ws_n, dtype=torch.uint8, device=cuda)
-    _lib.check(L.mk_prop_rows(G.data_ptr(), ny2, nz2, dy, dz, k, z, k, 0.0, 0.0, ws.data_ptr(),
+    _lib.check(L.mk_prop_cols(G.data_ptr(), ny2, nz2, dy, dz, k, z, k, 0.0, 0.0, ws.data_ptr(),
                               ws_n, sh))
-    got = torch.fft.ifft(G, dim=0, norm="forward")
+    got = torch.fft.ifft(G, dim=-1, norm="forward")
     engine.sync()
     err = float((got - ref).abs().max() / ref.abs().max())
     assert err <= 2e-6 * max(1.0, np.log2(ny2 * nz2) / 8), err
 
 
-def test_fused_row_pass_rejects_bad_rows(cuda):
+def test_fused_column_pass_rejects_bad_shapes(cuda):
     from mosaic_gb300 import _lib, engine
     L = _lib.load()
     buf = torch.zeros((4, 24), dtype=torch.complex64, device=cuda)
     ws = torch.empty(4096, dtype=torch.uint8, device=cuda)
     sh = engine._stream_handle()
     k = 2 * np.pi / 1.2398e-10
-    assert L.mk_prop_rows(buf.data_ptr(), 24, 4, 1e-6, 1e-6, k, 0.01, k, 0.0, 0.0, ws.data_ptr(),
+    assert L.mk_prop_cols(buf.data_ptr(), 4, 24, 1e-6, 1e-6, k, 0.01, k, 0.0, 0.0, ws.data_ptr(),
                           4096, sh) == _lib.MK_EINVAL          # 24 is not a power of two
-    assert L.mk_prop_rows(buf.data_ptr(), 16384, 1, 1e-6, 1e-6, k, 0.01, k, 0.0, 0.0,
+    assert L.mk_prop_cols(buf.data_ptr(), 1, 16384, 1e-6, 1e-6, k, 0.01, k, 0.0, 0.0,
                           ws.data_ptr(), 4096, sh) == _lib.MK_EINVAL   # longer than 8192
-    assert L.mk_prop_rows(buf.data_ptr(), 16, 4, 1e-6, 1e-6, k, 0.01, k, 0.0, 0.0, ws.data_ptr(),
+    assert L.mk_prop_cols(buf.data_ptr(), 24, 4, 1e-6, 1e-6, k, 0.01, k, 0.0, 0.0, ws.data_ptr(),
+                          4096, sh) == _lib.MK_EINVAL          # rows not a power of two
+    assert L.mk_prop_cols(buf.data_ptr(), 16, 4, 1e-6, 1e-6, k, 0.01, k, 0.0, 0.0, ws.data_ptr(),
                           8, sh) == _lib.MK_ENOMEM             # workspace too small
 
 

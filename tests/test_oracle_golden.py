@@ -128,3 +128,26 @@ def test_depth_blur_matches_oracle():
     for rad in (1, 3, 6):
         got = engine._gauss_blur(torch.tensor(m), rad).numpy()
         assert np.allclose(got, oracle.blur_map(m, rad), rtol=0, atol=1e-6), rad
+
+
+def test_reference_kernel_built_from_its_source(golden):
+    """The reference's own compute_scattering_cffi, compiled from its source
+    by oracle/ref_build.py (skipped where neither a reference checkout nor
+    the extracted source is present), reproduces the fixtures it made, and
+    the oracle; it is the CPU baseline the benchmark times."""
+    import pytest
+    if oracle.ref_lib() is None:
+        pytest.skip("reference source not available on this machine")
+    d = golden("kernel_cases.npz")
+    for i in range(int(d["n"])):
+        p = f"c{i}_"
+        ny, nz, rf, ap, dc, k, pdeg, ex, ey, ez = d[p + "meta"]
+        a, amp, c = d[p + "anom"], d[p + "amp"], d[p + "cxyz"]
+        args = (d[p + "pos_m"], d[p + "wk"], d[p + "f0z"], a.real, a.imag, amp.real, amp.imag,
+                c[0], c[1], c[2], k, int(ny), int(nz), rf, ap, (pdeg, ex, ey, ez), dc)
+        got = oracle.scatter_ref(*args, n_threads=3, slice_atoms=100)
+        m = np.abs(got).max()
+        # float32 output per slice; contraction as the host compiler chooses
+        assert np.abs(got - d[p + "out_numpy"]).max() / m <= 1e-5, i
+        assert np.abs(got - d[p + "out_cffi"]).max() / m <= 1e-5, i
+        assert np.abs(got - oracle.scatter_f64(*args, n_threads=2)).max() / m <= 1e-5, i

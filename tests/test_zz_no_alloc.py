@@ -69,7 +69,7 @@ def test_noalloc_entry_caps_slices_to_the_scratch(cuda):
     run with those 8 slices (same plan, same fixed-order reduction) and
     agrees with the 64-slice run within the FP32 path's tolerance."""
     L = _lib.load()
-    w = workloads.fcc_cu_32k(cells=10, npix=512)
+    w = workloads.fcc_cu_32k(cells=13, npix=512)
     B = w.beam
     phys = B.physics(**w.sc_kwargs)
     atoms = B.stage_atoms(w.sample, w.stage, device=cuda)
