@@ -288,10 +288,10 @@ class SurrogateScan:
         rank: principal components of the normalised frames the network
             predicts; scale_weight: loss weight of the log peak output
             against the (variance-weighted) components.
-        refine_steps: when judges fail, further training steps on all exact
-            frames (training + judged) before the failed blocks are predicted
-            again and re-judged once (0: failed blocks go straight to the
-            exact sum).
+        refine_steps: further training steps on all exact frames (training +
+            judged) before the unjudged frames are predicted again and failed
+            blocks re-judged once (0: no refinement, failed blocks go straight
+            to the exact sum).
     """
 
     def __init__(self, beam, sample, detector, stage, theta, chi, roi=128, stride=4, raster=False,
@@ -364,6 +364,17 @@ class SurrogateScan:
             I[idx] = sh[:2] + I[idx]
             del I, T2, sh
             torch.cuda.synchronize()
+
+    def _train_distance(self, idx):
+        """Grid distance of each frame (indices into the scan) to its nearest
+        training frame."""
+        tr = self.ij[self.train].astype(np.float64)
+        q = self.ij[np.asarray(idx)].astype(np.float64)
+        d = np.full(len(q), np.inf)
+        for c in range(0, len(tr), 512):
+            t = tr[c: c + 512]
+            d = np.minimum(d, np.sqrt(((q[:, None, :] - t[None, :, :]) ** 2).sum(-1)).min(1))
+        return d
 
     def _targets(self, I_train):
         """Training targets from the exact training frames: the frame basis of
@@ -445,51 +456,56 @@ class SurrogateScan:
         I_pred = shape.clamp_min_(0.0) * torch.exp(Yp[:, basis.rank:] * lsd + lmu)
         sync()
         t["predict"] = time.perf_counter() - t0
-        # judge every judge_every-th predicted frame; a failed judge sends its
-        # block of predicted frames to the exact sum
+        # Judging: the predicted frames in raster order form blocks of
+        # judge_every; each block's judged frame is the one farthest from the
+        # training frames (the hardest to interpolate), so a passing judge
+        # vouches for the easier frames around it.
         blocks = [np.arange(b, min(b + self.judge_every, len(pred_idx)))
                   for b in range(0, len(pred_idx), self.judge_every)]
-        judged = np.array([blk[0] for blk in blocks], dtype=np.int64)
+        far = self._train_distance(pred_idx)
+        judged = np.array([blk[int(np.argmax(far[blk]))] for blk in blocks], dtype=np.int64)
         t0 = time.perf_counter()
         I_j = self.exact(pred_idx[judged])
         err_j = frame_rel_error(I_pred[judged], I_j).cpu().numpy()
         sync()
         t["judge"] = time.perf_counter() - t0
         I_model = I_pred.clone() if exact_all else None
-        I_pred[torch.as_tensor(judged, device=self.dev)] = I_j
-        failed = [blk for blk, e in zip(blocks, err_j) if e > self.tol]
+        jd = torch.as_tensor(judged, device=self.dev)
+        I_pred[jd] = I_j
+        failed = [(blk, j) for blk, j, e in zip(blocks, judged, err_j) if e > self.tol]
         probes = np.zeros(0, np.int64)
         err_p = np.zeros(0)
         t0 = time.perf_counter()
-        if failed and self.refine_steps > 0:
+        rest = np.setdiff1d(np.arange(len(pred_idx)), judged)
+        if self.refine_steps > 0 and rest.size:
             # Every exact frame so far (training and judged) trains the network
-            # further; the failed blocks are predicted again and one more frame
-            # of each is judged; only blocks failing that too go to the exact sum.
+            # further, and every frame not computed exactly is predicted again
+            # by it. A block whose judge failed has one more frame judged
+            # against the refined network (its farthest remaining one); only a
+            # block failing that too goes to the exact sum.
             Tj = self._frame_targets(I_j, basis, cs, lmu, lsd)
             sel = torch.as_tensor(np.concatenate([tr, pred_idx[judged]]), device=self.dev)
             self.losses = np.concatenate([self.losses, self.net.fit_graph(
                 feats[sel].contiguous(), torch.cat([T, Tj]).contiguous(), steps=self.refine_steps,
                 lr=0.3 * self.lr, col_w=col_w)])
-            redo = np.concatenate([blk[1:] for blk in failed])
-            if redo.size:
-                Yr = self.net.predict(feats[torch.as_tensor(pred_idx[redo], device=self.dev)])
-                sh = basis.decode(self.net, (Yr[:, : basis.rank] * cs).contiguous())
-                I_pred[torch.as_tensor(redo, device=self.dev)] = \
-                    sh.clamp_min_(0.0) * torch.exp(Yr[:, basis.rank:] * lsd + lmu)
-            with_rest = [blk for blk in failed if len(blk) > 1]
-            probes = np.array([blk[len(blk) // 2] for blk in with_rest], dtype=np.int64)
+            rs = torch.as_tensor(rest, device=self.dev)
+            Yr = self.net.predict(feats[torch.as_tensor(pred_idx[rest], device=self.dev)])
+            sh = basis.decode(self.net, (Yr[:, : basis.rank] * cs).contiguous())
+            I_pred[rs] = sh.clamp_min_(0.0) * torch.exp(Yr[:, basis.rank:] * lsd + lmu)
+            if exact_all:
+                I_model[rs] = I_pred[rs]
+            with_rest = [(blk[blk != j], j) for blk, j in failed if len(blk) > 1]
+            probes = np.array([r[int(np.argmax(far[r]))] for r, _ in with_rest], dtype=np.int64)
             if probes.size:
                 I_p = self.exact(pred_idx[probes])
                 err_p = frame_rel_error(I_pred[probes], I_p).cpu().numpy()
-                if exact_all:
-                    I_model[torch.as_tensor(redo, device=self.dev)] = \
-                        I_pred[torch.as_tensor(redo, device=self.dev)]
                 I_pred[torch.as_tensor(probes, device=self.dev)] = I_p
-            still = [(blk, p) for blk, p, e in zip(with_rest, probes, err_p) if e > self.tol]
-            fb = (np.concatenate([blk[(blk != blk[0]) & (blk != p)] for blk, p in still])
-                  if still else np.zeros(0, np.int64))
+            still = [(r, p) for (r, _), p, e in zip(with_rest, probes, err_p) if e > self.tol]
+            fb = (np.concatenate([r[r != p] for r, p in still]) if still
+                  else np.zeros(0, np.int64))
         else:
-            fb = np.concatenate([blk[1:] for blk in failed]) if failed else np.zeros(0, np.int64)
+            fb = (np.concatenate([blk[blk != j] for blk, j in failed]) if failed
+                  else np.zeros(0, np.int64))
         sync()
         t["refine"] = time.perf_counter() - t0
         t0 = time.perf_counter()
