@@ -348,6 +348,16 @@ int mk_prop_cols(float *spectrum, int ny2, int nz2, double dy, double dz, double
 int mk_prop_crop_abs2(const float *grid, int ny2, int nz2, int y0, int z0, int ny, int nz,
                       float scale, float *field, float *intensity, void *stream);
 
+/* --- tensor cores (tcgen05) --------------------------------------------- */
+/* No counterpart in the reference: the self-check of the library's
+ * tensor-core path. C (128 x N, float32, row-major) = A (128 x K) . B^T with
+ * B (N x K), both row-major 16-bit (FP16, or BF16 when bf16 != 0), on one
+ * tcgen05.mma tile accumulating in tensor memory: it exercises the operand
+ * and instruction descriptors and the TMEM round trip the other tcgen05
+ * kernels use. N a multiple of 16 in [16, 256], K a multiple of 16 in
+ * [16, 128]; device pointers. */
+int mk_tc_gemm(int N, int K, int bf16, const void *A, const void *B, float *C, void *stream);
+
 /* --- scan surrogate (BF16 MLP) ------------------------------------------ */
 /* No counterpart in the reference: the learned part of the scan path. BF16
  * operands, FP32 accumulation on the tensor cores (mma.sync m16n8k16).
