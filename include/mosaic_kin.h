@@ -368,6 +368,20 @@ int mk_tc_gemm(int N, int K, int bf16, const void *A, const void *B, float *C, v
 int mk_gemm_bf16(int M, int N, int K, const void *A, long long sam, long long sak, const void *B,
                  long long sbk, long long sbn, float *C, long long ldc, const float *bias,
                  int flags, void *Cb, long long ldcb, void *stream);
+/* The same product on the Blackwell tensor cores (tcgen05.mma, FP32
+ * accumulation in tensor memory), same operand conventions, with a fused
+ * epilogue: v = A.B (+ bias[n]) (+ C[m, n] when flags & 1), ReLU (flags & 4),
+ * then zero where relu_mask[m*ldm + n] <= 0 (relu_mask non-NULL: the
+ * derivative of a ReLU layer whose outputs relu_mask holds), times
+ * row_scale[m] (non-NULL), stored at row row_map[m] of C / Cb (non-NULL;
+ * not with flags & 1). A CTA computes a 128 x 64 (N >= 2048: 128 x 128)
+ * tile through three 64-deep shared-memory stages; long-K, few-tile
+ * products (the weight gradients) split K over up to 8 CTAs that add into
+ * a zeroed C. */
+int mk_gemm_tc(int M, int N, int K, const void *A, long long sam, long long sak, const void *B,
+               long long sbk, long long sbn, float *C, long long ldc, const float *bias, int flags,
+               void *Cb, long long ldcb, const float *relu_mask, long long ldm,
+               const float *row_scale, const long long *row_map, void *stream);
 /* Inputs of the network: (x, y) and sin/cos(2 pi f_j x), sin/cos(2 pi f_j y),
  * f_j = f0 ratio^j, j < n_freq, zero-padded to `width` bf16 columns. */
 int mk_fourier_features(int n, const float *xy, int n_freq, float f0, float ratio, int width,

@@ -175,6 +175,10 @@ SIGNATURES = {
                                     ctypes.c_longlong, _vp, ctypes.c_longlong, ctypes.c_longlong,
                                     _vp, ctypes.c_longlong, _vp, ctypes.c_int, _vp,
                                     ctypes.c_longlong, _vp]),
+    "mk_gemm_tc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_longlong,
+                                  ctypes.c_longlong, _vp, ctypes.c_longlong, ctypes.c_longlong,
+                                  _vp, ctypes.c_longlong, _vp, ctypes.c_int, _vp,
+                                  ctypes.c_longlong, _vp, ctypes.c_longlong, _vp, _vp, _vp]),
     "mk_fourier_features": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_int, _vp, _vp]),
     "mk_relu_backward": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp]),

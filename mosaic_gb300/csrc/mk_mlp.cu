@@ -240,20 +240,40 @@ extern "C" int mk_relu_backward(long long n, const float *grad, const float *pre
     return MK_OK;
 }
 
-// db[n] = sum_m g[m, n]: one thread per column, fixed order.
-__global__ void mk_colsum_kernel(int M, int N, const float *__restrict__ g, float *__restrict__ db)
+// db[n] = sum_m g[m, n]: a block of 8 warps per 32 columns; warp w sums
+// rows w, w + 8, ... of its column (lane), four rows in flight, and the 8
+// partial sums are added in warp order (deterministic).
+__global__ void __launch_bounds__(256) mk_colsum_kernel(int M, int N, const float *__restrict__ g,
+                                                        float *__restrict__ db)
 {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    float s = 0.f;
-    for (int m = 0; m < M; ++m) s += g[(long long)m * N + n];
-    db[n] = s;
+    __shared__ float part[8][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = blockIdx.x * 32 + lane;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    if (n < N) {
+        int m = warp;
+        for (; m + 24 < M; m += 32) {
+            s0 += g[(long long)m * N + n];
+            s1 += g[(long long)(m + 8) * N + n];
+            s2 += g[(long long)(m + 16) * N + n];
+            s3 += g[(long long)(m + 24) * N + n];
+        }
+        for (; m < M; m += 8) s0 += g[(long long)m * N + n];
+    }
+    part[warp][lane] = (s0 + s1) + (s2 + s3);
+    __syncthreads();
+    if (warp == 0 && n < N) {
+        float s = 0.f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += part[w][lane];
+        db[n] = s;
+    }
 }
 
 extern "C" int mk_bias_grad(int M, int N, const float *g, float *db, void *stream)
 {
     MK_REQUIRE(M > 0 && N > 0 && g && db, "mk_bias_grad: bad arguments");
-    mk_colsum_kernel<<<(N + 255) / 256, 256, 0, mk_stream(stream)>>>(M, N, g, db);
+    mk_colsum_kernel<<<(N + 31) / 32, 256, 0, mk_stream(stream)>>>(M, N, g, db);
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
 }

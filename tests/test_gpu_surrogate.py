@@ -109,33 +109,37 @@ def test_frame_basis_decode_on_the_gemm(cuda):
     VV = (basis.V @ basis.V.T).cpu().numpy()
     assert np.allclose(VV, np.eye(39), atol=1e-4)
     net = MLP(4, 4, hidden=8, n_hidden=1, device=cuda)
-    Xr = basis.decode(net, basis.C.contiguous())
+    Xr = basis.decode(net, basis.coefficients(X).contiguous())
     assert float((Xr - X).abs().max()) < 1e-4
 
 
 def test_surrogate_scan_gains_over_exact(cuda):
     """A small strained crystal (2.05M atoms), 49 x 49 theta x chi grid over
     +-0.2 deg, 64 x 64 ROI: exact training frames every 4th point per axis
-    (169), the MLP for the rest, every 8th predicted frame re-judged. Every
-    frame is also computed exactly (timed: the exact-only scan), so both the
-    network's own error on every predicted frame and the gain are measured."""
+    (169 = a 13 x 13 grid), the spline + network prediction for the rest,
+    every 8th predicted frame judged. Every frame is also computed exactly
+    (timed: the exact-only scan), so the error of every returned frame, of
+    the prediction alone and of the spline alone, and the gain, are all
+    measured."""
     w = workloads.cu_bumps_scan_4m(cells=80, npix=128)
     th = np.radians(np.linspace(-0.2, 0.2, 49))
     ch = np.radians(np.linspace(-0.2, 0.2, 49))
     sc = SurrogateScan(w.beam, w.sample, w.detector, w.stage, th, ch, roi=64, stride=4,
                        judge_every=8, tol=0.02, sc_kwargs=w.sc_kwargs)
     res = sc.run(exact_all=True)
-    me, fe = res["model_err"], res["final_err"]
-    print({k: v for k, v in res.items() if k not in ("frames", "judge_err", "model_err", "final_err")},
-          "model err pct 50/90/100", np.percentile(me, [50, 90, 100]),
-          "final err pct 50/90/100", np.percentile(fe, [50, 90, 100]))
+    me, fe, be = res["model_err"], res["final_err"], res["base_err"]
+    pct = lambda x: np.percentile(x, [50, 90, 100])
+    print({k: v for k, v in res.items() if k not in ("frames", "judge_err", "judge_err_base",
+                                                      "model_err", "final_err", "base_err")},
+          "prediction err pct 50/90/100", pct(me), "spline-only", pct(be),
+          "judged held out", pct(res["judge_err"]), "spline-only", pct(res["judge_err_base"]))
     assert res["n_train"] == 169 and res["n_frames"] == 2401 and res["exact_measured"]
     assert np.isfinite(me).all() and torch.isfinite(res["frames"]).all()
-    # the trained network alone, on every predicted frame
-    assert np.median(me) < 0.01
-    assert (me <= 0.02).mean() >= 0.9
-    # after judging and fallback
-    assert (fe <= 0.02).mean() >= 0.95
-    assert res["n_fallback"] <= 6 * res["n_failed_rejudges"] and res["n_rejudged"] <= res["n_failed_judges"]
+    # every returned frame within the tolerance, and the prediction alone too
+    assert fe.max() <= 0.02 and me.max() <= 0.02
+    # the network adds to the spline on the frames it did not train on
+    assert np.percentile(res["judge_err"], 90) < np.percentile(res["judge_err_base"], 90)
+    assert res["n_fallback"] <= 7 * res["n_failed_judges"]
     # frames/s over the exact-only scan, both timed here
     assert res["gain"] > 1.5, res["gain"]
+

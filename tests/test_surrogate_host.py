@@ -1,21 +1,16 @@
-"""Host-side pieces of the scan surrogate that need no GPU: the principal
-component basis of the training frames."""
+"""Host side of the scan surrogate, on the CPU: the spline weights that
+interpolate the training frames over the motor grid."""
 import numpy as np
-import torch
 
 from mosaic_gb300 import surrogate
 
 
-def test_frame_basis_spans_the_frames():
-    rng = np.random.default_rng(2)
-    # 30 frames of 200 pixels on a 6-dimensional subspace (plus the mean)
-    Z = rng.standard_normal((30, 6)) @ rng.standard_normal((6, 200))
-    X = torch.tensor(Z + 3.0, dtype=torch.float32)
-    basis = surrogate.FrameBasis(X, 16)
-    assert basis.rank == 6
-    assert np.allclose((basis.V @ basis.V.T).numpy(), np.eye(6), atol=1e-4)
-    rec = basis.C @ basis.V + basis.mu
-    assert float((rec - X).abs().max()) < 1e-3 * float(X.abs().max())
-    # coefficients are ordered by variance
-    v = basis.C.var(0).numpy()
-    assert np.all(np.diff(v) <= 1e-6 * v[0])
+def test_spline_matrix_interpolates_cubics():
+    """The not-a-knot cubic spline through grid nodes reproduces a cubic
+    polynomial exactly, between the nodes and beyond the last one."""
+    nodes = np.arange(0, 23, 4)                     # 0, 4, ..., 20 (position 22 extrapolated)
+    W = surrogate.spline_matrix(23, nodes)
+    x = np.arange(23, dtype=np.float64)
+    f = lambda v: 0.3 * v ** 3 - 2.0 * v ** 2 + v - 5.0
+    assert np.allclose(W @ f(nodes.astype(np.float64)), f(x), rtol=1e-10, atol=1e-8)
+    assert np.allclose(surrogate.spline_matrix(5, [0, 4]) @ np.array([1.0, 3.0]), 1.0 + 0.5 * np.arange(5))
