@@ -188,43 +188,79 @@ class MLP:
         the same arithmetic and cosine schedule, without a host round trip per
         step (the step number and learning rate live in device memory,
         mk_adam_sched). Returns the final loss (1-element array)."""
-        if steps <= 0:
-            return np.zeros(0)
+        return fit_graphs([self], [X], [T], steps, lr, lr_final, [col_w])[0]
+
+    def _graph_state(self, steps, lr, lr_final):
+        """Device-side schedule and step counter of a captured training run;
+        makes the first call of its kernels outside the capture."""
         sh = engine._stream_handle
         sched = lr_final + 0.5 * (lr - lr_final) * (
             1 + np.cos(np.pi * np.arange(steps) / max(steps - 1, 1)))
         lr_d = torch.tensor(sched, dtype=torch.float32, device=self.dev)
         step0 = int(self.steps)
         counter = torch.tensor([step0], dtype=torch.int32, device=self.dev)
-        # load the step's kernels before capture (on throw-away buffers)
         tmp = torch.zeros(4, dtype=torch.float32, device=self.dev)
         check(self.L.mk_adam_sched(1, _p(tmp[0:]), _p(tmp[1:]), _p(tmp[2:]), _p(tmp[3:]), None,
                                    _p(lr_d), _p(counter), step0, 0.9, 0.999, 1e-8, 0.0, sh()))
         cnt2 = counter.clone()
         check(self.L.mk_counter_add(_p(cnt2), 1, sh()))
-        torch.cuda.synchronize(self.dev)
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g):
-            acts, posts, Y = self.forward(X)
-            loss, G, Gb = self.mse(Y, T, col_w)
-            dW, db = self.backward(acts, posts, G, Gb)
-            s = sh()
-            check(self.L.mk_adam_sched(self.P.numel(), _p(self.P), _p(self.gP), _p(self.mP),
-                                       _p(self.vP), _p(self.Pb), _p(lr_d), _p(counter), step0,
-                                       0.9, 0.999, 1e-8, 0.0, s))
-            check(self.L.mk_counter_add(_p(counter), 1, s))
-        for _ in range(int(steps)):
-            g.replay()
-        self.steps += int(steps)
-        out = np.array([float(loss)])
-        del g
-        return out
+        return lr_d, counter, step0
+
+    def _step(self, X, T, col_w, lr_d, counter, step0):
+        """One training step on the current stream (captured): returns the
+        loss as a device scalar."""
+        acts, posts, Y = self.forward(X)
+        loss, G, Gb = self.mse(Y, T, col_w)
+        self.backward(acts, posts, G, Gb)
+        s = engine._stream_handle()
+        check(self.L.mk_adam_sched(self.P.numel(), _p(self.P), _p(self.gP), _p(self.mP),
+                                   _p(self.vP), _p(self.Pb), _p(lr_d), _p(counter), step0,
+                                   0.9, 0.999, 1e-8, 0.0, s))
+        check(self.L.mk_counter_add(_p(counter), 1, s))
+        return loss
 
     def predict(self, X, chunk=4096):
         outs = []
         for i in range(0, int(X.shape[0]), chunk):
             outs.append(self.forward(X[i:i + chunk])[2])
         return torch.cat(outs)
+
+
+def fit_graphs(nets, Xs, Ts, steps=1500, lr=2e-3, lr_final=1e-4, col_ws=None):
+    """Train independent networks together: one CUDA graph holds a training
+    step of every network, each on its own stream (forked from and joined
+    back to the current one), and is replayed ``steps`` times, so the
+    networks' small kernels run side by side on the GPU. Per network the
+    arithmetic is ``MLP.fit_graph``'s. Returns each network's final loss
+    (1-element arrays)."""
+    if steps <= 0:
+        return [np.zeros(0) for _ in nets]
+    col_ws = col_ws or [None] * len(nets)
+    states = [net._graph_state(steps, lr, lr_final) for net in nets]
+    dev = nets[0].dev
+    torch.cuda.synchronize(dev)
+    cur = torch.cuda.current_stream(dev)
+    side = [torch.cuda.Stream(dev) for _ in nets[1:]]
+    g = torch.cuda.CUDAGraph()
+    losses = [None] * len(nets)
+    with torch.cuda.graph(g):
+        cap = torch.cuda.current_stream(dev)
+        for i, net in enumerate(nets):
+            st = cap if i == 0 else side[i - 1]
+            if i:
+                st.wait_stream(cap)
+            with torch.cuda.stream(st):
+                losses[i] = net._step(Xs[i], Ts[i], col_ws[i], *states[i])
+        for st in side:
+            cap.wait_stream(st)
+    for _ in range(int(steps)):
+        g.replay()
+    cur.synchronize()
+    for net in nets:
+        net.steps += int(steps)
+    out = [np.array([float(l)]) for l in losses]
+    del g
+    return out
 
 
 def fourier_features(xy, n_freq=16, device="cuda", f_max=0.5, f_min=0.25):
@@ -382,6 +418,7 @@ class SurrogateScan:
         chi0 = float(stage.motor_value[stage.motor_index("chi")])
         self.steps = [dict(mu=mu0 + self.theta[i], chi=chi0 + self.chi[j]) for i, j in self.ij]
         self._staged = None
+        self._side, self._keep = None, []
 
     def prepare(self):
         """Stage the atoms and tiles once (setup shared by every exact call,
@@ -407,6 +444,9 @@ class SurrogateScan:
         cw = (sc * sc / (sc * sc).sum() * sc.numel()).float().contiguous()
         net.fit(feats, Tf, steps=2, col_w=cw)
         net.fit_graph(feats, Tf, steps=2, col_w=cw)
+        net2 = MLP(feats.shape[1], basis.rank + 1, hidden=32, n_hidden=2, seed=self.seed + 1,
+                   device=self.dev)
+        fit_graphs([net, net2], [feats, feats], [Tf, Tf], steps=2, col_ws=[cw, cw])
         Y = 0.5 * (net.predict(feats) + net.predict(feats))
         I_pred = self._decode(net, basis, base[: T.shape[0]] + Y.double() * sc)
         err = frame_rel_error(I_pred[:4], I[:4])
@@ -457,15 +497,30 @@ class SurrogateScan:
         return basis.decode(net, D[:, :r].float().contiguous(), out=out, row_scale=scale,
                             row_map=rows, clamp=True)
 
-    def exact(self, idx):
-        """Exact intensities (len(idx), roi*roi) of the given frames, batched
-        launches of at most ``batch_frames`` frames."""
+    def exact(self, idx, first=256):
+        """Exact intensities (len(idx), roi*roi) of the given frames, in
+        batched launches of at most ``batch_frames`` frames (the first of at
+        most ``first``). The batches' sums run on a side stream, so that the
+        set-up of the next batch (frame geometry on the host, pixel arrays
+        and bounds on the device) overlaps the previous batch's sum; the
+        small first batch keeps the set-up that cannot overlap short. The
+        current stream waits for the result."""
         idx = np.asarray(idx)
+        P = self.roi * self.roi
         if idx.size == 0:
-            return torch.zeros((0, self.roi * self.roi), dtype=torch.float32, device=self.dev)
-        outs = []
-        for b in range(0, idx.size, self.batch_frames):
-            sub = idx[b: b + self.batch_frames]
+            return torch.zeros((0, P), dtype=torch.float32, device=self.dev)
+        if self._side is None:
+            self._side = torch.cuda.Stream(self.dev)
+        side = self._side
+        side.synchronize()                  # the previous call's batches are done:
+        self._keep = []                     # their buffers may go
+        cur = torch.cuda.current_stream(self.dev)
+        out = torch.empty((idx.size, P), dtype=torch.float32, device=self.dev)
+        cuts = [0, min(int(first), idx.size)]
+        while cuts[-1] < idx.size:
+            cuts.append(min(cuts[-1] + self.batch_frames, idx.size))
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            sub = idx[a:b]
             frames = frames_from_motors(self.stage, self.detector, [self.steps[i] for i in sub],
                                         [self.roi] * len(sub))
             if len(frames) == 1:           # a one-frame batch still goes through the scan path
@@ -474,9 +529,20 @@ class SurrogateScan:
             scan = BatchedScan(self.beam, self.sample, frames, staged=self._staged, tune=False,
                                **self.kw)
             self._staged = self._staged or scan
-            out, _ = scan.run()
-            outs.append((out * out).sum(1).reshape(len(frames), -1)[: len(sub)].float())
-        return torch.cat(outs)
+            side.wait_stream(cur)
+            with torch.cuda.stream(side):
+                f, _ = scan.run(side)
+                out[a:b] = (f * f).sum(1).reshape(len(frames), -1)[: len(sub)].float()
+                done = torch.cuda.Event()
+                done.record(side)
+            # a batch's buffers stay alive until the side stream is done with
+            # them; two batches back it long is
+            while len(self._keep) >= 2:
+                self._keep[0][1].synchronize()
+                self._keep.pop(0)
+            self._keep.append((scan, done))
+        cur.wait_stream(side)
+        return out
 
     def run(self, verify=0, exact_all=False):
         """Run the scan. ``exact_all`` also computes every frame exactly (the
@@ -527,15 +593,16 @@ class SurrogateScan:
         scale = (R_j.std(0) if len(judged) > 1 else R_j.abs().amax(0)).clamp_min(1e-12)
         col_w = (scale * scale / (scale * scale).sum() * (r + 1)).float().contiguous()
         feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=self.f_max, f_min=self.f_min)
-        self.nets, self.losses = [], []
+        self.nets, Xs, Ts = [], [], []
         for f in (0, 1):
             rows = np.concatenate([tr, pred_idx[judged[fold == f]]])
-            Tf = (torch.cat([R_tr, R_j[torch.as_tensor(fold == f, device=self.dev)]]) / scale
-                  ).float().contiguous()
-            net = MLP(feats.shape[1], r + 1, self.hidden, self.n_hidden, self.seed + f, self.dev)
-            self.losses.append(net.fit_graph(feats[torch.as_tensor(rows, device=self.dev)].contiguous(),
-                                             Tf, steps=self.fit_steps, lr=self.lr, col_w=col_w))
-            self.nets.append(net)
+            Ts.append((torch.cat([R_tr, R_j[torch.as_tensor(fold == f, device=self.dev)]]) / scale
+                       ).float().contiguous())
+            Xs.append(feats[torch.as_tensor(rows, device=self.dev)].contiguous())
+            self.nets.append(MLP(feats.shape[1], r + 1, self.hidden, self.n_hidden, self.seed + f,
+                                 self.dev))
+        self.losses = fit_graphs(self.nets, Xs, Ts, steps=self.fit_steps, lr=self.lr,
+                                 col_ws=[col_w, col_w])
         sync()
         t["fit"] = time.perf_counter() - t0
         # Every judged frame is predicted by the network that did not train on
@@ -604,6 +671,8 @@ class SurrogateScan:
             res.update(exact_seconds=n * t["exact"] / (len(tr) + len(judged)), exact_measured=False)
         res["exact_frames_per_s"] = n / res["exact_seconds"]
         res["gain"] = res["exact_seconds"] / total
+        sync()
+        self._keep = []
         if verify and not exact_all:
             rng = np.random.default_rng(self.seed + 1)
             unjudged = np.setdiff1d(np.arange(len(pred_idx)), np.concatenate([judged, fb]))
