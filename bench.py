@@ -18,10 +18,12 @@ shards into independent exposures; there is no data-path collective) and
 `value` is the sum over ranks of terms / max-over-ranks time ("weak" scaling).
 
 Besides the timed steps, rank 0 reports (outside the timed region): the FP64
-plain kernel on a pixel subset (speed and error reference), the batched scan
-(48 frames of the 4M-atom rocking scan in one graph-captured launch), the
-surrogate-assisted 101 x 101 theta x chi scan (frames/s against the exact
-batched scan) and the CPU baseline.
+plain kernel on 1,029 pixels spread over the whole detector (speed and error
+reference), the batched scan (all 724 frames of the 4M-atom rocking scan in
+one graph-captured launch), the surrogate-assisted 101 x 101 theta x chi scan
+(frames/s against the exact batched scan of all 10,201 frames, which is run
+and timed too, and every returned frame's error against it) and the CPU
+baseline.
 
 --impl reference times the reference's CPU implementation on the host cores
 (its own compute_scattering_cffi compiled from source into oracle/_ref, or,
@@ -661,9 +663,11 @@ def main():
                     help="skip the surrogate-assisted scan leg (101 x 101 frames)")
     ap.add_argument("--surrogate-verify", type=int, default=64,
                     help="unjudged predicted frames checked against the exact sum (untimed)")
-    ap.add_argument("--surrogate-exact-all", action="store_true",
+    ap.add_argument("--surrogate-exact-all", action=argparse.BooleanOptionalAction, default=True,
                     help="also compute every frame exactly: the measured exact-only scan time "
-                         "and the error of every frame (adds the exact scan's ~2.5 min)")
+                         "and the error of every returned frame (the exact scan takes ~2 min; "
+                         "--no-surrogate-exact-all estimates it from the exact launch instead "
+                         "and checks --surrogate-verify sampled frames)")
     ap.add_argument("--no-pairs", action="store_true",
                     help="one sin/cos per term (the pixel-pair and quad forms off)")
     ap.add_argument("--launch", default="",

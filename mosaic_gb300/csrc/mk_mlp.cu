@@ -240,25 +240,28 @@ extern "C" int mk_relu_backward(long long n, const float *grad, const float *pre
     return MK_OK;
 }
 
-// db[n] = sum_m g[m, n]: a block of 8 warps per 32 columns; warp w sums
-// rows w, w + 8, ... of its column (lane), four rows in flight, and the 8
-// partial sums are added in warp order (deterministic).
+// db[n] = sum_m g[m, n]: block (x, y) sums 32 columns over the y-th slice
+// of rows (8 warps, warp w taking rows w, w + 8, ..., four in flight), adds
+// its 8 warp sums and then adds the result into db (zeroed first) with an
+// atomic add: many blocks keep enough loads in flight for a tall, narrow g.
+#define MK_COLSUM_ROWS 128
 __global__ void __launch_bounds__(256) mk_colsum_kernel(int M, int N, const float *__restrict__ g,
                                                         float *__restrict__ db)
 {
     __shared__ float part[8][33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = blockIdx.x * 32 + lane;
+    const int m_lo = blockIdx.y * MK_COLSUM_ROWS, m_hi = min(M, m_lo + MK_COLSUM_ROWS);
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
     if (n < N) {
-        int m = warp;
-        for (; m + 24 < M; m += 32) {
+        int m = m_lo + warp;
+        for (; m + 24 < m_hi; m += 32) {
             s0 += g[(long long)m * N + n];
             s1 += g[(long long)(m + 8) * N + n];
             s2 += g[(long long)(m + 16) * N + n];
             s3 += g[(long long)(m + 24) * N + n];
         }
-        for (; m < M; m += 8) s0 += g[(long long)m * N + n];
+        for (; m < m_hi; m += 8) s0 += g[(long long)m * N + n];
     }
     part[warp][lane] = (s0 + s1) + (s2 + s3);
     __syncthreads();
@@ -266,14 +269,18 @@ __global__ void __launch_bounds__(256) mk_colsum_kernel(int M, int N, const floa
         float s = 0.f;
 #pragma unroll
         for (int w = 0; w < 8; ++w) s += part[w][lane];
-        db[n] = s;
+        atomicAdd(&db[n], s);
     }
 }
 
 extern "C" int mk_bias_grad(int M, int N, const float *g, float *db, void *stream)
 {
     MK_REQUIRE(M > 0 && N > 0 && g && db, "mk_bias_grad: bad arguments");
-    mk_colsum_kernel<<<(N + 31) / 32, 256, 0, mk_stream(stream)>>>(M, N, g, db);
+    dim3 grid((N + 31) / 32, (M + MK_COLSUM_ROWS - 1) / MK_COLSUM_ROWS);
+    MK_REQUIRE(grid.y < 65536, "mk_bias_grad: M too large");
+    cudaStream_t st = mk_stream(stream);
+    MK_CHECK_CUDA(cudaMemsetAsync(db, 0, sizeof(float) * (size_t)N, st));
+    mk_colsum_kernel<<<grid, 256, 0, st>>>(M, N, g, db);
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
 }

@@ -591,15 +591,19 @@ class SurrogateScan:
         R_tr = T_tr - base[torch.as_tensor(tr, device=self.dev)]
         R_j = T_j - base[torch.as_tensor(pred_idx[judged], device=self.dev)]
         scale = (R_j.std(0) if len(judged) > 1 else R_j.abs().amax(0)).clamp_min(1e-12)
-        col_w = (scale * scale / (scale * scale).sum() * (r + 1)).float().contiguous()
+        # network outputs padded to a multiple of 8 (16-byte rows for the
+        # GEMMs); the padding columns carry zero targets and zero loss weight
+        n_out = (r + 1 + 7) // 8 * 8
+        col_w = torch.zeros(n_out, dtype=torch.float32, device=self.dev)
+        col_w[: r + 1] = (scale * scale / (scale * scale).sum() * (r + 1)).float()
         feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=self.f_max, f_min=self.f_min)
         self.nets, Xs, Ts = [], [], []
         for f in (0, 1):
             rows = np.concatenate([tr, pred_idx[judged[fold == f]]])
-            Ts.append((torch.cat([R_tr, R_j[torch.as_tensor(fold == f, device=self.dev)]]) / scale
-                       ).float().contiguous())
+            Tf = (torch.cat([R_tr, R_j[torch.as_tensor(fold == f, device=self.dev)]]) / scale).float()
+            Ts.append(torch.nn.functional.pad(Tf, (0, n_out - (r + 1))).contiguous())
             Xs.append(feats[torch.as_tensor(rows, device=self.dev)].contiguous())
-            self.nets.append(MLP(feats.shape[1], r + 1, self.hidden, self.n_hidden, self.seed + f,
+            self.nets.append(MLP(feats.shape[1], n_out, self.hidden, self.n_hidden, self.seed + f,
                                  self.dev))
         self.losses = fit_graphs(self.nets, Xs, Ts, steps=self.fit_steps, lr=self.lr,
                                  col_ws=[col_w, col_w])
@@ -609,7 +613,7 @@ class SurrogateScan:
         # it; the other frames by the mean of the two.
         t0 = time.perf_counter()
         F = feats[torch.as_tensor(pred_idx, device=self.dev)]
-        Y0, Y1 = (net.predict(F) for net in self.nets)
+        Y0, Y1 = (net.predict(F)[:, : r + 1] for net in self.nets)
         corr = 0.5 * (Y0 + Y1)
         j0 = torch.as_tensor(judged[fold == 0], device=self.dev)
         j1 = torch.as_tensor(judged[fold == 1], device=self.dev)
