@@ -382,13 +382,27 @@ int mk_gemm_tc(int M, int N, int K, const void *A, long long sam, long long sak,
                long long sbk, long long sbn, float *C, long long ldc, const float *bias, int flags,
                void *Cb, long long ldcb, const float *relu_mask, long long ldm,
                const float *row_scale, const long long *row_map, void *stream);
+/* mk_gemm_tc over `groups` independent products of the same shape in one
+ * launch (grid z = group): group q reads A + q*gs[0], B + q*gs[1], bias +
+ * q*gs[4], relu_mask + q*gs[5] and writes C + q*gs[2], Cb + q*gs[3], with
+ * gs = group_strides (6 element strides, host array; a stride of 0 shares
+ * an input between groups). row_scale / row_map need groups == 1. */
+int mk_gemm_tc_groups(int groups, const long long *group_strides, int M, int N, int K,
+                      const void *A, long long sam, long long sak, const void *B, long long sbk,
+                      long long sbn, float *C, long long ldc, const float *bias, int flags,
+                      void *Cb, long long ldcb, const float *relu_mask, long long ldm,
+                      const float *row_scale, const long long *row_map, void *stream);
 /* Inputs of the network: (x, y) and sin/cos(2 pi f_j x), sin/cos(2 pi f_j y),
  * f_j = f0 ratio^j, j < n_freq, zero-padded to `width` bf16 columns. */
 int mk_fourier_features(int n, const float *xy, int n_freq, float f0, float ratio, int width,
                         void *out, void *stream);
 int mk_relu_backward(long long n, const float *grad, const float *pre, float *gout,
                      void *gout_bf16, void *stream);
+/* db[n] = sum over rows m of g[m, n] (g row-major M x N); the _groups form
+ * does `groups` of them at once: g + q*g_stride -> db + q*db_stride. */
 int mk_bias_grad(int M, int N, const float *g, float *db, void *stream);
+int mk_bias_grad_groups(int groups, int M, int N, const float *g, long long g_stride, float *db,
+                        long long db_stride, void *stream);
 /* MSE over n entries: grad = 2(y - t)/n (float and/or bf16), partial sums of
  * squares per 256-block in `partials` (ceil(n/256) doubles). */
 int mk_mse(long long n, const float *y, const float *t, float *grad, void *grad_bf16,

@@ -179,6 +179,13 @@ SIGNATURES = {
                                   ctypes.c_longlong, _vp, ctypes.c_longlong, ctypes.c_longlong,
                                   _vp, ctypes.c_longlong, _vp, ctypes.c_int, _vp,
                                   ctypes.c_longlong, _vp, ctypes.c_longlong, _vp, _vp, _vp]),
+    "mk_gemm_tc_groups": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         _vp, ctypes.c_longlong, ctypes.c_longlong, _vp,
+                                         ctypes.c_longlong, ctypes.c_longlong, _vp,
+                                         ctypes.c_longlong, _vp, ctypes.c_int, _vp,
+                                         ctypes.c_longlong, _vp, ctypes.c_longlong, _vp, _vp, _vp]),
+    "mk_bias_grad_groups": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
+                                           ctypes.c_longlong, _vp, ctypes.c_longlong, _vp]),
     "mk_fourier_features": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_int, _vp, _vp]),
     "mk_relu_backward": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _vp, _vp]),

@@ -48,6 +48,8 @@ struct MkTcGemm {
     long long ldm;
     const float *row_scale;     // multiplies row m
     const long long *row_map;   // output row of row m
+    int slices;                 // split-K slices per group (gridDim.z = groups * slices)
+    long long gA, gB, gC, gCb, gbias, gmask;   // element strides between groups
 };
 
 // 16-byte asynchronous global -> shared copy; bytes beyond src_bytes are
@@ -197,9 +199,17 @@ __global__ void __launch_bounds__(MK_TCG_NT) mk_gemm_tc_kernel(MkTcGemm g, int *
     constexpr uint32_t SBO = (MK_TCG_BK / 8) * 128;                 // between 8-row groups
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.y * MK_TCG_BM, n0 = blockIdx.x * BN;
-    const int k_lo = blockIdx.z * g.k_per_slice;
+    const int grp = blockIdx.z / g.slices, slice = blockIdx.z - grp * g.slices;
+    const int k_lo = slice * g.k_per_slice;
     const int k_hi = min(g.K, k_lo + g.k_per_slice);
     const int nchunks = k_hi > k_lo ? (k_hi - k_lo + MK_TCG_BK - 1) / MK_TCG_BK : 0;
+    // this CTA's group of the batched product
+    g.A += grp * g.gA;
+    g.B += grp * g.gB;
+    if (g.C) g.C += grp * g.gC;
+    if (g.Cb) g.Cb += grp * g.gCb;
+    if (g.bias) g.bias += grp * g.gbias;
+    if (g.mask) g.mask += grp * g.gmask;
 
     if (warp == 0) mk_tmem_alloc(tmem_slot, NCOLS);
     if (tid == 0) {
@@ -284,7 +294,7 @@ __global__ void __launch_bounds__(MK_TCG_NT) mk_gemm_tc_kernel(MkTcGemm g, int *
         const bool row_ok = m < g.M;
         const long long orow = row_ok ? (g.row_map ? g.row_map[m] : (long long)m) : 0;
         const float rs = (row_ok && g.row_scale) ? g.row_scale[m] : 1.f;
-        const bool split = gridDim.z > 1;
+        const bool split = g.slices > 1;
         const bool c_vec = g.C && ((uintptr_t)g.C & 15) == 0 && (g.ldc & 3) == 0;
         const bool b_vec = g.bias && ((uintptr_t)g.bias & 15) == 0;
         const bool m_vec = g.mask && ((uintptr_t)g.mask & 15) == 0 && (g.ldm & 3) == 0;
@@ -394,11 +404,12 @@ static int mk_tcg_launch(const MkTcGemm &g, dim3 grid, cudaStream_t st, int *sta
     return MK_OK;
 }
 
-extern "C" int mk_gemm_tc(int M, int N, int K, const void *A, long long sam, long long sak,
-                          const void *B, long long sbk, long long sbn, float *C, long long ldc,
-                          const float *bias, int flags, void *Cb, long long ldcb,
-                          const float *relu_mask, long long ldm, const float *row_scale,
-                          const long long *row_map, void *stream)
+extern "C" int mk_gemm_tc_groups(int groups, const long long *group_strides, int M, int N, int K,
+                                 const void *A, long long sam, long long sak, const void *B,
+                                 long long sbk, long long sbn, float *C, long long ldc,
+                                 const float *bias, int flags, void *Cb, long long ldcb,
+                                 const float *relu_mask, long long ldm, const float *row_scale,
+                                 const long long *row_map, void *stream)
 {
     MK_REQUIRE(M > 0 && N > 0 && K > 0 && A && B, "mk_gemm_tc: bad shape or null operand");
     MK_REQUIRE(C || Cb, "mk_gemm_tc: no output");
@@ -407,6 +418,15 @@ extern "C" int mk_gemm_tc(int M, int N, int K, const void *A, long long sam, lon
     MK_REQUIRE(!(flags & MK_GEMM_ACCUMULATE) || !row_map,
                "mk_gemm_tc: accumulate reads row m of C; it cannot be combined with row_map");
     MK_REQUIRE(!relu_mask || ldm >= N, "mk_gemm_tc: mask row stride below N");
+    MK_REQUIRE(groups >= 1 && groups <= 1024, "mk_gemm_tc: groups must be in [1, 1024]");
+    long long gs[6] = {0, 0, 0, 0, 0, 0};
+    if (groups > 1) {
+        MK_REQUIRE(group_strides, "mk_gemm_tc: group strides needed for groups > 1");
+        for (int i = 0; i < 6; ++i) gs[i] = group_strides[i];
+        MK_REQUIRE((!C || gs[2] != 0) && (!Cb || gs[3] != 0),
+                   "mk_gemm_tc: groups must write to different outputs");
+        MK_REQUIRE(!row_scale && !row_map, "mk_gemm_tc: row_scale / row_map need groups == 1");
+    }
     cudaStream_t st = mk_stream(stream);
     mk_register_status_reader(mk_tcg_read_status);
     int *status = nullptr;
@@ -423,11 +443,13 @@ extern "C" int mk_gemm_tc(int M, int N, int K, const void *A, long long sam, lon
     g.C = C; g.ldc = ldc; g.bias = bias;
     g.Cb = static_cast<__nv_bfloat16 *>(Cb); g.ldcb = ldcb;
     g.mask = relu_mask; g.ldm = ldm; g.row_scale = row_scale; g.row_map = row_map;
+    g.gA = gs[0]; g.gB = gs[1]; g.gC = gs[2]; g.gCb = gs[3]; g.gbias = gs[4]; g.gmask = gs[5];
     g.k_per_slice = (K + MK_TCG_BK - 1) / MK_TCG_BK * MK_TCG_BK;
+    g.slices = 1;
     // Few output tiles and a long K (the weight gradients: K = batch):
     // split K over up to 8 slices that add into C, when the epilogue is a
     // plain store or accumulate into C.
-    const int tiles = (int)(grid.x * grid.y);
+    const int tiles = (int)(grid.x * grid.y) * groups;
     if (tiles < 64 && K >= 4 * MK_TCG_BK && C && !Cb && !relu_mask && !row_scale && !row_map &&
         !(flags & (MK_GEMM_BIAS | MK_GEMM_RELU))) {
         const int chunks = (K + MK_TCG_BK - 1) / MK_TCG_BK;
@@ -435,12 +457,24 @@ extern "C" int mk_gemm_tc(int M, int N, int K, const void *A, long long sam, lon
         if (z > 1) {
             const int per = (chunks + z - 1) / z;
             g.k_per_slice = per * MK_TCG_BK;
-            z = (chunks + per - 1) / per;               // every slice non-empty
-            grid.z = (unsigned)z;
+            g.slices = (chunks + per - 1) / per;        // every slice non-empty
             if (!(flags & MK_GEMM_ACCUMULATE))
-                MK_CHECK_CUDA(cudaMemset2DAsync(C, sizeof(float) * (size_t)ldc, 0,
-                                                sizeof(float) * (size_t)N, (size_t)M, st));
+                for (int q = 0; q < groups; ++q)
+                    MK_CHECK_CUDA(cudaMemset2DAsync(C + q * gs[2], sizeof(float) * (size_t)ldc, 0,
+                                                    sizeof(float) * (size_t)N, (size_t)M, st));
         }
     }
+    MK_REQUIRE((long long)groups * g.slices < 65536, "mk_gemm_tc: too many groups");
+    grid.z = (unsigned)(groups * g.slices);
     return bn == 128 ? mk_tcg_launch<128>(g, grid, st, status) : mk_tcg_launch<64>(g, grid, st, status);
+}
+
+extern "C" int mk_gemm_tc(int M, int N, int K, const void *A, long long sam, long long sak,
+                          const void *B, long long sbk, long long sbn, float *C, long long ldc,
+                          const float *bias, int flags, void *Cb, long long ldcb,
+                          const float *relu_mask, long long ldm, const float *row_scale,
+                          const long long *row_map, void *stream)
+{
+    return mk_gemm_tc_groups(1, nullptr, M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, flags, Cb,
+                             ldcb, relu_mask, ldm, row_scale, row_map, stream);
 }

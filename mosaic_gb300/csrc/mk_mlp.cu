@@ -246,9 +246,12 @@ extern "C" int mk_relu_backward(long long n, const float *grad, const float *pre
 // atomic add: many blocks keep enough loads in flight for a tall, narrow g.
 #define MK_COLSUM_ROWS 128
 __global__ void __launch_bounds__(256) mk_colsum_kernel(int M, int N, const float *__restrict__ g,
-                                                        float *__restrict__ db)
+                                                        long long g_stride, float *__restrict__ db,
+                                                        long long db_stride)
 {
     __shared__ float part[8][33];
+    g += blockIdx.z * g_stride;             // group blockIdx.z
+    db += blockIdx.z * db_stride;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = blockIdx.x * 32 + lane;
     const int m_lo = blockIdx.y * MK_COLSUM_ROWS, m_hi = min(M, m_lo + MK_COLSUM_ROWS);
@@ -273,16 +276,24 @@ __global__ void __launch_bounds__(256) mk_colsum_kernel(int M, int N, const floa
     }
 }
 
-extern "C" int mk_bias_grad(int M, int N, const float *g, float *db, void *stream)
+extern "C" int mk_bias_grad_groups(int groups, int M, int N, const float *g, long long g_stride,
+                                   float *db, long long db_stride, void *stream)
 {
-    MK_REQUIRE(M > 0 && N > 0 && g && db, "mk_bias_grad: bad arguments");
-    dim3 grid((N + 31) / 32, (M + MK_COLSUM_ROWS - 1) / MK_COLSUM_ROWS);
-    MK_REQUIRE(grid.y < 65536, "mk_bias_grad: M too large");
+    MK_REQUIRE(groups >= 1 && M > 0 && N > 0 && g && db, "mk_bias_grad: bad arguments");
+    MK_REQUIRE(groups == 1 || db_stride >= N, "mk_bias_grad: groups' gradients overlap");
+    dim3 grid((N + 31) / 32, (M + MK_COLSUM_ROWS - 1) / MK_COLSUM_ROWS, groups);
+    MK_REQUIRE(grid.y < 65536 && groups < 65536, "mk_bias_grad: M or groups too large");
     cudaStream_t st = mk_stream(stream);
-    MK_CHECK_CUDA(cudaMemsetAsync(db, 0, sizeof(float) * (size_t)N, st));
-    mk_colsum_kernel<<<grid, 256, 0, st>>>(M, N, g, db);
+    for (int q = 0; q < groups; ++q)
+        MK_CHECK_CUDA(cudaMemsetAsync(db + q * db_stride, 0, sizeof(float) * (size_t)N, st));
+    mk_colsum_kernel<<<grid, 256, 0, st>>>(M, N, g, g_stride, db, db_stride);
     MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
+}
+
+extern "C" int mk_bias_grad(int M, int N, const float *g, float *db, void *stream)
+{
+    return mk_bias_grad_groups(1, M, N, g, 0, db, 0, stream);
 }
 
 // Mean squared error over the n entries, each weighted by its column's

@@ -55,64 +55,96 @@ def _p(t):
 
 class MLP:
     """Fully connected ReLU network, BF16 weights (FP32 masters), FP32
-    accumulation. All parameters live in one flat FP32 buffer (with its BF16
-    copy, Adam moments and gradient), so one Adam launch updates them all;
-    ``W[l]`` (N, K) and ``b[l]`` (N) are views into it."""
+    accumulation; ``groups`` independent networks of the same shape trained
+    and evaluated together (every GEMM and bias-gradient launch serves all
+    of them: grid z = network). All parameters live in one flat FP32 buffer
+    (with its BF16 copy, Adam moments and gradient), so one Adam launch
+    updates them all; ``W[l]`` (N, K) and ``b[l]`` (N) are views into it,
+    with a leading group axis when groups > 1."""
 
-    def __init__(self, n_in, n_out, hidden=256, n_hidden=4, seed=0, device="cuda"):
+    def __init__(self, n_in, n_out, hidden=256, n_hidden=4, seed=0, device="cuda", groups=1):
         self.L = engine._require_cuda()
         self.dev = torch.device(device)
+        self.G = int(groups)
         self.dims = [int(n_in)] + [int(hidden)] * int(n_hidden) + [int(n_out)]
         shapes = [(self.dims[l + 1], self.dims[l]) for l in range(len(self.dims) - 1)]
-        n_w = [N * K for N, K in shapes]
-        n_b = [N for N, _ in shapes]
-        # weights first, each starting on a 16-byte boundary of the bf16 copy
+        nl = len(shapes)
+        pad8 = lambda n: (n + 7) // 8 * 8      # 16-byte boundaries of the bf16 copy
+        self._wpad = [pad8(N * K) for N, K in shapes]
+        self._bpad = [pad8(N) for N, _ in shapes]
         offs, o = [], 0
-        for n in n_w + n_b:
+        for n in self._wpad + self._bpad:      # layer blocks of G networks each
             offs.append(o)
-            o += (n + 7) // 8 * 8
+            o += self.G * n
         total = o
         f32 = dict(dtype=torch.float32, device=self.dev)
         self.P = torch.zeros(total, **f32)
         self.Pb = torch.zeros(total, dtype=torch.bfloat16, device=self.dev)
         self.mP, self.vP, self.gP = (torch.zeros(total, **f32) for _ in range(3))
-        nl = len(shapes)
-        view = lambda buf, l, shape: buf[offs[l]: offs[l] + int(np.prod(shape))].view(*shape)
-        self.W = [view(self.P, l, shapes[l]) for l in range(nl)]
-        self.Wb = [view(self.Pb, l, shapes[l]) for l in range(nl)]
-        self.b = [view(self.P, nl + l, (n_b[l],)) for l in range(nl)]
-        self.dW = [view(self.gP, l, shapes[l]) for l in range(nl)]
-        self.db = [view(self.gP, nl + l, (n_b[l],)) for l in range(nl)]
-        rng = np.random.default_rng(seed)
-        for l, (N, K) in enumerate(shapes):
-            std = np.sqrt((1.0 if l == nl - 1 else 2.0) / K)
-            self.W[l].copy_(torch.tensor(rng.standard_normal((N, K)) * std, **f32))
+        G = self.G
+
+        def view(buf, i, shape, gstride):
+            if G == 1:
+                return buf[offs[i]: offs[i] + int(np.prod(shape))].view(*shape)
+            st = [gstride] + [int(np.prod(shape[j + 1:])) for j in range(len(shape))]
+            return torch.as_strided(buf, (G,) + tuple(shape), st, offs[i])
+
+        self.W = [view(self.P, l, shapes[l], self._wpad[l]) for l in range(nl)]
+        self.Wb = [view(self.Pb, l, shapes[l], self._wpad[l]) for l in range(nl)]
+        self.b = [view(self.P, nl + l, (shapes[l][0],), self._bpad[l]) for l in range(nl)]
+        self.dW = [view(self.gP, l, shapes[l], self._wpad[l]) for l in range(nl)]
+        self.db = [view(self.gP, nl + l, (shapes[l][0],), self._bpad[l]) for l in range(nl)]
+        for g in range(G):
+            rng = np.random.default_rng(seed + g)
+            for l, (N, K) in enumerate(shapes):
+                std = np.sqrt((1.0 if l == nl - 1 else 2.0) / K)
+                w = self.W[l] if G == 1 else self.W[l][g]
+                w.copy_(torch.tensor(rng.standard_normal((N, K)) * std, **f32))
         self.Pb.copy_(self.P.to(torch.bfloat16))
         self.steps = 0
 
     @property
     def n_params(self):
-        return sum(w.numel() + b.numel() for w, b in zip(self.W, self.b))
+        """Parameters of one network of the group."""
+        return sum(w[0].numel() + b[0].numel() if self.G > 1 else w.numel() + b.numel()
+                   for w, b in zip(self.W, self.b))
 
     def _gemm(self, M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, flags, Cb, ldcb, mask=None,
-              ldm=0, row_scale=None, row_map=None):
-        """C (+)= A B on the tcgen05 GEMM (mk_gemm_tc), fused epilogue."""
-        check(self.L.mk_gemm_tc(M, N, K, _p(A), sam, sak, _p(B), sbk, sbn, _p(C), ldc, _p(bias),
-                                flags, _p(Cb), ldcb, _p(mask), ldm, _p(row_scale), _p(row_map),
-                                engine._stream_handle()))
+              ldm=0, row_scale=None, row_map=None, gstrides=None):
+        """C (+)= A B on the tcgen05 GEMM, fused epilogue; ``gstrides`` (A, B,
+        C, Cb, bias, mask element strides) runs the G networks' products in
+        one launch."""
+        if gstrides is None or self.G == 1:
+            check(self.L.mk_gemm_tc(M, N, K, _p(A), sam, sak, _p(B), sbk, sbn, _p(C), ldc, _p(bias),
+                                    flags, _p(Cb), ldcb, _p(mask), ldm, _p(row_scale), _p(row_map),
+                                    engine._stream_handle()))
+        else:
+            gs = (ctypes.c_longlong * 6)(*[int(v) for v in gstrides])
+            check(self.L.mk_gemm_tc_groups(self.G, gs, M, N, K, _p(A), sam, sak, _p(B), sbk, sbn,
+                                           _p(C), ldc, _p(bias), flags, _p(Cb), ldcb, _p(mask), ldm,
+                                           None, None, engine._stream_handle()))
+
+    def _new(self, B, N, dtype):
+        shape = (B, N) if self.G == 1 else (self.G, B, N)
+        return torch.empty(shape, dtype=dtype, device=self.dev)
 
     def forward(self, X):
-        """X (B, n_in) bf16 -> (layer inputs (bf16), hidden post-activations (f32), Y (f32))."""
-        B = int(X.shape[0])
+        """X (B, n_in) bf16 -- shared by the G networks -- or (G, B, n_in) ->
+        (layer inputs (bf16), hidden post-activations (f32), Y (f32)), each
+        with a leading group axis when G > 1."""
+        B = int(X.shape[-2])
+        shared = X.dim() == 2
         acts, posts = [X], []
         Y = None
         for l in range(len(self.dims) - 1):
             K, N = self.dims[l], self.dims[l + 1]
             last = l == len(self.dims) - 2
-            C = torch.empty((B, N), dtype=torch.float32, device=self.dev)
-            Cb = None if last else torch.empty((B, N), dtype=torch.bfloat16, device=self.dev)
+            C = self._new(B, N, torch.float32)
+            Cb = None if last else self._new(B, N, torch.bfloat16)
+            ga = 0 if (l == 0 and shared) else B * K
             self._gemm(B, N, K, acts[-1], K, 1, self.Wb[l], 1, K, C, N, self.b[l],
-                       GEMM_BIAS | (0 if last else GEMM_RELU), Cb, N)
+                       GEMM_BIAS | (0 if last else GEMM_RELU), Cb, N,
+                       gstrides=(ga, self._wpad[l], B * N, B * N, self._bpad[l], 0))
             if last:
                 Y = C
             else:
@@ -125,31 +157,41 @@ class MLP:
         into the flat gradient buffer: returns its (dW, db) views. The input
         gradient of a hidden layer carries the ReLU derivative in its
         GEMM's epilogue (the layer's outputs as the mask)."""
-        B = int(G.shape[0])
+        B = int(G.shape[-2])
         for l in range(len(self.dims) - 2, -1, -1):
             K, N = self.dims[l], self.dims[l + 1]
-            self._gemm(N, K, B, Gb, 1, N, acts[l], K, 1, self.dW[l], K, None, 0, None, 0)
-            check(self.L.mk_bias_grad(B, N, _p(G), _p(self.db[l]), engine._stream_handle()))
+            gx = 0 if (l == 0 and acts[0].dim() == 2) else B * K
+            self._gemm(N, K, B, Gb, 1, N, acts[l], K, 1, self.dW[l], K, None, 0, None, 0,
+                       gstrides=(B * N, gx, self._wpad[l], 0, 0, 0))
+            check(self.L.mk_bias_grad_groups(self.G, B, N, _p(G), B * N, _p(self.db[l]),
+                                             self._bpad[l], engine._stream_handle()))
             if l == 0:
                 break
-            G2 = torch.empty((B, K), dtype=torch.float32, device=self.dev)
-            Gb2 = torch.empty((B, K), dtype=torch.bfloat16, device=self.dev)
+            G2 = self._new(B, K, torch.float32)
+            Gb2 = self._new(B, K, torch.bfloat16)
             self._gemm(B, K, N, Gb, N, 1, self.Wb[l], K, 1, G2, K, None, 0, Gb2, K,
-                       mask=posts[l - 1], ldm=K)
+                       mask=posts[l - 1], ldm=K,
+                       gstrides=(B * N, self._wpad[l], B * K, B * K, 0, B * K))
             G, Gb = G2, Gb2
         return self.dW, self.db
 
     def mse(self, Y, T, col_w=None):
         """(loss as a device scalar, dL/dY f32, bf16); ``col_w`` weights the
-        output columns (float32 device vector)."""
+        output columns (float32 device vector). With G networks the loss is
+        the sum of theirs and each network's gradient is its own loss's."""
         n = Y.numel()
         G = torch.empty_like(Y)
         Gb = torch.empty(Y.shape, dtype=torch.bfloat16, device=self.dev)
         part = torch.empty((n + 255) // 256, dtype=torch.float64, device=self.dev)
-        if col_w is None:
+        if col_w is None and self.G == 1:
             check(self.L.mk_mse(n, _p(Y), _p(T), _p(G), _p(Gb), _p(part), engine._stream_handle()))
         else:
-            check(self.L.mk_mse_weighted(n, int(Y.shape[1]), _p(Y), _p(T), _p(col_w), _p(G),
+            # 2 w (y - t) / n over all G networks' entries: weights times G
+            # make each network's gradient that of its own mean
+            w = (col_w if col_w is not None else torch.ones(Y.shape[-1], device=self.dev))
+            if self.G > 1:
+                w = (w * float(self.G)).contiguous()
+            check(self.L.mk_mse_weighted(n, int(Y.shape[-1]), _p(Y), _p(T), _p(w), _p(G),
                                          _p(Gb), _p(part), engine._stream_handle()))
         return part.sum() / n, G, Gb
 
@@ -166,13 +208,13 @@ class MLP:
         decay. Returns the loss history."""
         gen = torch.Generator(device=self.dev)
         gen.manual_seed(seed)
-        n = int(X.shape[0])
+        n = int(X.shape[-2])
         losses = []
         for s in range(steps):
             a = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * s / max(steps - 1, 1)))
             if batch and batch < n:
                 idx = torch.randperm(n, generator=gen, device=self.dev)[:batch]
-                Xb, Tb = X[idx], T[idx]
+                Xb, Tb = X.index_select(-2, idx), T.index_select(-2, idx)
             else:
                 Xb, Tb = X, T
             acts, posts, Y = self.forward(Xb)
@@ -220,10 +262,11 @@ class MLP:
         return loss
 
     def predict(self, X, chunk=4096):
+        """Outputs for inputs X (B, n_in): (B, n_out), or (G, B, n_out)."""
         outs = []
         for i in range(0, int(X.shape[0]), chunk):
             outs.append(self.forward(X[i:i + chunk])[2])
-        return torch.cat(outs)
+        return torch.cat(outs, dim=-2)
 
 
 def fit_graphs(nets, Xs, Ts, steps=1500, lr=2e-3, lr_final=1e-4, col_ws=None):
@@ -444,9 +487,11 @@ class SurrogateScan:
         cw = (sc * sc / (sc * sc).sum() * sc.numel()).float().contiguous()
         net.fit(feats, Tf, steps=2, col_w=cw)
         net.fit_graph(feats, Tf, steps=2, col_w=cw)
-        net2 = MLP(feats.shape[1], basis.rank + 1, hidden=32, n_hidden=2, seed=self.seed + 1,
-                   device=self.dev)
-        fit_graphs([net, net2], [feats, feats], [Tf, Tf], steps=2, col_ws=[cw, cw])
+        pair = MLP(feats.shape[1], basis.rank + 1, hidden=32, n_hidden=2, seed=self.seed,
+                   device=self.dev, groups=2)
+        pair.fit_graph(torch.stack([feats, feats]).contiguous(), torch.stack([Tf, Tf]).contiguous(),
+                       steps=2, col_w=cw)
+        pair.predict(feats)
         Y = 0.5 * (net.predict(feats) + net.predict(feats))
         I_pred = self._decode(net, basis, base[: T.shape[0]] + Y.double() * sc)
         err = frame_rel_error(I_pred[:4], I[:4])
@@ -597,23 +642,28 @@ class SurrogateScan:
         col_w = torch.zeros(n_out, dtype=torch.float32, device=self.dev)
         col_w[: r + 1] = (scale * scale / (scale * scale).sum() * (r + 1)).float()
         feats = fourier_features(self.xy, self.n_freq, self.dev, f_max=self.f_max, f_min=self.f_min)
-        self.nets, Xs, Ts = [], [], []
+        # the two networks as one group of 2 (each GEMM launch serves both);
+        # the shorter fold repeats its last row to give both the same batch
+        Xs, Ts = [], []
         for f in (0, 1):
             rows = np.concatenate([tr, pred_idx[judged[fold == f]]])
             Tf = (torch.cat([R_tr, R_j[torch.as_tensor(fold == f, device=self.dev)]]) / scale).float()
-            Ts.append(torch.nn.functional.pad(Tf, (0, n_out - (r + 1))).contiguous())
-            Xs.append(feats[torch.as_tensor(rows, device=self.dev)].contiguous())
-            self.nets.append(MLP(feats.shape[1], n_out, self.hidden, self.n_hidden, self.seed + f,
-                                 self.dev))
-        self.losses = fit_graphs(self.nets, Xs, Ts, steps=self.fit_steps, lr=self.lr,
-                                 col_ws=[col_w, col_w])
+            Ts.append(torch.nn.functional.pad(Tf, (0, n_out - (r + 1))))
+            Xs.append(feats[torch.as_tensor(rows, device=self.dev)])
+        nb = max(int(x.shape[0]) for x in Xs)
+        grow = lambda x: torch.cat([x, x[-1:].expand(nb - x.shape[0], -1)]) if x.shape[0] < nb else x
+        X2 = torch.stack([grow(x) for x in Xs]).contiguous()
+        T2 = torch.stack([grow(x) for x in Ts]).contiguous()
+        self.net = MLP(feats.shape[1], n_out, self.hidden, self.n_hidden, self.seed, self.dev, groups=2)
+        self.losses = [self.net.fit_graph(X2, T2, steps=self.fit_steps, lr=self.lr, col_w=col_w)]
         sync()
         t["fit"] = time.perf_counter() - t0
         # Every judged frame is predicted by the network that did not train on
         # it; the other frames by the mean of the two.
         t0 = time.perf_counter()
         F = feats[torch.as_tensor(pred_idx, device=self.dev)]
-        Y0, Y1 = (net.predict(F)[:, : r + 1] for net in self.nets)
+        Y = self.net.predict(F)
+        Y0, Y1 = Y[0, :, : r + 1], Y[1, :, : r + 1]
         corr = 0.5 * (Y0 + Y1)
         j0 = torch.as_tensor(judged[fold == 0], device=self.dev)
         j1 = torch.as_tensor(judged[fold == 1], device=self.dev)
@@ -621,7 +671,7 @@ class SurrogateScan:
         corr[j1] = Y0[j1]
         D = base[torch.as_tensor(pred_idx, device=self.dev)] + corr.double() * scale
         jd = torch.as_tensor(judged, device=self.dev)
-        err_j = frame_rel_error(self._decode(self.nets[0], basis, D[jd]), I_j).cpu().numpy()
+        err_j = frame_rel_error(self._decode(self.net, basis, D[jd]), I_j).cpu().numpy()
         sync()
         t["predict_judge"] = time.perf_counter() - t0
         failed = [blk[blk != j] for blk, j, e in zip(blocks, judged, err_j) if e > self.tol]
@@ -634,7 +684,7 @@ class SurrogateScan:
         frames[torch.as_tensor(tr, device=self.dev)] = I_train
         frames[torch.as_tensor(pred_idx[judged], device=self.dev)] = I_j
         keep = np.setdiff1d(np.arange(len(pred_idx)), np.concatenate([judged, fb]))
-        self._decode(self.nets[0], basis, D[torch.as_tensor(keep, device=self.dev)], out=frames,
+        self._decode(self.net, basis, D[torch.as_tensor(keep, device=self.dev)], out=frames,
                      rows=torch.as_tensor(pred_idx[keep], device=self.dev))
         sync()
         t["decode"] = time.perf_counter() - t0
@@ -645,7 +695,7 @@ class SurrogateScan:
         t["fallback"] = time.perf_counter() - t0
         total = sum(t.values())
         # the network's gain, held out: the judged frames from the spline alone
-        I_base_j = self._decode(self.nets[0], basis, base[torch.as_tensor(pred_idx[judged],
+        I_base_j = self._decode(self.net, basis, base[torch.as_tensor(pred_idx[judged],
                                                                           device=self.dev)])
         err_jb = frame_rel_error(I_base_j, I_j).cpu().numpy()
         exact_frames = len(tr) + len(judged) + int(fb.size)
@@ -653,8 +703,7 @@ class SurrogateScan:
                    n_fallback=int(fb.size), n_failed_judges=len(failed), exact_frames=exact_frames,
                    judge_err=err_j, judge_err_base=err_jb, times=t, setup_seconds=setup_s,
                    seconds=total, frames_per_s=n / total,
-                   final_loss=[float(l[-1]) for l in self.losses],
-                   params=self.nets[0].n_params, rank=r)
+                   final_loss=float(self.losses[-1][-1]), params=self.net.n_params, rank=r)
         if exact_all:
             sync()
             t0 = time.perf_counter()
@@ -665,9 +714,9 @@ class SurrogateScan:
             pi = torch.as_tensor(pred_idx, device=self.dev)
             # the prediction of every predicted frame (judged ones by the
             # network that did not see them), and the spline's alone
-            I_b = self._decode(self.nets[0], basis, D)
+            I_b = self._decode(self.net, basis, D)
             res["model_err"] = frame_rel_error(I_b, I_all[pi]).cpu().numpy()
-            self._decode(self.nets[0], basis, base[pi], out=I_b)
+            self._decode(self.net, basis, base[pi], out=I_b)
             res["base_err"] = frame_rel_error(I_b, I_all[pi]).cpu().numpy()
             del I_b
             res["final_err"] = frame_rel_error(frames, I_all).cpu().numpy()

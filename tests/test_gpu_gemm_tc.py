@@ -150,3 +150,38 @@ def test_rejects_bad_arguments(cuda):
                         None, 0, None, None, sh) == _lib.MK_EINVAL
     assert L.mk_gemm_tc(8, 8, 8, _p(buf), 8, 1, _p(buf), 1, 8, _p(out), 8, None, ACC, None, 0,
                         None, 0, None, _p(rows), sh) == _lib.MK_EINVAL
+
+
+def test_groups_shared_input_and_split_k(cuda):
+    """Three products in one launch (mk_gemm_tc_groups): a shared A (group
+    stride 0) against per-group B, bias and output; and per-group long-K
+    weight-gradient products split over CTAs."""
+    import ctypes
+    L = _lib.load()
+    rng = np.random.default_rng(13)
+    G, M, N, K = 3, 200, 96, 72
+    A = torch.tensor(rng.standard_normal((M, K)), dtype=torch.float32).bfloat16()
+    W = torch.tensor(rng.standard_normal((G, N, K)), dtype=torch.float32).bfloat16()
+    bias = torch.tensor(rng.standard_normal((G, N)), dtype=torch.float32)
+    C = torch.full((G, M, N), float("nan"), dtype=torch.float32, device=cuda)
+    gs = (ctypes.c_longlong * 6)(0, N * K, M * N, 0, N, 0)
+    _lib.check(L.mk_gemm_tc_groups(G, gs, M, N, K, _p(A.to(cuda)), K, 1, _p(W.to(cuda)), 1, K,
+                                   _p(C), N, _p(bias.to(cuda)), BIAS | RELU, None, 0, None, 0,
+                                   None, None, engine._stream_handle()))
+    engine.sync()
+    for g in range(G):
+        ref = torch.relu(A.double() @ W[g].double().T + bias[g].double())
+        assert float((C[g].cpu().double() - ref).abs().max()) <= _tol(ref, K), g
+    # G^T X per group, K = 900 rows: split K
+    Kb = 900
+    Gm = torch.tensor(rng.standard_normal((G, Kb, 64)), dtype=torch.float32).bfloat16()
+    X = torch.tensor(rng.standard_normal((G, Kb, 48)), dtype=torch.float32).bfloat16()
+    E = torch.full((G, 64, 48), float("nan"), dtype=torch.float32, device=cuda)
+    gs = (ctypes.c_longlong * 6)(Kb * 64, Kb * 48, 64 * 48, 0, 0, 0)
+    _lib.check(L.mk_gemm_tc_groups(G, gs, 64, 48, Kb, _p(Gm.to(cuda)), 1, 64, _p(X.to(cuda)), 48, 1,
+                                   _p(E), 48, None, 0, None, 0, None, 0, None, None,
+                                   engine._stream_handle()))
+    engine.sync()
+    for g in range(G):
+        ref = Gm[g].double().T @ X[g].double()
+        assert float((E[g].cpu().double() - ref).abs().max()) <= _tol(ref, Kb), g

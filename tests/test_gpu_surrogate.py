@@ -143,3 +143,41 @@ def test_surrogate_scan_gains_over_exact(cuda):
     # frames/s over the exact-only scan, both timed here
     assert res["gain"] > 1.5, res["gain"]
 
+
+
+def test_grouped_networks_match_separate_ones(cuda):
+    """A group of two networks (every launch serving both) computes what two
+    separate networks with the same seeds compute on their own data: same
+    initial weights, outputs, gradients, and the same weights after captured
+    training."""
+    rng = np.random.default_rng(8)
+    X = torch.tensor(omlp.bf16(rng.standard_normal((2, 40, 24))), dtype=torch.bfloat16, device=cuda)
+    T = torch.tensor(rng.standard_normal((2, 40, 16)), dtype=torch.float32, device=cuda)
+    w = torch.tensor(rng.uniform(0.5, 2.0, 16), dtype=torch.float32, device=cuda)
+    grp = MLP(24, 16, hidden=32, n_hidden=2, seed=5, device=cuda, groups=2)
+    sep = [MLP(24, 16, hidden=32, n_hidden=2, seed=5 + g, device=cuda) for g in range(2)]
+    for l in range(len(sep[0].W)):
+        for g in range(2):
+            assert torch.equal(grp.W[l][g], sep[g].W[l])
+    acts, posts, Y = grp.forward(X)
+    loss, G, Gb = grp.mse(Y, T, w)
+    dW, db = grp.backward(acts, posts, G, Gb)
+    losses = []
+    for g in range(2):
+        a, p, y = sep[g].forward(X[g].contiguous())
+        assert torch.allclose(Y[g], y, rtol=1e-6, atol=1e-6)
+        l_, G_, Gb_ = sep[g].mse(y, T[g].contiguous(), w)
+        losses.append(float(l_))
+        dW_, db_ = sep[g].backward(a, p, G_, Gb_)
+        for l in range(len(dW_)):
+            assert torch.allclose(dW[l][g], dW_[l], rtol=1e-5, atol=1e-7), (g, l)
+            assert torch.allclose(db[l][g], db_[l], rtol=1e-5, atol=1e-7), (g, l)
+    assert abs(float(loss) - sum(losses)) <= 1e-5 * sum(losses)
+    grp.fit_graph(X, T, steps=30, lr=3e-3, col_w=w)
+    for g in range(2):
+        sep[g].fit_graph(X[g].contiguous(), T[g].contiguous(), steps=30, lr=3e-3, col_w=w)
+        for l in range(len(sep[g].W)):
+            assert torch.allclose(grp.W[l][g], sep[g].W[l], rtol=1e-4, atol=1e-6), (g, l)
+    Yp = grp.predict(X[0].contiguous())
+    assert Yp.shape == (2, 40, 16)
+    assert torch.allclose(Yp[1], sep[1].predict(X[0].contiguous()), rtol=1e-5, atol=1e-6)
