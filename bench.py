@@ -366,6 +366,91 @@ def _mlp_rate(params, n_train, steps, seconds):
                     "the tensor cores; the whole fit is ~2 % of the scan's time"}
 
 
+def fp64_spread_check(w, field, dev, n_grid=32):
+    """The FP64 plain GPU kernel on pixels spread over the whole detector
+    (the 4 corners, the 4 edge midpoints, the centre and an n_grid x n_grid
+    edge-to-edge grid) of workload ``w``, all atoms: its rate (the speed
+    bar) and the errors of ``field`` (complex (nz, ny), the FP32 split
+    result) against it. The pixel-sharing forms drop terms that grow toward
+    the detector's edges and corners, so the error is taken there too."""
+    import torch
+
+    from mosaic_gb300 import engine, workloads
+    B = w.beam
+    kw = w.sc_kwargs
+    phys = B.physics(kw["apply_polarization"], kw["spherical_decay"], kw["remove_forward"])
+    pos_h, idx_h, labels = B.collect_atoms(w.sample)
+    table = engine.SpeciesTable.build(labels, B.tables, B._energy, B._debye_waller)
+    coords_m = np.asarray(w.detector.pixel_coordinates, dtype=np.float64) / 1e10
+    ny, nz = w.detector.shape
+    sel = workloads.spread_pixels(w.detector.shape, n_grid)
+    m = len(sel)
+    pix_s = engine.Pixels(coords_m[:, sel], m, 1, phys, device=dev)
+    a = engine.atoms_lab(torch.as_tensor(pos_h).to(dev), idx_h, w.stage.rotation,
+                         w.stage.translation, table, e0=B._beam_E0_map, grid=B._beam_grid(),
+                         device=dev)
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    ref = engine.run_plain(a, pix_s, phys)
+    f1.record()
+    engine.sync()
+    fp64_s = f0.elapsed_time(f1) * 1e-3
+    I_ref = (ref ** 2).sum(1).cpu().numpy()
+    I_out = np.abs(np.asarray(field).reshape(-1)[sel]) ** 2
+    strong = I_ref >= 1e-3 * I_ref.max()
+    edge = np.isin(sel, workloads.spread_pixels(w.detector.shape, 2)) & \
+        (sel != (nz // 2) * ny + ny // 2)
+    return {"fp64_gatom_px_s": float(pos_h.shape[0]) * m / fp64_s / 1e9, "pixels": m,
+            "rel_err_max_over_peak": float(np.abs(I_out - I_ref).max() / I_ref.max()),
+            "rel_err_l2": float(np.linalg.norm(I_out - I_ref) / np.linalg.norm(I_ref)),
+            "rel_err_corners_and_edge_midpoints": float(np.abs(I_out - I_ref)[edge].max()
+                                                        / I_ref.max()),
+            "rel_err_local_max_where_I_ge_1e-3_peak":
+                float((np.abs(I_out - I_ref)[strong] / I_ref[strong]).max()) if strong.any()
+                else None}
+
+
+def configs_leg(args, dev, reps=3):
+    """The other single-exposure configurations -- config 1 (32,000-atom fcc
+    Cu, 128^2) and config 3 (18.3M-atom Cu polycrystal, 1024^2) -- end to end
+    through the public entry point with host arrays (median of ``reps``
+    calls after one call that stages, and tunes on first use of the detector
+    size), each checked against the FP64 plain kernel on pixels spread over
+    its whole detector."""
+    import torch
+
+    from mosaic_gb300 import workloads
+    out = {}
+    for name in ("fcc_cu_32k", "cu_polycrystal_18m"):
+        w = workloads.build(name)
+        B = w.beam
+        kw = w.sc_kwargs
+        B.atomic_scattering_kinematic(w.sample, w.detector, w.stage, return_double=True, **kw)
+        times = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            field = B.atomic_scattering_kinematic(w.sample, w.detector, w.stage,
+                                                  return_double=True, **kw)
+            times.append(time.perf_counter() - t0)
+        s = float(np.median(times))
+        n_atoms = int(B.collect_atoms(w.sample)[0].shape[0])
+        n_pix = int(np.prod(w.detector.shape))
+        terms = float(n_atoms) * n_pix
+        chk = fp64_spread_check(w, field, dev, args.fp64_grid)
+        out[name] = {"atoms": n_atoms, "pixels": n_pix, "e2e_seconds": s,
+                     "e2e_gatom_px_s": terms / s / 1e9,
+                     "speedup_vs_fp64": terms / s / 1e9 / chk["fp64_gatom_px_s"],
+                     "path": B.last_run.get("path"), "tile_atoms": B.last_run.get("tile_atoms"),
+                     "launch": B.last_run.get("launch"),
+                     "accuracy_vs_fp64": chk}
+        del w, B, field
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -537,35 +622,10 @@ def run_ours(args):
         B._beam_E0_map.astype(np.complex64).nbytes + coords_m.nbytes
     d2h = n_pix * 16
 
-    # FP64 plain (same GPU) on pixels spread over the whole detector (corners,
-    # edge midpoints, centre and a 32 x 32 edge-to-edge grid): speed bar and
-    # error reference. The pixel-sharing forms drop terms that grow toward the
-    # detector's edges and corners, so the error is taken there too.
-    sel = workloads.spread_pixels(w.detector.shape, args.fp64_grid)
-    m = len(sel)
-    pix_s = engine.Pixels(coords_m[:, sel], m, 1, phys, device=dev)
-    a = engine.atoms_lab(pos_d, idx_h, w.stage.rotation, w.stage.translation, table,
-                         e0=B._beam_E0_map, grid=B._beam_grid(), device=dev)
-    torch.cuda.synchronize()
-    f0 = torch.cuda.Event(enable_timing=True)
-    f1 = torch.cuda.Event(enable_timing=True)
-    f0.record()
-    ref = engine.run_plain(a, pix_s, phys)
-    f1.record()
-    engine.sync()
-    fp64_s = f0.elapsed_time(f1) * 1e-3
-    fp64_rate = float(n_atoms) * m / fp64_s / 1e9
-    I_ref = (ref ** 2).sum(1).cpu().numpy()
-    I_out = (np.abs(field.reshape(-1)[sel]) ** 2)
-    rel_err = float(np.abs(I_out - I_ref).max() / I_ref.max())
-    l2_err = float(np.linalg.norm(I_out - I_ref) / np.linalg.norm(I_ref))
-    # the same per pixel against its own intensity, over the pixels within
-    # 1e-3 of the peak (the far wings hold almost nothing)
-    strong = I_ref >= 1e-3 * I_ref.max()
-    loc_err = float((np.abs(I_out - I_ref)[strong] / I_ref[strong]).max()) if strong.any() else None
-    edge = np.isin(sel, workloads.spread_pixels(w.detector.shape, 2)) & \
-        (sel != (nz // 2) * ny + ny // 2)
-    edge_err = float(np.abs(I_out - I_ref)[edge].max() / I_ref.max())
+    # FP64 plain (same GPU) on pixels spread over the whole detector: speed
+    # bar and error reference
+    chk = fp64_spread_check(w, field, dev, args.fp64_grid)
+    m, fp64_rate = chk["pixels"], chk["fp64_gatom_px_s"]
 
     peaks, peak_src = _peaks()
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -585,6 +645,7 @@ def run_ours(args):
     achieved = terms / (split_ms * 1e-3)
     gpu_launches = args.steps * 8
 
+    configs = configs_leg(args, dev) if (rank == 0 and not args.no_configs) else None
     scan = scan_leg(args, dev) if (rank == 0 and args.scan_frames > 0) else None
     surr = surrogate_leg(args, dev) if (rank == 0 and not args.no_surrogate) else None
     if rank == 0:
@@ -627,9 +688,12 @@ def run_ours(args):
             "fp64_plain": {"value": fp64_rate, "unit": "Gatom*pixel/s",
                            "subset": f"{m} pixels spread over the whole detector, all atoms",
                            "speedup_fp32_vs_fp64": (achieved / 1e9) / fp64_rate},
-            "accuracy": {"rel_err_max_over_peak": rel_err, "rel_err_l2": l2_err,
-                         "rel_err_corners_and_edge_midpoints": edge_err,
-                         "rel_err_local_max_where_I_ge_1e-3_peak": loc_err,
+            "accuracy": {"rel_err_max_over_peak": chk["rel_err_max_over_peak"],
+                         "rel_err_l2": chk["rel_err_l2"],
+                         "rel_err_corners_and_edge_midpoints":
+                             chk["rel_err_corners_and_edge_midpoints"],
+                         "rel_err_local_max_where_I_ge_1e-3_peak":
+                             chk["rel_err_local_max_where_I_ge_1e-3_peak"],
                          "pixels": m,
                          "reference": f"FP64 plain GPU kernel at {m} pixels spread over the whole "
                                       f"detector: the 4 corners, the 4 edge midpoints, the centre "
@@ -639,6 +703,7 @@ def run_ours(args):
             "autotune": [[float(t), c] for t, c in tune_tbl] if tune_tbl else [],
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "configs": configs,
             "scan": scan,
             "surrogate_scan": surr,
         }
@@ -659,6 +724,8 @@ def main():
     ap.add_argument("--fp64-grid", type=int, default=32,
                     help="side of the edge-to-edge pixel grid the FP64 reference is computed on")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip configs 1 and 3 (end to end through the entry point)")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip the surrogate-assisted scan leg (101 x 101 frames)")
     ap.add_argument("--surrogate-verify", type=int, default=64,

@@ -165,9 +165,10 @@ def test_groups_shared_input_and_split_k(cuda):
     bias = torch.tensor(rng.standard_normal((G, N)), dtype=torch.float32)
     C = torch.full((G, M, N), float("nan"), dtype=torch.float32, device=cuda)
     gs = (ctypes.c_longlong * 6)(0, N * K, M * N, 0, N, 0)
-    _lib.check(L.mk_gemm_tc_groups(G, gs, M, N, K, _p(A.to(cuda)), K, 1, _p(W.to(cuda)), 1, K,
-                                   _p(C), N, _p(bias.to(cuda)), BIAS | RELU, None, 0, None, 0,
-                                   None, None, engine._stream_handle()))
+    Ad, Wd, bd = A.to(cuda), W.to(cuda), bias.to(cuda)      # alive until the kernel has run
+    _lib.check(L.mk_gemm_tc_groups(G, gs, M, N, K, _p(Ad), K, 1, _p(Wd), 1, K, _p(C), N, _p(bd),
+                                   BIAS | RELU, None, 0, None, 0, None, None,
+                                   engine._stream_handle()))
     engine.sync()
     for g in range(G):
         ref = torch.relu(A.double() @ W[g].double().T + bias[g].double())
@@ -178,9 +179,9 @@ def test_groups_shared_input_and_split_k(cuda):
     X = torch.tensor(rng.standard_normal((G, Kb, 48)), dtype=torch.float32).bfloat16()
     E = torch.full((G, 64, 48), float("nan"), dtype=torch.float32, device=cuda)
     gs = (ctypes.c_longlong * 6)(Kb * 64, Kb * 48, 64 * 48, 0, 0, 0)
-    _lib.check(L.mk_gemm_tc_groups(G, gs, 64, 48, Kb, _p(Gm.to(cuda)), 1, 64, _p(X.to(cuda)), 48, 1,
-                                   _p(E), 48, None, 0, None, 0, None, 0, None, None,
-                                   engine._stream_handle()))
+    Gd, Xd = Gm.to(cuda), X.to(cuda)
+    _lib.check(L.mk_gemm_tc_groups(G, gs, 64, 48, Kb, _p(Gd), 1, 64, _p(Xd), 48, 1, _p(E), 48,
+                                   None, 0, None, 0, None, 0, None, None, engine._stream_handle()))
     engine.sync()
     for g in range(G):
         ref = Gm[g].double().T @ X[g].double()
