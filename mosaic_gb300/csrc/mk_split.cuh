@@ -568,18 +568,20 @@ __device__ __forceinline__ void mk_tile_terms_oct(
             cv = f2_fma(v2, f2_fma(v2, f2_fma(v2, k6, k4), k2), one);
             sv = f2_mul(dv, f2_fma(v2, f2_fma(v2, k5, k3), one));
         }
+        // the two quads share u and v: the four products of their factors
+        // are formed once and each quad's 8 sums take one FMA apiece
+        const mk_f2 pcc = f2_mul(cu, cv), pcs = f2_mul(cu, sv);
+        const mk_f2 psc = f2_mul(su, cv), pss = f2_mul(su, sv);
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const mk_f2 xc = f2_mul(ec[j], cu), yc = f2_mul(es[j], cu);
-            const mk_f2 xs = f2_mul(ec[j], su), ys = f2_mul(es[j], su);
-            acc[j][0] = f2_fma(xc, cv, acc[j][0]);
-            acc[j][1] = f2_fma(yc, cv, acc[j][1]);
-            acc[j][2] = f2_fma(xc, sv, acc[j][2]);
-            acc[j][3] = f2_fma(yc, sv, acc[j][3]);
-            acc[j][4] = f2_fma(xs, cv, acc[j][4]);
-            acc[j][5] = f2_fma(ys, cv, acc[j][5]);
-            acc[j][6] = f2_fma(xs, sv, acc[j][6]);
-            acc[j][7] = f2_fma(ys, sv, acc[j][7]);
+            acc[j][0] = f2_fma(ec[j], pcc, acc[j][0]);
+            acc[j][1] = f2_fma(es[j], pcc, acc[j][1]);
+            acc[j][2] = f2_fma(ec[j], pcs, acc[j][2]);
+            acc[j][3] = f2_fma(es[j], pcs, acc[j][3]);
+            acc[j][4] = f2_fma(ec[j], psc, acc[j][4]);
+            acc[j][5] = f2_fma(es[j], psc, acc[j][5]);
+            acc[j][6] = f2_fma(ec[j], pss, acc[j][6]);
+            acc[j][7] = f2_fma(es[j], pss, acc[j][7]);
         }
     }
 }
