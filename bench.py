@@ -61,13 +61,14 @@ MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR = 1, 10
 # eight accumulators 8, sin/cos argument scaling 1, per-atom coefficients 2)
 MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD = 0.5, 9
 # 2x4 pixel-octet form (two quads sharing their half differences): per octet
-# and atom 47 FP32 lane operations on tiles that pass the phase straight to
+# and atom 43 FP32 lane operations on tiles that pass the phase straight to
 # the sin/cos (three dot products 9, the two quad phases 2, the four sin/cos
-# argument scalings 2, u^2 and v^2 2, short polynomials 6, 2 x 4 products 8,
-# 2 x 8 accumulators 16, per-atom coefficients 2) and 51 with the mod-1
-# reduction (4 more); ~87 % of the headline's tiles take the first: ~6 per
-# term, 0.5 MUFU
-MUFU_PER_TERM_OCT, FP32_PER_TERM_OCT = 0.5, 6
+# argument scalings 2, u^2 and v^2 2, short polynomials 6, the four products
+# of the shared u and v factors 4, 2 x 8 accumulators 16, per-atom
+# coefficients 2) and 47 with the mod-1 reduction (4 more); ~87 % of the
+# headline's tiles take the first: 5.44 per term, counted as 5.4 (the lower
+# count gives the higher peak), 0.5 MUFU
+MUFU_PER_TERM_OCT, FP32_PER_TERM_OCT = 0.5, 5.4
 FORMS = {0: ("one sin/cos per term", MUFU_PER_TERM, FP32_PER_TERM),
          1: ("pixel pairs (one sin/cos per two terms)", MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR),
          2: ("2x2 pixel quads (one sin/cos per four terms)", MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD),

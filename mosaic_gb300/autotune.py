@@ -51,15 +51,22 @@ def _cache_path():
     return os.path.join(base, "tune.json")
 
 
+_SRC_HASH = []
+
+
 def _src_hash():
-    """Hash of every kernel source (a change to any of them retunes)."""
+    """Hash of every kernel source (a change to any of them retunes); taken
+    once per process, as the library it describes is loaded once."""
+    if _SRC_HASH:
+        return _SRC_HASH[0]
     h = hashlib.sha1()
     csrc = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
     for path in sorted(glob.glob(os.path.join(csrc, "*.cu")) + glob.glob(os.path.join(csrc, "*.cuh"))):
         h.update(os.path.basename(path).encode())
         with open(path, "rb") as fh:
             h.update(fh.read())
-    return h.hexdigest()[:12]
+    _SRC_HASH.append(h.hexdigest()[:12])
+    return _SRC_HASH[0]
 
 
 def _key(n_pix, kind="exposure"):

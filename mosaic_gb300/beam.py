@@ -262,55 +262,58 @@ class beam:
         labels, lab_index = [], {}
         off = 0
         self.last_stream_bytes = 0               # host -> device bytes of this call
-        with ThreadPoolExecutor(max_workers=1) as ex:
-            nxt = ex.submit(self._load_chunk, sample, 1) if n_chunks else None
-            for cid in range(1, n_chunks + 1):
-                codes, lab, pos = nxt.result()
-                nxt = ex.submit(self._load_chunk, sample, cid + 1) if cid < n_chunks else None
-                if codes.size == 0:
+        # one loader thread, kept by the beam for later calls
+        ex = getattr(self, "_loader", None)
+        if ex is None:
+            ex = self._loader = ThreadPoolExecutor(max_workers=1)
+        nxt = ex.submit(self._load_chunk, sample, 1) if n_chunks else None
+        for cid in range(1, n_chunks + 1):
+            codes, lab, pos = nxt.result()
+            nxt = ex.submit(self._load_chunk, sample, cid + 1) if cid < n_chunks else None
+            if codes.size == 0:
+                continue
+            remap = np.full(len(lab), -1, dtype=np.int32)
+            for i, el in enumerate(lab):
+                if not self.tables.has(el):
                     continue
-                remap = np.full(len(lab), -1, dtype=np.int32)
-                for i, el in enumerate(lab):
-                    if not self.tables.has(el):
-                        continue
-                    if el not in lab_index:
-                        lab_index[el] = len(labels)
-                        labels.append(el)
-                    remap[i] = lab_index[el]
-                # byte codes of known labels go to the device as they are and
-                # are mapped to the global species there; anything else is
-                # mapped (and filtered) on the host
-                on_device = codes.dtype == np.uint8 and bool((remap >= 0).all())
-                g = None
-                if not on_device:
-                    g = remap[codes]
-                    keep = g >= 0
-                    if not keep.all():
-                        pos, g = pos[keep], g[keep]
-                n = int(pos.shape[0])
-                if n == 0:
-                    continue
-                b = cid & 1
-                if done[b] is not None:
-                    done[b].synchronize()        # staging buffer b is free again
-                st_pos[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(pos)))
-                self.last_stream_bytes += 12 * n + (n + 4 * len(remap) if on_device else 4 * n)
+                if el not in lab_index:
+                    lab_index[el] = len(labels)
+                    labels.append(el)
+                remap[i] = lab_index[el]
+            # byte codes of known labels go to the device as they are and
+            # are mapped to the global species there; anything else is
+            # mapped (and filtered) on the host
+            on_device = codes.dtype == np.uint8 and bool((remap >= 0).all())
+            g = None
+            if not on_device:
+                g = remap[codes]
+                keep = g >= 0
+                if not keep.all():
+                    pos, g = pos[keep], g[keep]
+            n = int(pos.shape[0])
+            if n == 0:
+                continue
+            b = cid & 1
+            if done[b] is not None:
+                done[b].synchronize()        # staging buffer b is free again
+            st_pos[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(pos)))
+            self.last_stream_bytes += 12 * n + (n + 4 * len(remap) if on_device else 4 * n)
+            if on_device:
+                st_u8[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(codes)))
+            else:
+                st_idx[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(g, dtype=np.int32)))
+            with torch.cuda.stream(side):
+                pos_d[off:off + n].copy_(st_pos[b][:n], non_blocking=True)
                 if on_device:
-                    st_u8[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(codes)))
+                    lut = torch.from_numpy(remap).to(dev)      # ordered on this stream
+                    raw = st_u8[b][:n].to(dev, non_blocking=True)
+                    idx_d[off:off + n] = lut[raw.long()]
                 else:
-                    st_idx[b][:n].copy_(torch.from_numpy(np.ascontiguousarray(g, dtype=np.int32)))
-                with torch.cuda.stream(side):
-                    pos_d[off:off + n].copy_(st_pos[b][:n], non_blocking=True)
-                    if on_device:
-                        lut = torch.from_numpy(remap).to(dev)      # ordered on this stream
-                        raw = st_u8[b][:n].to(dev, non_blocking=True)
-                        idx_d[off:off + n] = lut[raw.long()]
-                    else:
-                        idx_d[off:off + n].copy_(st_idx[b][:n], non_blocking=True)
-                    ev = torch.cuda.Event()
-                    ev.record(side)
-                    done[b] = ev
-                off += n
+                    idx_d[off:off + n].copy_(st_idx[b][:n], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(side)
+                done[b] = ev
+            off += n
         torch.cuda.current_stream(dev).wait_stream(side)
         # the staging buffers must outlive the copies: wait before they go
         for ev in done:

@@ -165,22 +165,30 @@ class Pixels:
             raise ValueError(f"frames cover {off} pixels, xyz has {P}")
 
     def r0_min(self):
-        return float(self.r0.min())
+        """Smallest pixel distance (one read-back per Pixels object)."""
+        if getattr(self, "_r0_min", None) is None:
+            self._r0_min = float(self.r0.min())
+        return self._r0_min
 
     def pair_step(self):
         """Largest |u_2j - u_2j+1| over the pixel pairs (2j, 2j+1) of every
         frame, u the unit vector to the pixel: the pairs mode shares one
-        sin/cos between the two pixels of a pair."""
+        sin/cos between the two pixels of a pair (once per Pixels object)."""
+        if getattr(self, "_pair_step", None) is not None:
+            return self._pair_step
         u = self.u[:, :3].double()
+        worst = 0.0
         if all(off % 2 == 0 for off, _ in self.spans):
             h = self.n // 2
-            return float(torch.linalg.vector_norm(u[0:2 * h:2] - u[1:2 * h:2], dim=1).max()) if h else 0.0
-        worst = 0.0
-        for off, m in self.spans:
-            h = m // 2
             if h:
-                d = u[off:off + 2 * h:2] - u[off + 1:off + 2 * h:2]
-                worst = max(worst, float(torch.linalg.vector_norm(d, dim=1).max()))
+                worst = float(torch.linalg.vector_norm(u[0:2 * h:2] - u[1:2 * h:2], dim=1).max())
+        else:
+            for off, m in self.spans:
+                h = m // 2
+                if h:
+                    d = u[off:off + 2 * h:2] - u[off + 1:off + 2 * h:2]
+                    worst = max(worst, float(torch.linalg.vector_norm(d, dim=1).max()))
+        self._pair_step = worst
         return worst
 
     def row_lengths(self):
@@ -428,17 +436,30 @@ class Tiles:
                                _stream_handle(stream)))
         self._ws = ws   # keep until the stream has consumed it
 
+    def _extents(self):
+        """(largest tile radius, largest origin norm): one read-back per
+        object (its arrays do not change after the build)."""
+        if getattr(self, "_ext", None) is None:
+            if not self.n_tiles:
+                self._ext = (0.0, 0.0)
+            else:
+                o = self.origin[: self.n_tiles]
+                self._ext = tuple(torch.stack([o[:, 3].max(),
+                                               torch.linalg.vector_norm(o[:, :3], dim=1).max()]
+                                              ).tolist())
+        return self._ext
+
     def max_radius(self):
-        return float(self.origin[: self.n_tiles, 3].max()) if self.n_tiles else 0.0
+        return self._extents()[0]
 
     def max_origin_norm(self):
-        if not self.n_tiles:
-            return 0.0
-        return float(torch.linalg.vector_norm(self.origin[: self.n_tiles, :3], dim=1).max())
+        return self._extents()[1]
 
     def amp_is_real(self):
-        # atom pairs interleaved as re0 re1 im0 im1
-        return bool((self.amp.view(-1, 4)[:, 2:] == 0).all()) if self.n_tiles else True
+        # atom pairs interleaved as re0 re1 im0 im1; one read-back per object
+        if getattr(self, "_real", None) is None:
+            self._real = bool((self.amp.view(-1, 4)[:, 2:] == 0).all()) if self.n_tiles else True
+        return self._real
 
 
 DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
@@ -702,12 +723,26 @@ class TilesView:
                            self.species.data_ptr(), self.pos.data_ptr(), self.amp.data_ptr())
 
     def amp_is_real(self):
-        return bool((self.amp[: self.n_tiles * self.tile_atoms].reshape(-1, 4)[:, 2:] == 0).all())
+        if getattr(self, "_real", None) is None:
+            self._real = bool((self.amp[: self.n_tiles * self.tile_atoms].reshape(-1, 4)[:, 2:]
+                               == 0).all())
+        return self._real
+
+    def _extents(self):
+        """(largest tile radius, largest origin norm): one read-back per
+        object (its arrays do not change after the build)."""
+        if getattr(self, "_ext", None) is None:
+            if not self.n_tiles:
+                self._ext = (0.0, 0.0)
+            else:
+                o = self.origin[: self.n_tiles]
+                self._ext = tuple(torch.stack([o[:, 3].max(),
+                                               torch.linalg.vector_norm(o[:, :3], dim=1).max()]
+                                              ).tolist())
+        return self._ext
 
     def max_radius(self):
-        return float(self.origin[: self.n_tiles, 3].max()) if self.n_tiles else 0.0
+        return self._extents()[0]
 
     def max_origin_norm(self):
-        if not self.n_tiles:
-            return 0.0
-        return float(torch.linalg.vector_norm(self.origin[: self.n_tiles, :3], dim=1).max())
+        return self._extents()[1]
