@@ -159,11 +159,29 @@ def _peaks():
 TRAFFIC_PROFILES = os.path.join(HERE, "profiles")
 
 
+def split_src_hash():
+    """Hash of the sources the split kernel's launch is built from (its
+    template and instances, its host side, the tile build and the shared
+    header): the DRAM traffic of a launch depends on these alone."""
+    import glob
+    import hashlib
+    csrc = os.path.join(HERE, "mosaic_gb300", "csrc")
+    names = sorted(glob.glob(os.path.join(csrc, "mk_split*.cu")) +
+                   [os.path.join(csrc, n) for n in ("mk_split.cuh", "mk_sum_f32.cu",
+                                                    "mk_stage.cu", "mk_common.cuh")])
+    h = hashlib.sha1()
+    for path in names:
+        h.update(os.path.basename(path).encode())
+        with open(path, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:12]
+
+
 def profiled_traffic(config, n_pix, launch):
     """DRAM bytes per launch of the split kernel from a committed ncu
     summary of this workload (profiles/traffic_<config>.md, a line
-    ``dram_bytes_per_launch: N`` with the launch shape and kernel source
-    hash it was measured on), or None. Flagged when the kernel source or
+    ``dram_bytes_per_launch: N`` with the launch shape and the split
+    kernel's source hash (``split_src_hash``) it was measured on), or None. Flagged when the kernel source or
     the launch shape has changed since."""
     path = os.path.join(TRAFFIC_PROFILES, f"traffic_{config}.md")
     try:
@@ -181,12 +199,11 @@ def profiled_traffic(config, n_pix, launch):
         nbytes = int(vals["dram_bytes_per_launch"])
     except (KeyError, ValueError):
         return None
-    from mosaic_gb300 import autotune
     shape = ",".join(str(launch.get(k)) for k in ("pix_per_thread", "threads", "pairs"))
     return {"bytes_per_launch": nbytes, "file": os.path.relpath(path, HERE),
             "pixels": n_pix, "measured_launch": vals.get("launch"),
             "measured_src_hash": vals.get("src_hash"),
-            "same_kernel_source": vals.get("src_hash") == autotune._src_hash(),
+            "same_kernel_source": vals.get("src_hash") == split_src_hash(),
             "same_launch_shape": vals.get("launch") == shape,
             "how": vals.get("how")}
 

@@ -6,7 +6,7 @@
 // A(m, k) at A[m*sam + k*sak], B(k, n) at B[k*sbk + n*sbn] (bf16, any
 // strides: the same operand conventions as mk_gemm_bf16, so one kernel
 // serves the MLP's forward pass, its input and weight gradients and the
-// decoding of predicted frames). A CTA of 4 warps owns a 128 x BN tile of C:
+// decoding of predicted frames). A CTA of 8 warps owns a 128 x BN tile of C:
 // the K loop runs in chunks of 64 through MK_TCG_STAGES shared-memory
 // stages, two chunks ahead of the tensor core: every thread stages part of
 // a chunk into the K-major core-matrix layout of mk_tc.cuh (k-contiguous
@@ -14,9 +14,9 @@
 // batched 16-byte loads repacked in registers), one elected thread issues
 // the chunk's four tcgen05.mma (K = 16 each) and commits them to the
 // stage's mbarrier, which frees the stage for the chunk MK_TCG_STAGES
-// later. The epilogue reads the accumulator back with
-// tcgen05.ld (warp w: TMEM lanes 32w..32w+31 = tile rows), one row per
-// thread. Split-K over gridDim.z adds partial tiles into C with atomics.
+// later. The epilogue reads the accumulator back with tcgen05.ld (warp w:
+// TMEM lanes 32 (w % 4) .. + 31 = tile rows, columns of half w / 4), one
+// row per thread. Split-K over gridDim.z adds partial tiles into C with atomics.
 // Every mbarrier wait is bounded; on expiry the CTA records
 // MK_DEV_TIMEOUT_TMA, waits (bounded) for its issued MMAs, frees its TMEM
 // and returns.
@@ -27,7 +27,7 @@
 #define MK_TCG_BM 128
 #define MK_TCG_BK 64
 #define MK_TCG_STAGES 3
-#define MK_TCG_NT 128
+#define MK_TCG_NT 256
 
 #define MK_GEMM_ACCUMULATE 1
 #define MK_GEMM_BIAS 2
@@ -288,9 +288,12 @@ __global__ void __launch_bounds__(MK_TCG_NT) mk_gemm_tc_kernel(MkTcGemm g, int *
     if (__syncthreads_or(!ok)) {
         if (tid == 0) atomicExch(status, MK_DEV_TIMEOUT_TMA);
     } else {
-        // Epilogue: thread = one row of the tile, 16 columns per TMEM load;
-        // every operand of a 16-column group is loaded before any store.
-        const int m = m0 + 32 * warp + lane;
+        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (the lane
+        // quarter a warp may access) for half w / 4 of the columns; thread =
+        // one row of the tile, 16 columns per TMEM load; every operand of a
+        // 16-column group is loaded before any store.
+        const int quarter = warp & 3, half = warp >> 2;
+        const int m = m0 + 32 * quarter + lane;
         const bool row_ok = m < g.M;
         const long long orow = row_ok ? (g.row_map ? g.row_map[m] : (long long)m) : 0;
         const float rs = (row_ok && g.row_scale) ? g.row_scale[m] : 1.f;
@@ -300,10 +303,10 @@ __global__ void __launch_bounds__(MK_TCG_NT) mk_gemm_tc_kernel(MkTcGemm g, int *
         const bool m_vec = g.mask && ((uintptr_t)g.mask & 15) == 0 && (g.ldm & 3) == 0;
         const bool cb_vec = g.Cb && ((uintptr_t)g.Cb & 15) == 0 && (g.ldcb & 7) == 0;
 #pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 16) {
+        for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 16) {
             float v[16];
             if (nchunks > 0) {
-                mk_tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+                mk_tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0, v);
             } else {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) v[j] = 0.f;
