@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import hashlib
 import os
+import types
 import warnings
 
 import numpy as np
@@ -61,6 +62,7 @@ class beam:
         self._debye_waller = None           # element -> B [A^2]; None = no factor
         self.tables = tables or ScatteringTables()
         self.last_run = {}
+        self._pix_cache = None
 
     # ------------------------------------------------------------ beam setup
     def create_beam(self, energy, eV=True, beam_shape="rectangular", beam_size=(1000.0, 1000.0),
@@ -262,14 +264,17 @@ class beam:
         labels, lab_index = [], {}
         off = 0
         self.last_stream_bytes = 0               # host -> device bytes of this call
-        # one loader thread, kept by the beam for later calls
+        # one loader thread, kept by the beam for later calls (a one-chunk
+        # sample is read in place: there is nothing to overlap it with)
         ex = getattr(self, "_loader", None)
-        if ex is None:
+        if ex is None and n_chunks > 1:
             ex = self._loader = ThreadPoolExecutor(max_workers=1)
-        nxt = ex.submit(self._load_chunk, sample, 1) if n_chunks else None
+        submit = (ex.submit if n_chunks > 1 else
+                  lambda fn, *a: types.SimpleNamespace(result=lambda r=fn(*a): r))
+        nxt = submit(self._load_chunk, sample, 1) if n_chunks else None
         for cid in range(1, n_chunks + 1):
             codes, lab, pos = nxt.result()
-            nxt = ex.submit(self._load_chunk, sample, cid + 1) if cid < n_chunks else None
+            nxt = submit(self._load_chunk, sample, cid + 1) if cid < n_chunks else None
             if codes.size == 0:
                 continue
             remap = np.full(len(lab), -1, dtype=np.int32)
@@ -546,11 +551,25 @@ class beam:
             # computed on the device for every call; the reference's on-disk
             # cache (ein_cache_dir, recompute_cache) has nothing to save here
             self.apply_depth_ein(atoms)
-        pix = engine.Pixels(coords.astype(np.float64) / 1e10, Ny, Nz, phys)
+        pix = self._pixels_for(coords, Ny, Nz, phys)
         out = self.scatter_device(atoms, pix, phys)
         engine.sync()
         field = torch.view_as_complex(out).cpu().numpy().reshape(Nz, Ny)
         return field if return_double else field.astype(np.complex64)
+
+    def _pixels_for(self, coords, Ny, Nz, phys):
+        """The prepared pixels of these coordinates and physics: kept from
+        the previous call when both are unchanged (a detector is usually
+        fixed across exposures), so that their arrays and the pixel-grouping
+        bounds derived from them are not rebuilt every call."""
+        key = bytes(phys)
+        c = self._pix_cache
+        if (c is not None and c[1] == (Ny, Nz) and c[2] == key and c[0].shape == coords.shape
+                and np.array_equal(c[0], coords)):
+            return c[3]
+        pix = engine.Pixels(np.asarray(coords, dtype=np.float64) / 1e10, Ny, Nz, phys)
+        self._pix_cache = (np.array(coords, copy=True), (Ny, Nz), key, pix)
+        return pix
 
     def atomic_scattering_kinematic(self, sample, detector, stage, offset=None, use_gpu=True,
                                     remove_forward: bool = False, use_depth_ein: bool = False,
