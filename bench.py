@@ -469,6 +469,64 @@ def configs_leg(args, dev, reps=3):
     return out
 
 
+def gemm_profile_case():
+    """The scan surrogate's two tcgen05 GEMM shapes, each launched twice
+    (warm-up, then timed with CUDA events): (a) one MLP layer for the group
+    of two networks, 2 x (1,272 x 256 x 256), bias + ReLU epilogue with FP32
+    and BF16 outputs; (b) the frame decode, 8,334 x 16,384 x 192, epilogue
+    adding the mean frame, clamping, scaling rows and storing them at their
+    frames' rows of a 10,201-frame output. Launch order a, a, b, b (the
+    kernel-profile commands select launch 1 or 3)."""
+    import ctypes
+
+    import torch
+
+    from mosaic_gb300 import _lib, engine
+    L = _lib.load()
+    dev = torch.device("cuda")
+    p = lambda t: t.data_ptr() if t is not None else None
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    M, N, K, G = 1272, 256, 256, 2
+    A = torch.randn((G, M, K), device=dev, generator=g).bfloat16()
+    W = torch.randn((G, N, K), device=dev, generator=g).bfloat16()
+    b = torch.randn((G, N), device=dev, generator=g)
+    C = torch.empty((G, M, N), device=dev)
+    Cb = torch.empty((G, M, N), device=dev, dtype=torch.bfloat16)
+    gs = (ctypes.c_longlong * 6)(M * K, N * K, M * N, M * N, N, 0)
+    Md, Nd, Kd = 8334, 16384, 192
+    Ad = torch.randn((Md, Kd), device=dev, generator=g).bfloat16()
+    Bt = torch.randn((Nd, Kd), device=dev, generator=g).bfloat16()
+    mu = torch.randn(Nd, device=dev, generator=g)
+    scale = torch.rand(Md, device=dev, generator=g)
+    rows = torch.randperm(10201, device=dev, generator=g)[:Md].contiguous()
+    out = torch.empty((10201, Nd), device=dev)
+
+    def run_a():
+        _lib.check(L.mk_gemm_tc_groups(G, gs, M, N, K, p(A), K, 1, p(W), 1, K, p(C), N, p(b), 6,
+                                       p(Cb), N, None, 0, None, None, engine._stream_handle()))
+
+    def run_b():
+        _lib.check(L.mk_gemm_tc(Md, Nd, Kd, p(Ad), Kd, 1, p(Bt), 1, Kd, p(out), Nd, p(mu), 6, None,
+                                0, None, 0, p(scale), p(rows), engine._stream_handle()))
+
+    res = {}
+    for name, fn, flops, nbytes in (("mlp_layer_two_networks", run_a, 2.0 * G * M * N * K,
+                                     G * M * N * 6),
+                                    ("frame_decode", run_b, 2.0 * Md * Nd * Kd, Md * Nd * 4)):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[name] = {"us": ms * 1e3, "tflops": flops / ms / 1e9, "gb_s_written": nbytes / ms / 1e6}
+    _lib.check(L.mk_sync_status(engine._stream_handle()))
+    print(json.dumps({"gemm_profile": res}))
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -766,9 +824,14 @@ def main():
                     help="at most the 2x2 quad form (the 2x4 octet form off)")
     ap.add_argument("--scan-frames", type=int, default=724,
                     help="frames of the batched-scan leg (0: skip; the configuration has 724)")
+    ap.add_argument("--profile-gemm", action="store_true",
+                    help="kernel-profile case of the surrogate's tcgen05 GEMM shapes (no bench line)")
     ap.add_argument("--profile", action="store_true",
                     help="kernel-profile run: cached launch shape, timed steps only")
     args = ap.parse_args()
+    if args.profile_gemm:
+        gemm_profile_case()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
