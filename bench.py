@@ -69,11 +69,21 @@ MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD = 0.5, 9
 # headline's tiles take the first: 5.44 per term, counted as 5.4 (the lower
 # count gives the higher peak), 0.5 MUFU
 MUFU_PER_TERM_OCT, FP32_PER_TERM_OCT = 0.5, 5.4
+# 4x4 pixel-square form (four quads sharing their half differences): per
+# square and atom 65 FP32 lane operations on tiles that pass the phase
+# straight to the sin/cos (three dot products 9, the four quad phases 6, the
+# four sin/cos argument scalings 4, u^2 and v^2 2, short polynomials 6, the
+# four products of the shared u and v factors 4, 4 x 8 accumulators 32,
+# per-atom coefficients 2) and 69 with the mod-1 reduction: 4.06-4.31 per
+# term, counted as 4.0 (the lower count gives the higher peak), 0.5 MUFU
+MUFU_PER_TERM_SQ, FP32_PER_TERM_SQ = 0.5, 4.0
 FORMS = {0: ("one sin/cos per term", MUFU_PER_TERM, FP32_PER_TERM),
          1: ("pixel pairs (one sin/cos per two terms)", MUFU_PER_TERM_PAIR, FP32_PER_TERM_PAIR),
          2: ("2x2 pixel quads (one sin/cos per four terms)", MUFU_PER_TERM_QUAD, FP32_PER_TERM_QUAD),
          3: ("2x4 pixel octets (two quads sharing their half differences; one sin/cos per four "
-             "terms)", MUFU_PER_TERM_OCT, FP32_PER_TERM_OCT)}
+             "terms)", MUFU_PER_TERM_OCT, FP32_PER_TERM_OCT),
+         4: ("4x4 pixel squares (four quads sharing their half differences; one sin/cos per "
+             "four terms)", MUFU_PER_TERM_SQ, FP32_PER_TERM_SQ)}
 
 
 def _dist():
@@ -610,6 +620,8 @@ def run_ours(args):
             su.level = min(su.level, 1 if su.info["pairs_ok"] else 0)
         elif args.no_octets:
             su.level = min(su.level, 2)
+        elif args.no_squares:
+            su.level = min(su.level, 3)
         setups[T] = su
     if not setups:
         raise RuntimeError(f"{args.config}: the split form declines this geometry")
@@ -815,13 +827,15 @@ def main():
                     help="one sin/cos per term (the pixel-pair and quad forms off)")
     ap.add_argument("--launch", default="",
                     help="fixed launch shape 'pixels_per_thread,threads,mode' (mode 0 one sin/cos "
-                         "per term, 1 pairs, 2 quads, 3 octets; clamped to what the geometry "
+                         "per term, 1 pairs, 2 quads, 3 octets, 4 squares; clamped to what the geometry "
                          "allows) "
                          "instead of the autotuner's")
     ap.add_argument("--no-quads", action="store_true",
                     help="at most one sin/cos per pixel pair (the 2x2 quad and octet forms off)")
     ap.add_argument("--no-octets", action="store_true",
-                    help="at most the 2x2 quad form (the 2x4 octet form off)")
+                    help="at most the 2x2 quad form (the 2x4 octet and 4x4 square forms off)")
+    ap.add_argument("--no-squares", action="store_true",
+                    help="at most the 2x4 octet form (the 4x4 square form off)")
     ap.add_argument("--scan-frames", type=int, default=724,
                     help="frames of the batched-scan leg (0: skip; the configuration has 724)")
     ap.add_argument("--profile-gemm", action="store_true",

@@ -128,8 +128,8 @@ typedef struct {
 
 /* Launch shape of the split-phase kernel (autotuned by the host). */
 typedef struct {
-    int pix_per_thread;   /* 1, 2, 4 or 8 */
-    int threads;          /* 64, 128 or 256 */
+    int pix_per_thread;   /* 1, 2, 4 or 8; 16 with squares */
+    int threads;          /* 64, 128 or 256; 128 or 192 with squares */
     int slices;           /* tile ranges summed separately, reduced in FP64; <= 0: auto */
     int fresnel;          /* 1: keep the |d|^2 term of the in-tile distance; 0: drop it
                              (the caller checks k r_tile^2 / 2 R0_min against its budget);
@@ -148,11 +148,12 @@ typedef struct {
                              checks the half differences as for pairs and the dropped term
                              against its phase budget (pix_per_thread 4 or 8; an odd last
                              column or row repeats its pixels inside the quad).
-                             3: 2x4 pixel octets (see octet_radius_m) */
-    double pair_short_radius_m; /* with pairs or quads: tiles up to this radius keep the half
+                             3: 2x4 pixel octets (see octet_radius_m).
+                             4: 4x4 pixel squares (see octet_radius_m) */
+    double pair_short_radius_m; /* with pairs, quads, octets or squares: tiles up to this radius keep the half
                              differences below 0.07 rad and use the short polynomials
                              (0: none does) */
-    double sin_direct_max_rad; /* with quads or octets: tiles without the |d|^2 term whose
+    double sin_direct_max_rad; /* with quads, octets or squares: tiles without the |d|^2 term whose
                              in-tile phase bound stays below this [rad] pass the phase to the
                              MUFU sin/cos without the mod-1 reduction (its error grows
                              ~1e-7 |x|); 0: the library default, 100 rad; < 0: never */
@@ -161,7 +162,12 @@ typedef struct {
                              tiles up to this radius [m] take the octet form, wider ones the
                              quad form; the caller bounds the octet's dropped phase (the
                              departure of w from a plane over the 8 pixels, times k r) for
-                             that radius; <= 0: every tile takes the quad form */
+                             that radius; <= 0: every tile takes the quad form.
+                             With squares (pairs 4: four quads in a 4x4 block share their half
+                             differences, pix_per_thread 16, 128 or 192 threads, frames of whole
+                             squares: a row length and a row count that are multiples of 4)
+                             the same for the square form and the departure of w from a plane
+                             over its 16 pixels */
 } mk_launch;
 
 /* --- library ---------------------------------------------------------- */

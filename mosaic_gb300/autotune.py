@@ -34,6 +34,7 @@ CANDIDATES = [(4, 128), (4, 256), (2, 256), (8, 128), (2, 128), (8, 64), (4, 64)
 PAIR_CANDIDATES = [(4, 128), (4, 256), (8, 128), (2, 256), (8, 64)]
 QUAD_CANDIDATES = [(4, 128), (4, 256), (8, 128), (8, 64), (4, 64)]
 OCTET_CANDIDATES = [(8, 128), (8, 256), (8, 64)]
+SQUARE_CANDIDATES = [(16, 128), (16, 192)]
 TILE_SIZES = (512, 1024, 2048)
 DEFAULT_TILE_ATOMS = 1024
 DEFAULT = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
@@ -126,7 +127,7 @@ def lookup(n_pix, level=0, kind="exposure", tile_atoms=None):
             (tile_atoms is None or int(c.get("tile_atoms", DEFAULT_TILE_ATOMS)) == int(tile_atoms)):
         c.pop("tile_atoms", None)
         return c
-    return engine.default_launch(level)
+    return engine.default_launch(level, tile_atoms)
 
 
 def pick(finalists, times, level):
@@ -136,7 +137,7 @@ def pick(finalists, times, level):
     over to full problems (a 64-thread shape led the probe by 0.5 % and ran
     the 8.19M-atom step 3 % slower)."""
     best = finalists[min(range(len(times)), key=lambda i: times[i])]
-    dflt = dict(engine.default_launch(level), tile_atoms=DEFAULT_TILE_ATOMS)
+    dflt = dict(engine.default_launch(level, DEFAULT_TILE_ATOMS), tile_atoms=DEFAULT_TILE_ATOMS)
     for cfg, t in zip(finalists, times):
         c = dict(cfg)
         c.setdefault("tile_atoms", DEFAULT_TILE_ATOMS)
@@ -148,7 +149,7 @@ def pick(finalists, times, level):
 @dataclass
 class Setup:
     """One tile size's tiles and what its geometry allows: grouping
-    ``level`` (0 none, 1 pairs, 2 quads, 3 octets) with ``info`` from
+    ``level`` (0 none, 1 pairs, 2 quads, 3 octets, 4 squares) with ``info`` from
     engine.pixel_grouping, and whether the |d|^2 term is kept (``fresnel``)
     beyond ``fresnel_radius`` [m]."""
     tiles: object
@@ -166,6 +167,8 @@ def candidates_for(level, pairs_ok):
         out += [(p, t, 2) for p, t in QUAD_CANDIDATES]
     if level >= 3:
         out += [(p, t, 3) for p, t in OCTET_CANDIDATES]
+    if level >= 4:
+        out += [(p, t, 4) for p, t in SQUARE_CANDIDATES]
     return out
 
 

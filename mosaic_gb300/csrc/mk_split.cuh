@@ -58,7 +58,7 @@ struct MkSplitArgs {
     float fres_r;      // tiles wider than this [m] keep the |d|^2 term (FRESNEL kernels)
     float pair_short_r; // pair/quad kernels: tiles up to this radius [m] use the short polynomials
     float sin_direct;   // quad kernels: in-tile phase bound [rad] below which the reduction is skipped
-    float oct_r;        // octet kernels: tiles up to this radius [m] take the octet form, the rest quads
+    float oct_r;        // octet / square kernels: tiles up to this radius [m] take that form, the rest quads
     // analyser (ANA kernels, single exposures): kind 1 top-hat / 2 Darwin,
     // beam direction and analyser axis in FP64, 4 sin^2(alpha/2), half-width
     int analyser;
@@ -126,6 +126,16 @@ __device__ __forceinline__ float4 mk_ld_fold(const float4 *p)
     float4 v;
     asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
                  : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+
+// A tile's FP64 origin read again for the fold (opaque, like mk_ld_fold).
+__device__ __forceinline__ double4 mk_ld_origin(const double4 *p)
+{
+    double4 v;
+    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%4];\n\t"
+                 "ld.global.nc.v2.f64 {%2, %3}, [%4+16];"
+                 : "=d"(v.x), "=d"(v.y), "=d"(v.z), "=d"(v.w) : "l"(p));
     return v;
 }
 
@@ -586,8 +596,120 @@ __device__ __forceinline__ void mk_tile_terms_oct(
     }
 }
 
+// 4x4 pixel squares: four 2x2 quads in a 2x2 arrangement (quad j at row
+// pair j >> 1 and column pair j & 1 of the square) share one pair of half
+// differences u, v -- the means of the four quads' -- and take their quad
+// phases from the square's mean phase sigma_c: each quad centre sits one
+// pixel step from the square centre along the row and one across it, a row
+// step is 2u and a column step 2v, so
+//   2 pi sigma_j = 2 pi sigma_c + s_j 2u + t_j 2v,   s_j = +-1, t_j = +-1,
+// and inside quad j the quad form applies unchanged. Dropped beyond the
+// quad form: the departure of w over the 16 pixels from a plane, which the
+// host bounds from the FP64 pixel directions against its phase budget. Per
+// atom pair: three dot products (9), the four quad phases (6), four
+// sin/cos, u^2 and v^2 (2), the polynomials (6), the four products of the
+// shared factors (4) and 4 x 8 accumulators (32): ~61 FP32 lane operations
+// per 16 terms (3.8 a term, against 5.4 for octets), with the MUFU doing
+// one sin/cos per 4 terms as in every quad form.
+// acc[j][0..7] = K, R, S, Q (re, im) of quad j, f32x2 over atoms 2q, 2q+1.
+template <bool FR, bool CPLX, bool SHORT, bool RAD>
+__device__ __forceinline__ void mk_tile_terms_sq(
+    const float4 *__restrict__ P, const float4 *__restrict__ E, int T, mk_f2 sx, mk_f2 sy, mk_f2 sz,
+    mk_f2 ux, mk_f2 uy, mk_f2 uz, mk_f2 vx, mk_f2 vy, mk_f2 vz, mk_f2 hq, mk_f2 bx, mk_f2 by,
+    mk_f2 bz, mk_f2 (&acc)[4][8])
+{
+    const mk_f2 magic = f2_splat(MK_ROUND_MAGIC), two_pi = f2_splat(TWO_PI_F);
+    const mk_f2 one = f2_splat(1.f), m_one = f2_splat(-1.f);
+    const mk_f2 two = f2_splat(2.f), m_two = f2_splat(-2.f);
+    const mk_f2 k2 = f2_splat(-0.5f), k3 = f2_splat(-1.f / 6.f);
+    const mk_f2 k4 = f2_splat(1.f / 24.f), k5 = f2_splat(1.f / 120.f), k6 = f2_splat(-1.f / 720.f);
+    const ulonglong2 *P2 = reinterpret_cast<const ulonglong2 *>(P);
+    const ulonglong2 *E2 = reinterpret_cast<const ulonglong2 *>(E);
+#pragma unroll (kPairUnroll)
+    for (int q = 0; q < T / 2; ++q) {
+        const ulonglong2 A = P2[2 * q], B = P2[2 * q + 1], M = E2[q];
+        const mk_f2 X = A.x, Y = A.y, Z = B.x, W = B.y, ER = M.x, EI = M.y;
+        const mk_f2 e0 = CPLX ? one : ER;
+        const mk_f2 c2 = f2_mul(e0, k2), s2 = f2_mul(e0, k3);
+        mk_f2 c4 = 0ull, s4 = 0ull, c6 = 0ull;
+        if (!SHORT) {
+            c4 = f2_mul(e0, k4);
+            s4 = f2_mul(e0, k5);
+            c6 = f2_mul(e0, k6);
+        }
+        mk_f2 sig = f2_fma(Z, sz, f2_fma(Y, sy, f2_mul(X, sx)));
+        if (FR) {
+            const mk_f2 db = f2_fma(Z, bz, f2_fma(Y, by, f2_mul(X, bx)));
+            const mk_f2 sp = f2_sub(db, sig);
+            sig = f2_fma(f2_fma(f2_mul(sp, m_one), sp, W), hq, sig);
+        }
+        const mk_f2 du = f2_fma(Z, uz, f2_fma(Y, uy, f2_mul(X, ux)));
+        const mk_f2 dv = f2_fma(Z, vz, f2_fma(Y, vy, f2_mul(X, vx)));
+        const mk_f2 rc = RAD ? sig : f2_mul(f2_sub(sig, f2_sub(f2_add(sig, magic), magic)), two_pi);
+        // quad phases: rows t = -1 (quads 0, 1) and t = +1 (quads 2, 3),
+        // columns s = -1 (quads 0, 2) and s = +1 (quads 1, 3)
+        const mk_f2 rlo = f2_fma(dv, m_two, rc), rhi = f2_fma(dv, two, rc);
+        const float2 r0 = f2_unpack(f2_fma(du, m_two, rlo));
+        const float2 r1 = f2_unpack(f2_fma(du, two, rlo));
+        const float2 r2 = f2_unpack(f2_fma(du, m_two, rhi));
+        const float2 r3 = f2_unpack(f2_fma(du, two, rhi));
+        mk_f2 ec[4], es[4];
+        {
+            float s0, c0, s1, c1;
+            __sincosf(r0.x, &s0, &c0);
+            __sincosf(r0.y, &s1, &c1);
+            ec[0] = f2_pack(c0, c1); es[0] = f2_pack(s0, s1);
+            __sincosf(r1.x, &s0, &c0);
+            __sincosf(r1.y, &s1, &c1);
+            ec[1] = f2_pack(c0, c1); es[1] = f2_pack(s0, s1);
+            __sincosf(r2.x, &s0, &c0);
+            __sincosf(r2.y, &s1, &c1);
+            ec[2] = f2_pack(c0, c1); es[2] = f2_pack(s0, s1);
+            __sincosf(r3.x, &s0, &c0);
+            __sincosf(r3.y, &s1, &c1);
+            ec[3] = f2_pack(c0, c1); es[3] = f2_pack(s0, s1);
+        }
+        if (CPLX) {
+            const mk_f2 EIn = f2_mul(EI, m_one);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const mk_f2 c = ec[j];
+                ec[j] = f2_fma(ER, c, f2_mul(EIn, es[j]));
+                es[j] = f2_fma(ER, es[j], f2_mul(EI, c));
+            }
+        }
+        const mk_f2 u2 = f2_mul(du, du), v2 = f2_mul(dv, dv);
+        mk_f2 cu, su, cv, sv;
+        if (SHORT) {
+            cu = f2_fma(u2, c2, e0);
+            su = f2_mul(du, f2_fma(u2, s2, e0));
+            cv = f2_fma(v2, k2, one);
+            sv = f2_mul(dv, f2_fma(v2, k3, one));
+        } else {
+            cu = f2_fma(u2, f2_fma(u2, f2_fma(u2, c6, c4), c2), e0);
+            su = f2_mul(du, f2_fma(u2, f2_fma(u2, s4, s2), e0));
+            cv = f2_fma(v2, f2_fma(v2, f2_fma(v2, k6, k4), k2), one);
+            sv = f2_mul(dv, f2_fma(v2, f2_fma(v2, k5, k3), one));
+        }
+        const mk_f2 pcc = f2_mul(cu, cv), pcs = f2_mul(cu, sv);
+        const mk_f2 psc = f2_mul(su, cv), pss = f2_mul(su, sv);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            acc[j][0] = f2_fma(ec[j], pcc, acc[j][0]);
+            acc[j][1] = f2_fma(es[j], pcc, acc[j][1]);
+            acc[j][2] = f2_fma(ec[j], pcs, acc[j][2]);
+            acc[j][3] = f2_fma(es[j], pcs, acc[j][3]);
+            acc[j][4] = f2_fma(ec[j], psc, acc[j][4]);
+            acc[j][5] = f2_fma(es[j], psc, acc[j][5]);
+            acc[j][6] = f2_fma(ec[j], pss, acc[j][6]);
+            acc[j][7] = f2_fma(es[j], pss, acc[j][7]);
+        }
+    }
+}
+
 // PM (pixel mode): 0 one sin/cos a term, 1 pixel pairs, 2 pixel quads, 3
-// pixel octets (2x4: two quads sharing their half differences).
+// pixel octets (2x4: two quads sharing their half differences), 4 pixel
+// squares (4x4: four quads sharing them).
 // Blocks per SM the register allocation is held to: the 8-pixel quad kernels
 // (their per-pixel state lives in shared memory) aim at MK_QUAD8_WARPS warps
 // per SM, the rest are free.
@@ -597,11 +719,15 @@ __device__ __forceinline__ void mk_tile_terms_oct(
 #ifndef MK_OCT_WARPS
 #define MK_OCT_WARPS 12
 #endif
+#ifndef MK_SQ_WARPS
+#define MK_SQ_WARPS 12
+#endif
 template <int NT, int PIX, int PM, bool ANA>
 constexpr int mk_min_blocks()
 {
     return (PM == 2 && PIX == 8 && !ANA && MK_QUAD8_WARPS * 32 / NT > 1) ? MK_QUAD8_WARPS * 32 / NT
            : (PM == 3 && MK_OCT_WARPS * 32 / NT > 1)                  ? MK_OCT_WARPS * 32 / NT
+           : (PM == 4 && MK_SQ_WARPS * 32 / NT > 1)                   ? MK_SQ_WARPS * 32 / NT
                                                                        : 1;
 }
 
@@ -793,6 +919,131 @@ __device__ __forceinline__ void mk_octet_tile(const MkSplitArgs &A, const mk_fra
     }
 }
 
+// The 4x4 pixel-square form for one tile (pixels 4j..4j+3 are the thread's
+// quad j = a, b, c, d at row pair j >> 1 and column pair j & 1).
+template <bool CPLX>
+__device__ __forceinline__ void mk_square_tile(const MkSplitArgs &A, const mk_frame_desc &F,
+                                               const double4 &o, bool fr_tile,
+                                               const float4 *__restrict__ P,
+                                               const float4 *__restrict__ E, int T,
+                                               const float (&wx)[16], const float (&wy)[16],
+                                               const float (&wz)[16], const float (&hq)[16],
+                                               float (&csr)[16], float (&csi)[16])
+{
+    // square vectors: mean w of the 16 pixels, and the four quads' mean
+    // half-difference vectors along the row (u) and across rows (v)
+    const float hpi4 = 0.392699081698724f;   // (pi/2) / 4 quads
+    float msx = 0.f, msy = 0.f, msz = 0.f, mh = 0.f;
+    float ax = 0.f, ay = 0.f, az = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+        msx += wx[p]; msy += wy[p]; msz += wz[p]; mh += hq[p];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int a = 4 * j, b = a + 1, c = a + 2, d = a + 3;
+        ax += (wx[b] - wx[a]) + (wx[d] - wx[c]);
+        ay += (wy[b] - wy[a]) + (wy[d] - wy[c]);
+        az += (wz[b] - wz[a]) + (wz[d] - wz[c]);
+        cx += (wx[c] - wx[a]) + (wx[d] - wx[b]);
+        cy += (wy[c] - wy[a]) + (wy[d] - wy[b]);
+        cz += (wz[c] - wz[a]) + (wz[d] - wz[b]);
+    }
+    ax *= hpi4; ay *= hpi4; az *= hpi4; cx *= hpi4; cy *= hpi4; cz *= hpi4;
+    msx *= 0.0625f; msy *= 0.0625f; msz *= 0.0625f; mh *= 0.0625f;
+    mk_f2 acc[4][8];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int m = 0; m < 8; ++m) acc[j][m] = 0ull;
+    const mk_f2 bx = f2_splat(F.b[0]), by = f2_splat(F.b[1]), bz = f2_splat(F.b[2]);
+    const bool short_tile = (float)o.w <= A.pair_short_r;
+    // direct sin/cos argument (warp-uniform): the quad phases reach
+    // kappa r (2 pi |s| + 2 |u| + 2 |v|)
+    bool rad = false;
+    if (!fr_tile && short_tile) {
+        const float bound = (TWO_PI_F * sqrtf(fmaf(msz, msz, fmaf(msy, msy, msx * msx))) +
+                             2.f * sqrtf(fmaf(az, az, fmaf(ay, ay, ax * ax))) +
+                             2.f * sqrtf(fmaf(cz, cz, fmaf(cy, cy, cx * cx)))) *
+                            A.kappa * (float)o.w;
+        rad = __all_sync(0xffffffffu, bound <= A.sin_direct);
+    }
+    const mk_f2 ux = f2_splat(ax), uy = f2_splat(ay), uz = f2_splat(az);
+    const mk_f2 vx = f2_splat(cx), vy = f2_splat(cy), vz = f2_splat(cz);
+    const mk_f2 hp = f2_splat(mh);
+    if (rad) {
+        const mk_f2 sx = f2_splat(msx * TWO_PI_F), sy = f2_splat(msy * TWO_PI_F),
+                    sz = f2_splat(msz * TWO_PI_F);
+        mk_tile_terms_sq<false, CPLX, true, true>(P, E, T, sx, sy, sz, ux, uy, uz, vx, vy, vz,
+                                                  hp, bx, by, bz, acc);
+    } else {
+        const mk_f2 sx = f2_splat(msx), sy = f2_splat(msy), sz = f2_splat(msz);
+        if (fr_tile) {
+            if (short_tile)
+                mk_tile_terms_sq<true, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy, uz, vx,
+                                                          vy, vz, hp, bx, by, bz, acc);
+            else
+                mk_tile_terms_sq<true, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy, uz, vx,
+                                                           vy, vz, hp, bx, by, bz, acc);
+        } else {
+            if (short_tile)
+                mk_tile_terms_sq<false, CPLX, true, false>(P, E, T, sx, sy, sz, ux, uy, uz, vx,
+                                                           vy, vz, hp, bx, by, bz, acc);
+            else
+                mk_tile_terms_sq<false, CPLX, false, false>(P, E, T, sx, sy, sz, ux, uy, uz,
+                                                            vx, vy, vz, hp, bx, by, bz, acc);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float h[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const float2 t2 = f2_unpack(acc[j][m]);   // halves: even, odd atoms
+            h[m] = t2.x + t2.y;
+        }
+        const float Kr = h[0], Ki = h[1], Rr = h[2], Ri = h[3];
+        const float Sr = h[4], Si = h[5], Qr = h[6], Qi = h[7];
+        // A(s, t) = K - s t Q + i t R + i s S
+        csr[4 * j] = (Kr - Qr) + (Ri + Si);       // a (-, -)
+        csi[4 * j] = (Ki - Qi) - (Rr + Sr);
+        csr[4 * j + 1] = (Kr + Qr) + (Ri - Si);   // b (+, -)
+        csi[4 * j + 1] = (Ki + Qi) - (Rr - Sr);
+        csr[4 * j + 2] = (Kr + Qr) - (Ri - Si);   // c (-, +)
+        csi[4 * j + 2] = (Ki + Qi) + (Rr - Sr);
+        csr[4 * j + 3] = (Kr - Qr) - (Ri + Si);   // d (+, +)
+        csi[4 * j + 3] = (Ki - Qi) + (Rr + Sr);
+    }
+}
+
+// Tiles wider than the square form's radius: the square's four quads on
+// their own, two at a time (the 2-quad loop; its register use stays below
+// the square loop's).
+template <bool CPLX>
+__device__ __forceinline__ void mk_square_quads_tile(const MkSplitArgs &A, const mk_frame_desc &F,
+                                                     const double4 &o, bool fr_tile,
+                                                     const float4 *__restrict__ P,
+                                                     const float4 *__restrict__ E, int T,
+                                                     const float (&wx)[16], const float (&wy)[16],
+                                                     const float (&wz)[16], const float (&hq)[16],
+                                                     float (&csr)[16], float (&csi)[16])
+{
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float hx[8], hy[8], hz[8], hh[8], hr[8], hi[8];
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            hx[p] = wx[8 * h + p]; hy[p] = wy[8 * h + p]; hz[p] = wz[8 * h + p]; hh[p] = hq[8 * h + p];
+        }
+        mk_quads_tile<2, CPLX>(A, F, o, fr_tile, P, E, T, hx, hy, hz, hh, hr, hi);
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            csr[8 * h + p] = hr[p];
+            csi[8 * h + p] = hi[p];
+        }
+    }
+}
+
 template <int NT, int PIX, bool FRESNEL, bool CPLX, int PM, bool ANA>
 __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
     mk_split_kernel(const __grid_constant__ MkSplitArgs A)
@@ -808,7 +1059,7 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
     // with it and w rebuilt in the fold they fit three 128-thread blocks per
     // SM (152 registers) instead of two (234); measured +2 % on the 8.19M-atom
     // step, while the 4-pixel kernels (126 registers already) lost 1.4 %.
-    constexpr bool KS = ((PM == 2 || PM == 3) && PIX == 8);
+    constexpr bool KS = ((PM == 2 || PM == 3) && PIX == 8) || (PM == 4 && PIX == 16);
     float4 *s_kahan = reinterpret_cast<float4 *>(s_amp + 2 * T);
     const int tid = threadIdx.x;
     const uint32_t tile_bytes = (uint32_t)T * (uint32_t)(sizeof(float4) + sizeof(float2));
@@ -850,6 +1101,17 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
         }
 
         int pix[PIX];
+        // squares: the thread's pixels from the square's first pixel and the
+        // row length (two registers across the tile loop instead of 16)
+        int sqb = 0, sqr = 0;
+        auto pixat = [&](int p) -> int {
+            if constexpr (PM == 4)
+                return sqb >= F.n_pix ? F.n_pix
+                                      : sqb + (2 * (p >> 3) + ((p >> 1) & 1)) * sqr +
+                                            2 * ((p >> 2) & 1) + (p & 1);
+            else
+                return pix[p];
+        };
         float accr[PIX], acci[PIX], cmpr[PIX], cmpi[PIX];
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
@@ -885,6 +1147,23 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
             } else {
 #pragma unroll
                 for (int p = 0; p < PIX; ++p) pix[p] = F.n_pix;
+            }
+        }
+        if constexpr (PM == 4) {
+            // square of the thread: rows 4 gz .. 4 gz + 3, columns 4 gy ..
+            // 4 gy + 3; quad j at rows 4 gz + 2 (j >> 1) (+1), columns
+            // 4 gy + 2 (j & 1) (+1). The planner admits only frames of whole
+            // squares (row % 4 == 0, row count % 4 == 0); past the last square
+            // the pixels get n_pix (loads clamp, stores skip).
+            static_assert(PIX == 16, "squares are 16 pixels a thread");
+            const int row = max(F.row, 1), rows = F.n_pix / row;
+            const int gpr = row >> 2, n_sq = gpr * (rows >> 2);
+            const int gi = pb * NT + tid;
+            sqr = row;
+            sqb = F.n_pix;
+            if (gi < n_sq) {
+                const int gz = gi / gpr, gy = gi - gz * gpr;
+                sqb = 4 * gz * row + 4 * gy;   // pixel 4j + e at sqb + pixat's offset
             }
         }
         if constexpr (PM == 2) {
@@ -923,7 +1202,7 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
             float wx[PIX], wy[PIX], wz[PIX], hq[PIX];
 #pragma unroll
             for (int p = 0; p < PIX; ++p) {
-                const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
+                const long long g = F.pix_off + min(pixat(p), F.n_pix - 1);
                 const float4 uu = A.u[g];
                 const float uo = fmaf(uu.z, oz, fmaf(uu.y, oy, uu.x * ox));
                 wx[p] = F.b[0] - (uu.x - (ox - uo * uu.x) * uu.w);
@@ -942,7 +1221,7 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                 bool need_atom = false, all_zero = true;
 #pragma unroll
                 for (int p = 0; p < PIX; ++p) {
-                    const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
+                    const long long g = F.pix_off + min(pixat(p), F.n_pix - 1);
                     const double4 qq = A.q[g];
                     const double ip = (double)A.u[g].w;
                     const double ux = A.an_b[0] - qq.x * A.inv_kappa;
@@ -991,7 +1270,7 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                     } else {
                         ag0[p] = 1.f;
                     }
-                    if (pix[p] < F.n_pix && ag0[p] != 0.f) all_zero = false;
+                    if (pixat(p) < F.n_pix && ag0[p] != 0.f) all_zero = false;
                 }
                 warp_atom = __any_sync(0xffffffffu, need_atom);
                 warp_zero = __all_sync(0xffffffffu, all_zero && !need_atom);
@@ -1028,6 +1307,13 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                 else
                     mk_tile_terms_ana<PIX, false, CPLX>(P, E, T, wx, wy, wz, hq, F.b[0], F.b[1], F.b[2],
                                                         agx, agy, agz, ath, ag0, ag1, csr, csi);
+            } else if constexpr (PM == 4) {
+                // tiles wider than the square form's radius (the host bounds
+                // its dropped phase per radius): the square's quads on their own
+                if ((float)o.w > A.oct_r)
+                    mk_square_quads_tile<CPLX>(A, F, o, fr_tile, P, E, T, wx, wy, wz, hq, csr, csi);
+                else
+                    mk_square_tile<CPLX>(A, F, o, fr_tile, P, E, T, wx, wy, wz, hq, csr, csi);
             } else if constexpr (PM == 3) {
                 // tiles wider than the octet form's radius (the host bounds its
                 // dropped phase per radius): the thread's two quads on their own
@@ -1105,24 +1391,29 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                 mk_issue_tile(A, s_pos, s_amp, bar, buf, t + 2, T, tile_bytes);
             }
             // Fold: tile sum x factor x exp(2 pi i phi0), Kahan-compensated.
+            // The square kernels read the tile origin again here rather
+            // than keep it across the atom loop (registers).
             const int s = A.tspecies[t];
-            const float oo = fmaf(oz, oz, fmaf(oy, oy, ox * ox));
+            const double4 of = PM == 4 ? mk_ld_origin(A.origin + t) : o;
+            const float fox = PM == 4 ? (float)of.x : ox, foy = PM == 4 ? (float)of.y : oy,
+                        foz = PM == 4 ? (float)of.z : oz;
+            const float oo = fmaf(foz, foz, fmaf(foy, foy, fox * fox));
 #pragma unroll
             for (int p = 0; p < PIX; ++p) {
-                const long long g = F.pix_off + min(pix[p], F.n_pix - 1);
+                const long long g = F.pix_off + min(pixat(p), F.n_pix - 1);
                 const float4 uu = KS ? mk_ld_fold(A.u + g) : A.u[g];
                 const double4 qq = A.q[g];
-                const float uo = fmaf(uu.z, oz, fmaf(uu.y, oy, uu.x * ox));
-                const double q0 = qq.x * o.x + qq.y * o.y + qq.z * o.z;
+                const float uo = fmaf(uu.z, foz, fmaf(uu.y, foy, uu.x * fox));
+                const double q0 = qq.x * of.x + qq.y * of.y + qq.z * of.z;
                 float ph = (float)(q0 - rint(q0)) + A.kappa * 0.5f * fmaf(-uo, uo, oo) * uu.w;
                 ph -= rintf(ph);
                 float s0, c0;
                 __sincosf(ph * TWO_PI_F, &s0, &c0);
                 float fx = wx[p], fy = wy[p], fz = wz[p];
                 if constexpr (KS && !ANA) {   // w again, from the fresh load
-                    fx = F.b[0] - (uu.x - (ox - uo * uu.x) * uu.w);
-                    fy = F.b[1] - (uu.y - (oy - uo * uu.y) * uu.w);
-                    fz = F.b[2] - (uu.z - (oz - uo * uu.z) * uu.w);
+                    fx = F.b[0] - (uu.x - (fox - uo * uu.x) * uu.w);
+                    fy = F.b[1] - (uu.y - (foy - uo * uu.y) * uu.w);
+                    fz = F.b[2] - (uu.z - (foz - uo * uu.z) * uu.w);
                 }
                 const float2 Fc = mk_factor(A, s, F, fx, fy, fz, (float)qq.w,
                                             1.f / fmaf(-uo, uu.w, 1.f));
@@ -1155,8 +1446,8 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                 const float4 k4 = s_kahan[p * NT + tid];
                 accr[p] = k4.x; acci[p] = k4.y; cmpr[p] = k4.z; cmpi[p] = k4.w;
             }
-            if (pix[p] < F.n_pix && ((keep >> p) & 1u))
-                A.partial[F.part_off + (long long)slice * F.n_pix + pix[p]] =
+            if (pixat(p) < F.n_pix && ((keep >> p) & 1u))
+                A.partial[F.part_off + (long long)slice * F.n_pix + pixat(p)] =
                     make_double2((double)accr[p] - (double)cmpr[p], (double)acci[p] - (double)cmpi[p]);
         }
     }
@@ -1205,6 +1496,9 @@ mk_split_fn mk_pick_quad(int nt, int pix, bool fresnel, bool cplx, bool ana);
 // Pixel-octet instances (64/128/256 threads, 8 pixels a thread, no
 // analyser); defined in mk_split_oct.cu.
 mk_split_fn mk_pick_oct(int nt, int pix, bool fresnel, bool cplx, bool ana);
+// Pixel-square instances (128 or 192 threads, 16 pixels a thread, no
+// analyser); defined in mk_split_sq.cu and mk_split_sq192.cu.
+mk_split_fn mk_pick_sq(int nt, int pix, bool fresnel, bool cplx, bool ana);
 
 #define MK_PIX_CASES(NT_)                                                  \
     switch (pix) {                                                         \

@@ -165,6 +165,7 @@ int mk_launch_reduce(const double2 *partial, int slices, int n_pix, const double
 // ----------------------------------------------------------------- launch
 static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, int pair, bool ana)
 {
+    if (pair == 4) return mk_pick_sq(nt, pix, fresnel, cplx, ana);
     if (pair == 3) return mk_pick_oct(nt, pix, fresnel, cplx, ana);
     if (pair == 2) return mk_pick_quad(nt, pix, fresnel, cplx, ana);
     switch (nt) {
@@ -175,12 +176,13 @@ static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, int pair, b
     }
 }
 
-// Two tile buffers; 8-pixel quad and octet kernels add their per-pixel
-// Kahan state.
+// Two tile buffers; 8-pixel quad, octet and square kernels add their
+// per-pixel Kahan state.
 static size_t mk_split_smem(int T, const mk_launch *launch)
 {
     size_t b = 128 + (size_t)2 * T * (sizeof(float4) + sizeof(float2));
-    if ((launch->pairs == 2 || launch->pairs == 3) && launch->pix_per_thread == 8)
+    if (((launch->pairs == 2 || launch->pairs == 3) && launch->pix_per_thread == 8) ||
+        (launch->pairs == 4 && launch->pix_per_thread == 16))
         b += sizeof(float4) * (size_t)launch->pix_per_thread * launch->threads;
     return b;
 }
@@ -199,7 +201,9 @@ static int mk_launch_shape(int tile_atoms, const mk_launch *launch, MkLaunchShap
                launch->threads, launch->pix_per_thread, launch->pairs,
                ana ? " with the analyser (128/256 threads; 2/4 pixels, or quads with 4/8; no pairs)"
                    : (launch->pairs == 2 ? " (quads: 4 or 8 pixels a thread)"
-                      : launch->pairs == 3 ? " (octets: 8 pixels a thread, no analyser)" : ""));
+                      : launch->pairs == 3 ? " (octets: 8 pixels a thread, no analyser)"
+                      : launch->pairs == 4 ? " (squares: 16 pixels, 128 or 192 threads, no analyser)"
+                                           : ""));
     const size_t smem = mk_split_smem(tile_atoms, launch);
     MK_CHECK_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
@@ -234,10 +238,10 @@ extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const int *fr
                    n_items_out && n_partial_out,
                "mk_scan_plan: null argument or no frames");
     MK_REQUIRE(tiles->n_tiles >= 1, "mk_scan_plan: no tiles");
-    MK_REQUIRE(launch->pairs >= 0 && launch->pairs <= 3,
-               "mk_scan_plan: pairs must be 0, 1, 2 or 3");
+    MK_REQUIRE(launch->pairs >= 0 && launch->pairs <= 4,
+               "mk_scan_plan: pairs must be 0, 1, 2, 3 or 4");
     if (launch->pairs >= 2) {
-        MK_REQUIRE(frame_rows, "mk_scan_plan: pixel quads and octets need the row length of every frame");
+        MK_REQUIRE(frame_rows, "mk_scan_plan: pixel quads, octets and squares need the row length of every frame");
         for (int f = 0; f < n_frames; ++f)
             MK_REQUIRE(frame_rows[f] >= 1 && frame_pixels[f] % frame_rows[f] == 0,
                        "mk_scan_plan: frame %d: %d pixels are not whole rows of %d",
@@ -250,12 +254,19 @@ extern "C" int mk_scan_plan(int n_frames, const int *frame_pixels, const int *fr
                        "multiple of 4 pixels and an even row count are needed",
                        f, frame_rows[f], frame_pixels[f] / frame_rows[f]);
     }
+    if (launch->pairs == 4) {
+        for (int f = 0; f < n_frames; ++f)
+            MK_REQUIRE(frame_rows[f] % 4 == 0 && (frame_pixels[f] / frame_rows[f]) % 4 == 0,
+                       "mk_scan_plan: frame %d (%d x %d pixels) is not whole 4x4 squares: rows of a "
+                       "multiple of 4 pixels and a row count that is a multiple of 4 are needed",
+                       f, frame_rows[f], frame_pixels[f] / frame_rows[f]);
+    }
     MkLaunchShape sh;
     int rc = mk_launch_shape(tiles->tile_atoms, launch, &sh);
     if (rc != MK_OK) return rc;
     const int ppb = launch->threads * launch->pix_per_thread;
     // pixel slots of a frame: quads round both sides up to even (the odd
-    // edge repeats its pixels); octets tile the frame exactly
+    // edge repeats its pixels); octets and squares tile the frame exactly
     auto slots = [&](int f) -> long long {
         if (launch->pairs != 2) return frame_pixels[f];
         const long long row = frame_rows[f], rows = frame_pixels[f] / row;

@@ -282,6 +282,54 @@ class Pixels:
         self._octet_steps = dict(plane=plane, extent=extent, step=step)
         return dict(self._octet_steps)
 
+    def squares_fit(self):
+        """True when every frame is whole 4x4 squares: a row length and a
+        row count that are multiples of 4."""
+        return all(ny % 4 == 0 and nz % 4 == 0 for ny, nz in self.shapes)
+
+    def square_steps(self):
+        """Departure from a plane of the FP64 unit vectors u to the pixels
+        over the 4x4 squares of every frame (rows 4i..4i+3, columns
+        4j..4j+3), exactly as the square kernels model them: the mean of the
+        16 u plus the column offset (-1.5..1.5) times the mean row step of
+        the four quads (their steps b - a and d - c) plus the row offset
+        times their mean column step (c - a, d - b). Returns the largest
+        norm of that residual (``plane``), the largest |u - mean|
+        (``extent``) and the largest mean step (``step``); None when a frame
+        is not whole squares. Computed once per Pixels object."""
+        if getattr(self, "_square_steps", None) is not None:
+            return dict(self._square_steps)
+        if not self.squares_fit():
+            return None
+        x = self.xyz
+        u = x / torch.linalg.vector_norm(x, dim=1, keepdim=True)
+        groups = {}
+        for (off, m), shp in zip(self.spans, self.shapes):
+            groups.setdefault(shp, []).append(off)
+        parts = []
+        mo = (torch.arange(4, device=u.device, dtype=u.dtype) - 1.5).view(1, 1, 1, 4, 1)
+        to = (torch.arange(4, device=u.device, dtype=u.dtype) - 1.5).view(1, 4, 1, 1, 1)
+        nrm = lambda t: torch.linalg.vector_norm(t, dim=-1).amax()
+        for (ny, nz), offs in groups.items():
+            m = ny * nz
+            if len(offs) == 1:
+                U = u[offs[0]:offs[0] + m]
+            else:
+                idx = (torch.as_tensor(offs, device=u.device)[:, None] +
+                       torch.arange(m, device=u.device)[None, :])
+                U = u[idx.reshape(-1)]
+            U = U.reshape(-1, 4, ny // 4, 4, 3)          # (row quads, 4, squares, 4, 3)
+            mean = U.mean(dim=(1, 3), keepdim=True)
+            # within-quad steps only: columns 0->1 and 2->3, rows 0->1 and 2->3
+            g = (U[:, :, :, 1::2] - U[:, :, :, 0::2]).mean(dim=(1, 3), keepdim=True)
+            h = (U[:, 1::2] - U[:, 0::2]).mean(dim=(1, 3), keepdim=True)
+            res = U - (mean + mo * g + to * h)
+            parts.append(torch.stack([nrm(res), nrm(U - mean),
+                                      torch.maximum(nrm(g), nrm(h))]))
+        plane, extent, step = torch.stack(parts).amax(0).tolist()
+        self._square_steps = dict(plane=plane, extent=extent, step=step)
+        return dict(self._square_steps)
+
 
 @dataclass
 class Atoms:
@@ -465,12 +513,24 @@ class Tiles:
 DEFAULT_LAUNCH = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
 
 
-def default_launch(level=0):
+SQUARE_MAX_TILE_ATOMS = 512
+
+
+def default_launch(level=0, tile_atoms=None):
     """Untuned launch shape for a pixel-sharing level (0 none, 1 pairs, 2
-    quads, 3 octets): quads run two per thread (8 pixels; measured 1.6-2 %
-    above one on the 8.19M-atom exposure and the 128^2 scan frames), octets
-    are 8 pixels a thread."""
-    return dict(DEFAULT_LAUNCH, pairs=int(level), pix_per_thread=8 if int(level) >= 2 else 4)
+    quads, 3 octets, 4 squares): quads run two per thread (8 pixels;
+    measured 1.6-2 % above one on the 8.19M-atom exposure and the 128^2 scan
+    frames), octets are 8 pixels a thread, squares 16. Squares only with
+    tiles of at most SQUARE_MAX_TILE_ATOMS atoms (``tile_atoms``; None
+    counts as the default 1024): with larger tiles three 128-thread square
+    blocks do not fit an SM's shared memory, and at two blocks the square
+    kernel ran the 8.19M-atom exposure 1.5 % slower than octets, against
+    12 % faster at three."""
+    level = int(level)
+    if level >= 4 and (tile_atoms or 1024) > SQUARE_MAX_TILE_ATOMS:
+        level = 3
+    ppt = 16 if level >= 4 else 8 if level >= 2 else 4
+    return dict(DEFAULT_LAUNCH, pairs=level, pix_per_thread=ppt)
 PAIR_DELTA_MAX = 0.5     # rad: the long pair polynomials are then exact to ~2e-6 per term
 PAIR_SHORT_DELTA = 0.07  # rad: the short ones to 1e-6 (the kernel's MK_PAIR_SHORT_DELTA)
 
@@ -561,6 +621,36 @@ def octet_bounds(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0):
     return dict(radius_m=radius, cross=rate * r_eff + fixed, **st)
 
 
+def square_bounds(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0):
+    """Largest tile radius [m] whose 4x4 pixel-square form stays within the
+    phase budget, or None when a frame is not whole squares.
+
+    As ``octet_bounds`` for the square's 16 pixels: the residual of the FP64
+    pixel directions from the kernel's plane (``Pixels.square_steps``),
+    widened for the tile-origin term of w -- whose part quadratic in the
+    pixel offsets (m, t) (columns and rows, -1.5..1.5 steps s) is
+    (m^2 (g.o) g + t^2 (h.o) h + m t ((g.o) h + (h.o) g)) / |P|, off the
+    plane by at most (1 + 1 + 2 x 2.25) |o| s^2 / |P| over the square (2.5
+    over an octet, where the bound takes 12: the same margin gives 32) --
+    times k r, plus 4 ``fresnel_rad`` x the square's extent for the |d|^2
+    term taken at its centre. Tiles wider than the returned radius take the
+    quad form inside the square kernel. Returns dict(radius_m, cross (the
+    bound at min(radius, widest tile)), plane, extent, step)."""
+    st = pix.square_steps()
+    if st is None:
+        return None
+    r0 = max(pix.r0_min(), 1e-300)
+    o_ratio = tiles.max_origin_norm() / r0 if tiles.n_tiles else 0.0
+    grow = 1.0 + 2.0 * o_ratio
+    plane = st["plane"] * grow + 32.0 * o_ratio * st["step"] ** 2
+    rate = float(k) * plane * 1.05                      # rad per metre of tile radius
+    fixed = 4.0 * float(fresnel_rad) * st["extent"]
+    room = float(budget_rad) - fixed
+    radius = room / rate if (room > 0.0 and rate > 0.0) else (1.0 if room > 0.0 else 0.0)
+    r_eff = min(radius, tiles.max_radius()) if tiles.n_tiles else 0.0
+    return dict(radius_m=radius, cross=rate * r_eff + fixed, **st)
+
+
 def tile_fraction_within(tiles, radius_m):
     """Fraction of the tiles whose radius is at most ``radius_m``."""
     if not tiles.n_tiles:
@@ -571,7 +661,7 @@ def tile_fraction_within(tiles, radius_m):
 
 def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=False):
     """Widest legal sharing of one sin/cos between neighbouring pixels:
-    (level, info) with level 3 octets, 2 quads, 1 pairs, 0 none, and
+    (level, info) with level 4 squares, 3 octets, 2 quads, 1 pairs, 0 none, and
     info["pairs_ok"] whether pairs alone are legal. Pairs need ``pair_delta``
     <= PAIR_DELTA_MAX (a pair across a row end, with an odd row length,
     breaks it); quads need their half differences within it and their
@@ -579,7 +669,9 @@ def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=
     two quads sharing their half differences) need frames of whole octets
     and at least OCTET_MIN_TILE_FRACTION of the tiles narrow enough for
     their dropped phase to fit the budget (``octet_bounds``; the wider tiles
-    take the quad form). ``analyser`` (0 off,
+    take the quad form); squares (4x4: four quads sharing them) need that
+    and the same of frames of whole squares and of their own radius
+    (``square_bounds``). ``analyser`` (0 off,
     1 top-hat, 2 Darwin): the analyser kernels have quads for the top-hat
     (tiles the acceptance edge cuts take the per-atom loop) and no pairs or
     octets; a Darwin analyser expands per atom on every tile, so it shares
@@ -600,6 +692,13 @@ def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=
                 info.update(octet_cross_rad=ob["cross"], octet_radius_m=ob["radius_m"],
                             octet_tile_fraction=frac)
                 if frac >= OCTET_MIN_TILE_FRACTION:
+                    sb = square_bounds(tiles, pix, k, budget_rad, fresnel_rad)
+                    if sb is not None and sb["radius_m"] > 0.0:
+                        sfrac = tile_fraction_within(tiles, sb["radius_m"])
+                        info.update(square_cross_rad=sb["cross"], square_radius_m=sb["radius_m"],
+                                    square_tile_fraction=sfrac)
+                        if sfrac >= OCTET_MIN_TILE_FRACTION:
+                            return 4, info
                     return 3, info
         return 2, info
     return (1 if info["pairs_ok"] else 0), info
@@ -610,7 +709,7 @@ def analyser_launch(cfg):
     and 4/8 pixels, else one sin/cos per term with ANALYSER_LAUNCHES."""
     cfg = dict(cfg)
     nt, ppt = int(cfg.get("threads", 128)), int(cfg.get("pix_per_thread", 4))
-    if int(cfg.get("pairs", 0) or 0) == 3:
+    if int(cfg.get("pairs", 0) or 0) in (3, 4):
         cfg["pairs"] = 2
     if int(cfg.get("pairs", 0) or 0) == 2:
         if nt not in (128, 256) or ppt not in (4, 8):
@@ -629,6 +728,14 @@ def grouping_launch(cfg, level, tiles, pix, k, info):
     pairs_ok = bool(info.get("pairs_ok", level >= 1))
     mode = min(int(cfg.get("pairs", 0) or 0), int(level))
     ppt = int(cfg.get("pix_per_thread", 4))
+    if mode == 4 and (ppt != 16 or int(cfg.get("threads", 128)) not in (128, 192)):
+        mode = 3
+    if mode < 4 and (ppt == 16 or int(cfg.get("threads", 128)) == 192):
+        # 16 pixels a thread and 192-thread blocks exist only as squares
+        ppt = 8 if mode >= 2 else 4
+        cfg["pix_per_thread"] = ppt
+        if int(cfg.get("threads", 128)) == 192:
+            cfg["threads"] = 128
     if mode == 3 and ppt != 8:
         mode = 2
     if mode == 2 and ppt not in (4, 8):
@@ -636,7 +743,8 @@ def grouping_launch(cfg, level, tiles, pix, k, info):
     if mode == 1 and (ppt % 2 or not pairs_ok):
         mode = 0
     cfg["pairs"] = mode
-    cfg["octet_radius_m"] = float(info.get("octet_radius_m", 0.0)) if mode == 3 else 0.0
+    cfg["octet_radius_m"] = (float(info.get("octet_radius_m", 0.0)) if mode == 3 else
+                             float(info.get("square_radius_m", 0.0)) if mode == 4 else 0.0)
     if mode >= 2:
         cfg["pair_short_radius_m"] = info["quad_short_radius_m"]
     elif mode == 1:

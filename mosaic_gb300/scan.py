@@ -124,9 +124,10 @@ class BatchedScan:
         su = self._setup(self.tiles)
         self.tune_results = []
         if launch:
-            cfg, src = dict(engine.default_launch(su.level), **launch), "explicit"
+            cfg, src = dict(engine.default_launch(su.level, self.tiles.tile_atoms), **launch), "explicit"
         elif beam._kernel_launch:
-            cfg, src = dict(engine.default_launch(su.level), **beam._kernel_launch), "beam"
+            cfg, src = dict(engine.default_launch(su.level, self.tiles.tile_atoms),
+                            **beam._kernel_launch), "beam"
         else:
             from . import autotune
             best = autotune.cached(n_total, "scan")
@@ -144,7 +145,7 @@ class BatchedScan:
                 except _lib.DeclineError:
                     pass
             cfg = (autotune.lookup(n_total, su.level, "scan", self.tiles.tile_atoms) if best
-                   else engine.default_launch(su.level))
+                   else engine.default_launch(su.level, self.tiles.tile_atoms))
         self.launch_source = src
         self.out = torch.zeros((n_total, 2), dtype=torch.float64, device=dev)
         self.sums = torch.zeros(len(self.frames), dtype=torch.float64, device=dev)

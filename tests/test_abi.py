@@ -84,7 +84,8 @@ def test_struct_layouts_match_the_header(tmp_path):
 
 def test_scan_plan_checks_quad_rows_before_any_cuda_call():
     """Pixel quads need every frame's row length, and whole rows; octets
-    need whole 2x4 octets; an unknown pixel mode is refused: all argument
+    need whole 2x4 octets, squares whole 4x4 squares; an unknown pixel mode
+    is refused: all argument
     errors from mk_scan_plan, raised before it touches the GPU."""
     L = _lib.load()
     tiles = _lib.MkTiles(4, 128, None, None, None, None)
@@ -111,6 +112,14 @@ def test_scan_plan_checks_quad_rows_before_any_cuda_call():
     assert plan(ctypes.cast(odd, ctypes.c_void_p)) == _lib.MK_EINVAL
     assert b"octets" in L.mk_last_error()
     launch.pairs = 4
+    launch.pix_per_thread = 16
+    assert plan(ctypes.cast(odd, ctypes.c_void_p)) == _lib.MK_EINVAL   # 16 = 4 rows of 4: ok;
+    assert b"squares" in L.mk_last_error()                             # 12 = 2 rows of 6: not
+    sq_ok_first = (ctypes.c_int * 2)(4, 4)
+    npix[1] = 8                                                        # 8 = 2 rows of 4
+    assert plan(ctypes.cast(sq_ok_first, ctypes.c_void_p)) == _lib.MK_EINVAL
+    assert b"squares" in L.mk_last_error()
+    launch.pairs = 5
     assert plan(ctypes.cast(bad, ctypes.c_void_p)) == _lib.MK_EINVAL
     assert b"pairs must be" in L.mk_last_error()
 

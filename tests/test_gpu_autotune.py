@@ -44,7 +44,7 @@ def test_tune_picks_tile_size_and_shape_and_caches(cuda, fresh_cache):
         su, _ = B.split_setup(engine.Tiles(atoms, B.k, T, device=cuda), pix, phys)
         assert su is not None
         setups[T] = su
-    cands = [(4, 128, 0), (8, 128, 2), (8, 128, 3), (4, 64, 1)]
+    cands = [(4, 128, 0), (8, 128, 2), (8, 128, 3), (4, 64, 1), (16, 128, 4)]
     best, table = autotune.tune(setups, pix, phys, atoms.table, candidates=cands)
     assert best["tile_atoms"] in (256, 512)
     tried = {(c["pix_per_thread"], c["threads"], c["pairs"], c["tile_atoms"]) for _, c in table}
@@ -55,12 +55,13 @@ def test_tune_picks_tile_size_and_shape_and_caches(cuda, fresh_cache):
     assert (fresh_cache / "tune.json").exists()
     assert autotune.cached(pix.n) == best
     assert autotune.tile_atoms(pix.n) == best["tile_atoms"]
-    look = autotune.lookup(pix.n, 3, "exposure", best["tile_atoms"])
+    lv = setups[best["tile_atoms"]].level
+    look = autotune.lookup(pix.n, lv, "exposure", best["tile_atoms"])
     assert {k: look[k] for k in ("pix_per_thread", "threads", "pairs")} == \
         {k: best[k] for k in ("pix_per_thread", "threads", "pairs")}
     # another tile size, or a level below the winner's mode: the default
     other = 256 if best["tile_atoms"] == 512 else 512
-    assert autotune.lookup(pix.n, 3, "exposure", other) == engine.default_launch(3)
+    assert autotune.lookup(pix.n, lv, "exposure", other) == engine.default_launch(lv, other)
     assert autotune.lookup(pix.n, 0, "exposure", best["tile_atoms"]) == engine.default_launch(0) \
         or best["pairs"] == 0
 

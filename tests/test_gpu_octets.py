@@ -93,7 +93,7 @@ def test_octets_direct_sincos_argument(cuda):
     pix = engine.Pixels(np.asarray(D.pixel_coordinates, np.float64) / 1e10, *D.shape, phys,
                         device=cuda)
     level, info = engine.pixel_grouping(tiles, pix, B.k, 1e-6)
-    assert level == 3, info
+    assert level >= 3, info
     short_r = info["quad_short_radius_m"]
 
     def run(lim):
@@ -127,7 +127,7 @@ def test_octets_with_wide_tiles_taking_quads(cuda):
     pix = engine.Pixels(np.asarray(D.pixel_coordinates, np.float64) / 1e10, *D.shape, phys,
                         device=cuda)
     level, info = engine.pixel_grouping(tiles, pix, B.k, 1e-6)
-    assert level == 3, info
+    assert level >= 3, info
     radii = tiles.origin[: tiles.n_tiles, 3].cpu().numpy()
     assert tiles.n_tiles >= 8 and radii.max() <= info["octet_radius_m"]
     med = float(np.median(radii))

@@ -27,6 +27,8 @@ def _flat_pixels(ny, nz, pitch, dist, y0=0.0, z0=0.0, frames=None):
     st.quad_steps = lambda: engine.Pixels.quad_steps(st)
     st.octets_fit = lambda: engine.Pixels.octets_fit(st)
     st.octet_steps = lambda: engine.Pixels.octet_steps(st)
+    st.squares_fit = lambda: engine.Pixels.squares_fit(st)
+    st.square_steps = lambda: engine.Pixels.square_steps(st)
     u = st.xyz / torch.linalg.vector_norm(st.xyz, dim=1, keepdim=True)
     st.u = torch.cat([u.float(), torch.zeros(off, 1)], 1)
     st.pair_step = lambda: engine.Pixels.pair_step(st)
@@ -158,14 +160,14 @@ def test_octet_bounds_of_a_flat_detector():
     octets have none; small tiles admit octets, large ones only quads."""
     k = 2 * np.pi / 1.2398e-10
     p, R = 55e-6, 1.0
-    pix = _flat_pixels(16, 16, p, R)
+    pix = _flat_pixels(16, 14, p, R)     # whole octets, not whole 4x4 squares
     st = pix.octet_steps()
     assert 0.3 * (p / R) ** 2 < st["plane"] < 1.0 * (p / R) ** 2
     assert st["step"] == pytest.approx(p / R, rel=1e-3)
     assert st["extent"] == pytest.approx(np.hypot(1.5, 0.5) * p / R, rel=1e-2)
     for shape in ((15, 16), (16, 15), (18, 16), (2, 2)):
         assert _flat_pixels(*shape, p, R).octet_steps() is None, shape
-    multi = _flat_pixels(0, 0, p, R, frames=[(8, 4), (16, 16), (4, 2)])
+    multi = _flat_pixels(0, 0, p, R, frames=[(8, 4), (16, 14), (4, 2)])
     assert multi.octet_steps()["plane"] == pytest.approx(st["plane"], rel=0.5)
     assert _flat_pixels(0, 0, p, R, frames=[(8, 4), (6, 2)]).octet_steps() is None
     small, big = _tiles(2e-9, 6e-8), _tiles(4.6e-8, 6e-8)
@@ -198,7 +200,7 @@ def test_octet_bounds_of_a_flat_detector():
 
 def test_octet_launch_clamps():
     k = 2 * np.pi / 1.2398e-10
-    pix = _flat_pixels(16, 16, 55e-6, 1.0)
+    pix = _flat_pixels(16, 14, 55e-6, 1.0)
     small = _tiles(2e-9, 6e-8)
     lv, info = engine.pixel_grouping(small, pix, k, 1e-6)
     assert lv == 3
@@ -211,3 +213,97 @@ def test_octet_launch_clamps():
     assert g(dict(pix_per_thread=8, threads=128, pairs=3), 2)["pairs"] == 2
     assert engine.default_launch(3) == dict(pix_per_thread=8, threads=128, slices=0, pairs=3)
     assert engine.analyser_launch(dict(pix_per_thread=8, threads=128, pairs=3))["pairs"] == 2
+
+
+def test_square_bounds_of_a_flat_detector():
+    """The square's departure from the kernel's plane (the mean plus the
+    quads' mean row and column steps) is the curvature of the pixel
+    directions along and across rows, ~(p/R)^2 near the axis; frames that
+    are not whole squares have none; narrow tiles admit squares, wider ones
+    octets (whose bound is smaller), the widest only quads."""
+    k = 2 * np.pi / 1.2398e-10
+    p, R = 55e-6, 1.0
+    pix = _flat_pixels(16, 16, p, R)
+    st = pix.square_steps()
+    assert 0.3 * (p / R) ** 2 < st["plane"] < 2.0 * (p / R) ** 2
+    assert st["plane"] > pix.octet_steps()["plane"]
+    assert st["step"] == pytest.approx(p / R, rel=1e-3)
+    assert st["extent"] == pytest.approx(np.hypot(1.5, 1.5) * p / R, rel=1e-2)
+    for shape in ((16, 14), (14, 16), (16, 18), (2, 2), (4, 2)):
+        assert _flat_pixels(*shape, p, R).square_steps() is None, shape
+    multi = _flat_pixels(0, 0, p, R, frames=[(8, 4), (16, 16), (4, 8)])
+    assert multi.square_steps()["plane"] == pytest.approx(st["plane"], rel=0.5)
+    assert _flat_pixels(0, 0, p, R, frames=[(8, 4), (8, 2)]).square_steps() is None
+    small = _tiles(2e-9, 6e-8)
+    lv, info = engine.pixel_grouping(small, pix, k, 1e-6)
+    assert lv == 4 and info["square_cross_rad"] < 1e-6 and info["square_tile_fraction"] == 1.0
+    assert info["square_cross_rad"] > info["octet_cross_rad"]
+    assert info["square_radius_m"] < info["octet_radius_m"]
+    # tiles between the two radii: octets; a few of them among narrow
+    # tiles: squares (the wide ones take the quad form inside the kernel)
+    r_mid = 0.5 * (info["square_radius_m"] + info["octet_radius_m"])
+    mid = _tiles(r_mid, 6e-8)
+    lv, inf = engine.pixel_grouping(mid, pix, k, 1e-6)
+    assert lv == 3 and inf["square_tile_fraction"] == 0.0
+    mixed = _tiles(0, 6e-8, radii=[2e-9] * 7 + [r_mid])
+    lv, inf = engine.pixel_grouping(mixed, pix, k, 1e-6)
+    assert lv == 4 and inf["square_tile_fraction"] == pytest.approx(7 / 8)
+    assert engine.pixel_grouping(small, pix, k, 1e-6, analyser=1)[0] == 2
+    # the radius scales with the budget, the |d|^2 term's change counts
+    r1 = engine.square_bounds(small, pix, k, 1e-6)["radius_m"]
+    r2 = engine.square_bounds(small, pix, k, 2e-6)["radius_m"]
+    assert r2 == pytest.approx(2 * r1, rel=1e-9)
+    c0 = engine.square_bounds(small, pix, k, 1e-6)["cross"]
+    c1 = engine.square_bounds(small, pix, k, 1e-6, fresnel_rad=1e-3)["cross"]
+    assert c1 == pytest.approx(c0 + 4e-3 * st["extent"], rel=1e-9)
+
+
+def test_square_steps_match_the_kernel_model():
+    """square_steps' residual is the departure from exactly the model the
+    kernel uses: mean of the 16 directions plus offsets times the means of
+    the within-quad steps (columns 0->1, 2->3; rows 0->1, 2->3)."""
+    p, R = 55e-6, 0.3
+    pix = _flat_pixels(8, 4, p, R, y0=0.02, z0=0.05)
+    u = (pix.xyz / torch.linalg.vector_norm(pix.xyz, dim=1, keepdim=True)).numpy()
+    worst = 0.0
+    U = u.reshape(4, 8, 3)
+    for sq in range(2):
+        B = U[:, 4 * sq:4 * sq + 4]                  # rows x columns x 3
+        quads = [B[2 * (j >> 1):2 * (j >> 1) + 2, 2 * (j & 1):2 * (j & 1) + 2] for j in range(4)]
+        g = sum((q[0, 1] - q[0, 0]) + (q[1, 1] - q[1, 0]) for q in quads) / 8
+        h = sum((q[1, 0] - q[0, 0]) + (q[1, 1] - q[0, 1]) for q in quads) / 8
+        mean = B.reshape(-1, 3).mean(0)
+        for r in range(4):
+            for c in range(4):
+                model = mean + (c - 1.5) * g + (r - 1.5) * h
+                worst = max(worst, float(np.linalg.norm(B[r, c] - model)))
+    assert pix.square_steps()["plane"] == pytest.approx(worst, rel=1e-9)
+
+
+def test_square_launch_clamps():
+    k = 2 * np.pi / 1.2398e-10
+    pix = _flat_pixels(16, 16, 55e-6, 1.0)
+    small = _tiles(2e-9, 6e-8)
+    lv, info = engine.pixel_grouping(small, pix, k, 1e-6)
+    assert lv == 4
+    g = lambda cfg, level=lv: engine.grouping_launch(cfg, level, small, pix, k, info)
+    cfg = g(dict(pix_per_thread=16, threads=128, pairs=4))
+    assert cfg["pairs"] == 4 and cfg["pair_short_radius_m"] == info["quad_short_radius_m"]
+    assert cfg["octet_radius_m"] == info["square_radius_m"] > 0
+    assert g(dict(pix_per_thread=8, threads=128, pairs=3))["octet_radius_m"] == info["octet_radius_m"]
+    # squares need 16 pixels and 128 or 192 threads; 16 pixels and 192
+    # threads exist only as squares
+    assert g(dict(pix_per_thread=8, threads=128, pairs=4))["pairs"] == 3
+    assert g(dict(pix_per_thread=16, threads=192, pairs=4))["pairs"] == 4
+    c = g(dict(pix_per_thread=16, threads=256, pairs=4))
+    assert (c["pairs"], c["pix_per_thread"]) == (3, 8)
+    c = g(dict(pix_per_thread=16, threads=192, pairs=4), 3)
+    assert (c["pairs"], c["pix_per_thread"], c["threads"]) == (3, 8, 128)
+    c = g(dict(pix_per_thread=16, threads=128, pairs=4), 2)
+    assert (c["pairs"], c["pix_per_thread"]) == (2, 8)
+    c = g(dict(pix_per_thread=16, threads=128, pairs=4), 1)
+    assert (c["pairs"], c["pix_per_thread"]) == (1, 4)
+    assert engine.default_launch(4, 512) == dict(pix_per_thread=16, threads=128, slices=0, pairs=4)
+    assert engine.default_launch(4) == engine.default_launch(3) == engine.default_launch(4, 1024)
+    a = engine.analyser_launch(dict(pix_per_thread=16, threads=128, pairs=4))
+    assert (a["pairs"], a["pix_per_thread"]) == (2, 8)

@@ -116,3 +116,60 @@ def test_octets_are_two_side_by_side_quads():
         want = [(r, c), (r, c + 1), (r + 1, c), (r + 1, c + 1),
                 (r, c + 2), (r, c + 3), (r + 1, c + 2), (r + 1, c + 3)]
         assert [divmod(int(p), ny) for p in o] == want
+
+
+def square_pixels(n_pix, row, nt, pix_blocks):
+    """(loads, stores) of the square kernels' mapping (mk_split.cuh, PM == 4):
+    thread gi = pb * nt + tid owns rows 4 gz .. 4 gz + 3 and columns
+    4 gy .. 4 gy + 3, pixels 4j..4j+3 the quad a b c d at rows 4 gz + 2 (j >> 1)
+    (+1) and columns 4 gy + 2 (j & 1) (+1); past the last square the pixels
+    are n_pix (loads clamp, stores skip)."""
+    rows = n_pix // row
+    gpr = row >> 2
+    n_sq = gpr * (rows >> 2)
+    loads, stores = [], []
+    for pb in range(pix_blocks):
+        for tid in range(nt):
+            gi = pb * nt + tid
+            if gi >= n_sq:
+                loads += [n_pix - 1] * 16
+                continue
+            gz, gy = divmod(gi, gpr)
+            base = 4 * gz * row + 4 * gy
+            pix = []
+            for j in range(4):
+                a0 = base + 2 * (j >> 1) * row + 2 * (j & 1)
+                pix += [a0, a0 + 1, a0 + row, a0 + row + 1]
+            loads += pix
+            stores += pix
+    return np.array(loads), np.array(stores)
+
+
+SQUARE_SHAPES = [(4, 4), (8, 4), (4, 8), (16, 16), (64, 64), (128, 128), (20, 12), (512, 4),
+                 (4, 512), (256, 256)]
+
+
+def test_squares_store_every_pixel_once():
+    nt = 128
+    for ny, nz in SQUARE_SHAPES:
+        n_pix = ny * nz
+        pb = (n_pix + nt * 16 - 1) // (nt * 16)    # mk_scan_plan: whole squares, 16 pixels a thread
+        loads, stores = square_pixels(n_pix, ny, nt, pb)
+        assert loads.min() >= 0 and loads.max() < n_pix, (ny, nz)
+        assert len(stores) == n_pix and np.array_equal(np.sort(stores), np.arange(n_pix)), (ny, nz)
+
+
+def test_squares_are_four_quads_in_a_square():
+    """Quad j sits at row pair j >> 1 and column pair j & 1 of its square,
+    which is the order the kernel's quad phases assume (columns s = -1 for
+    quads 0, 2; rows t = -1 for quads 0, 1)."""
+    ny, nz = 20, 12
+    loads, _ = square_pixels(ny * nz, ny, 64, 1)
+    for sq in loads.reshape(-1, 16)[: (ny // 4) * (nz // 4)]:
+        r, c = divmod(int(sq[0]), ny)
+        assert r % 4 == 0 and c % 4 == 0
+        want = []
+        for j in range(4):
+            rr, cc = r + 2 * (j >> 1), c + 2 * (j & 1)
+            want += [(rr, cc), (rr, cc + 1), (rr + 1, cc), (rr + 1, cc + 1)]
+        assert [divmod(int(p), ny) for p in sq] == want
