@@ -646,6 +646,9 @@ def run_ours(args):
     launch = engine.grouping_launch(launch, level, tiles, pix, B.k, ginfo)
     B._kernel_launch = launch
     amp_real = tiles.amp_is_real()
+    # the per-(species, pixel) factor table where the geometry admits it,
+    # decided once (the check reads back the tile and pixel extents)
+    ftab = (not args.no_factor_table) and engine.factor_table_ok(tiles, pix, phys)
     split_times = []
 
     def step(record=False):
@@ -657,7 +660,8 @@ def run_ours(args):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
         out = engine.run_split(t, p, phys, table, launch=launch, fresnel=fresnel,
-                               amp_real=amp_real, fresnel_radius=su.fresnel_radius)
+                               amp_real=amp_real, fresnel_radius=su.fresnel_radius,
+                               factor_table=ftab)
         if record:
             e1.record()
             split_times.append((e0, e1))
@@ -688,7 +692,8 @@ def run_ours(args):
         # Kernel-profile run: one configuration, no side legs.
         if rank == 0:
             print(json.dumps({"profile": args.config, "ms_per_step": ms, "split_ms": split_ms,
-                              "value": value, "launch": launch, "fresnel": bool(fresnel)}))
+                              "value": value, "launch": launch, "fresnel": bool(fresnel),
+                              "factor_table": bool(ftab)}))
         return
 
     # End to end through the public entry point with host buffers.
@@ -731,7 +736,7 @@ def run_ours(args):
     form_bound = "mufu" if mufu / mufu_pt <= fma / fp32_pt else "fp32"
     traffic = profiled_traffic(args.config, n_pix, launch)
     achieved = terms / (split_ms * 1e-3)
-    gpu_launches = args.steps * 8
+    gpu_launches = args.steps * (8 + int(bool(ftab)))
 
     configs = configs_leg(args, dev) if (rank == 0 and not args.no_configs) else None
     scan = scan_leg(args, dev) if (rank == 0 and args.scan_frames > 0) else None
@@ -746,7 +751,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": {"workload": args.config, "atoms": n_atoms, "pixels": n_pix,
                        "terms_per_step": terms, "tile_atoms": B._kernel_tile_atoms,
-                       "launch": launch, "fresnel_term": bool(fresnel),
+                       "launch": launch, "fresnel_term": bool(fresnel), "factor_table": bool(ftab),
                        "l2": "inputs larger than L2 (positions + tiles ~300 MB); no flush",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": terms * world / e2e_s / 1e9, "unit": "Gatom*pixel/s",
@@ -834,6 +839,9 @@ def main():
                     help="at most one sin/cos per pixel pair (the 2x2 quad and octet forms off)")
     ap.add_argument("--no-octets", action="store_true",
                     help="at most the 2x2 quad form (the 2x4 octet and 4x4 square forms off)")
+    ap.add_argument("--no-factor-table", action="store_true",
+                    help="the scattering factor per (tile, pixel) instead of the per-(species, "
+                         "pixel) table")
     ap.add_argument("--no-squares", action="store_true",
                     help="at most the 2x4 octet form (the 4x4 square form off)")
     ap.add_argument("--scan-frames", type=int, default=724,

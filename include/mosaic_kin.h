@@ -90,6 +90,10 @@ typedef struct {
     double *q;            /* device (n_pix, 4): (k / 2 pi)(b - u_hat) [cycles/m], Q_cut [1/m] */
     float *u;             /* device (n_pix, 4): u_hat (x, y, z) and 1/|P| as float */
     double *phasor;       /* device (n_pix, 2) exp(i k |P|) */
+    float *factor;        /* device (n_species, n_pix, 2) or NULL: the scattering factor
+                             (f0 + f' + i f'') e^{-B s^2} sqrt(P_pol) of every species at every
+                             pixel's own direction, filled by mk_factor_table; the split kernels
+                             then read it instead of evaluating the factor per (tile, pixel) */
 } mk_pixels;
 
 /* One frame of a batched launch (an exposure's pixels, or a scan step's
@@ -180,6 +184,20 @@ int mk_sync_status(void *stream);
 /* Per-pixel prologue. Replaces the per-pixel set-up inside
  * compute_scattering_cffi (Beam.py:716-746) and pixel_phasor (Beam.py:9241-9255). */
 int mk_pixels_prepare(const mk_pixels *px, const mk_physics *phys, void *stream);
+
+/* The scattering factor (f0 + f' + i f'') e^{-B s^2} sqrt(P_pol) of every
+ * species at every pixel's own direction, into px->factor (n_species, n_pix,
+ * 2) float32: once per (species, pixel), where the reference evaluates f0,
+ * f'/f'' and the polarization factor per (atom, pixel) (Beam.py:770-806).
+ * The split kernels read it when px->factor is set (spherical decay still per
+ * tile and pixel); the caller admits it where the tile origins stay close to
+ * the sample origin against the pixel distance (the direction to a tile then
+ * differs from the pixel's by 2 (|o| + r) / R0 < 1e-6). n_frames > 1: each
+ * pixel's incident direction and polarization from its frame in frames_dev
+ * (mk_scan_plan's table, on the device); else phys->beam_dir, phys->pol_e.
+ * remove_forward is refused (its Q < Q_cut test stays per tile and pixel). */
+int mk_factor_table(const mk_pixels *px, const mk_species *sp, const mk_physics *phys,
+                    int n_frames, const mk_frame_desc *frames_dev, void *stream);
 
 /* Stage transform and incident amplitude per atom. Replaces the float32
  * `pos @ R.T + T` of interact_beam_gpu/cpu (Beam.py:6277-6280, 5896-5902)

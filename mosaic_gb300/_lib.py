@@ -127,7 +127,7 @@ class MkPhysics(ctypes.Structure):
 
 class MkPixels(ctypes.Structure):
     _fields_ = [("ny", ctypes.c_int), ("nz", ctypes.c_int), ("xyz", _vp), ("r0", _vp),
-                ("q", _vp), ("u", _vp), ("phasor", _vp)]
+                ("q", _vp), ("u", _vp), ("phasor", _vp), ("factor", _vp)]
 
 
 class MkFrameDesc(ctypes.Structure):
@@ -157,6 +157,8 @@ SIGNATURES = {
     "mk_last_error": (ctypes.c_char_p, []),
     "mk_sync_status": (ctypes.c_int, [_vp]),
     "mk_pixels_prepare": (ctypes.c_int, [ctypes.POINTER(MkPixels), ctypes.POINTER(MkPhysics), _vp]),
+    "mk_factor_table": (ctypes.c_int, [ctypes.POINTER(MkPixels), ctypes.POINTER(MkSpecies),
+                                       ctypes.POINTER(MkPhysics), ctypes.c_int, _vp, _vp]),
     "mk_atoms_lab": (ctypes.c_int, [ctypes.c_int64, _vp, _fp, _fp, _vp, ctypes.c_int, ctypes.c_int,
                                     _dp, _vp, _vp, _vp]),
     "mk_tiles_workspace_size": (ctypes.c_size_t, [ctypes.c_int64]),

@@ -511,6 +511,7 @@ class beam:
                                        fresnel_radius=su.fresnel_radius)
                 self.last_run = dict(path="split_f32", n_tiles=tiles.n_tiles,
                                      tile_atoms=tiles.tile_atoms, fresnel=bool(su.fresnel),
+                                     factor_table=engine.factor_table_ok(tiles, pix, phys),
                                      launch=dict(cfg), launch_source=src, **su.info, **diag)
                 return res
             self.last_run = dict(path="plain_f64", **diag)

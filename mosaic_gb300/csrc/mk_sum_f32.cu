@@ -30,6 +30,7 @@
 //
 // Atom tiles reach shared memory by 1-D TMA bulk copies (cp.async.bulk),
 // double-buffered on two mbarriers; every wait is bounded (mk_common.cuh).
+#include <climits>
 #include <algorithm>
 #include <mutex>
 
@@ -367,6 +368,11 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
     A.fres_r = launch->fresnel_radius_m > 0.0 ? (float)launch->fresnel_radius_m : 0.f;
     A.pair_short_r = launch->pair_short_radius_m > 0.0 ? (float)launch->pair_short_radius_m : -1.f;
     A.oct_r = launch->octet_radius_m > 0.0 ? (float)launch->octet_radius_m : -1.f;
+    MK_REQUIRE(!(px->factor && phys->remove_forward),
+               "split kernel: a factor table cannot serve remove_forward (its Q < Q_cut test is "
+               "per tile and pixel)");
+    A.ftab = reinterpret_cast<const float2 *>(px->factor);
+    A.ftab_n = n_total;
     A.sin_direct = launch->sin_direct_max_rad == 0.0 ? MK_SIN_DIRECT_MAX
                    : launch->sin_direct_max_rad < 0.0 ? -1.f : (float)launch->sin_direct_max_rad;
     if (ana) {
@@ -391,6 +397,68 @@ static int mk_run_split(const mk_tiles *tiles, const mk_species *spc, const mk_p
                                                             n_frames, frames_dev, f0, sums);
         MK_CHECK_CUDA(cudaGetLastError());
     }
+    return MK_OK;
+}
+
+// ------------------------------------------------------ factor table
+// The scattering factor of every species at every pixel's own direction
+// u (w = b - u), in the kernels' float32 arithmetic (mk_factor), without the
+// spherical-decay ratio, which the split kernel applies per (tile, pixel).
+__global__ void mk_factor_table_kernel(const __grid_constant__ MkSplitArgs A, long long n_pix,
+                                       float2 *__restrict__ out)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_pix) return;
+    int f = 0;
+    if (A.n_frames > 1) {
+        int lo = 0, hi = A.n_frames - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (A.frames[mid].pix_off <= g) lo = mid; else hi = mid - 1;
+        }
+        f = lo;
+    }
+    const mk_frame_desc F = A.n_frames > 1 ? A.frames[f] : A.f0;
+    const float4 uu = A.u[g];
+    const float qcut = (float)A.q[g].w;
+    const float wx = F.b[0] - uu.x, wy = F.b[1] - uu.y, wz = F.b[2] - uu.z;
+    for (int s = 0; s < A.sp.n; ++s) out[(long long)s * n_pix + g] = mk_factor(A, s, F, wx, wy, wz, qcut, 1.f);
+}
+
+extern "C" int mk_factor_table(const mk_pixels *px, const mk_species *spc, const mk_physics *phys,
+                               int n_frames, const mk_frame_desc *frames_dev, void *stream)
+{
+    MK_REQUIRE(px && spc && phys, "mk_factor_table: null argument");
+    MK_REQUIRE(px->factor && px->u && px->q, "mk_factor_table: pixels not prepared or no factor buffer");
+    MK_REQUIRE(px->ny > 0 && px->nz > 0, "mk_factor_table: bad detector shape");
+    MK_REQUIRE(phys->k > 0.0, "mk_factor_table: k must be positive");
+    MK_REQUIRE(!phys->remove_forward,
+               "mk_factor_table: remove_forward needs the factor per (tile, pixel)");
+    MK_REQUIRE(n_frames <= 1 || frames_dev, "mk_factor_table: %d frames and no frame table", n_frames);
+    MK_REQUIRE(((uintptr_t)px->factor & 7) == 0, "mk_factor_table: factor buffer must be 8-byte aligned");
+    MkSplitArgs A;
+    memset(&A, 0, sizeof(A));
+    int rc = mk_species_pack(spc, &A.sp);
+    if (rc != MK_OK) return rc;
+    const long long n = (long long)px->ny * px->nz;
+    A.n_frames = n_frames > 1 ? n_frames : 1;
+    A.frames = frames_dev;
+    A.f0.n_pix = (int)std::min<long long>(n, INT_MAX);
+    for (int c = 0; c < 3; ++c) {
+        A.f0.b[c] = (float)phys->beam_dir[c];
+        A.f0.e[c] = (float)phys->pol_e[c];
+    }
+    A.q = reinterpret_cast<const double4 *>(px->q);
+    A.u = reinterpret_cast<const float4 *>(px->u);
+    A.k = (float)phys->k;
+    const double sf = phys->k * 0.25e-10 / MK_PI;
+    A.s2fac = (float)(sf * sf);
+    A.apply_pol = phys->apply_pol;
+    A.pdeg = (float)phys->pol_deg;
+    cudaStream_t st = mk_stream(stream);
+    mk_factor_table_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        A, n, reinterpret_cast<float2 *>(px->factor));
+    MK_CHECK_CUDA(cudaGetLastError());
     return MK_OK;
 }
 

@@ -65,6 +65,14 @@ class SpeciesTable:
                 b = None
         return cls(labels, wk, f0z, an, b)
 
+    def key(self):
+        """What the factor of each species depends on (labels, f0
+        coefficients, f(0), f' + i f'', Debye-Waller B)."""
+        dw = b"" if self.dw_b is None else np.asarray(self.dw_b, np.float32).tobytes()
+        return (tuple(self.labels), np.asarray(self.wk, np.float32).tobytes(),
+                np.asarray(self.f0z, np.float32).tobytes(),
+                np.asarray(self.anom, np.complex128).tobytes(), dw)
+
     def abi(self):
         self._keep = [np.ascontiguousarray(self.wk, np.float32),
                       np.ascontiguousarray(self.f0z, np.float32),
@@ -163,6 +171,27 @@ class Pixels:
             off += m
         if off != P:
             raise ValueError(f"frames cover {off} pixels, xyz has {P}")
+
+    def factor_table(self, table, phys, stream=None):
+        """(n_species, P, 2) float32 scattering factors of every species at
+        every pixel's own direction (``mk_factor_table``), for single
+        exposures (the physics' beam direction); kept per Pixels object for
+        the last species table and physics it was made for."""
+        key = (table.key(), float(phys.k), tuple(phys.beam_dir), int(phys.apply_pol),
+               float(phys.pol_deg), tuple(phys.pol_e))
+        cached = getattr(self, "_ftab", None)
+        if cached is not None and cached[0] == key:
+            return cached[1]
+        L = _require_cuda()
+        ftab = torch.empty((len(table.labels), self.n, 2), dtype=torch.float32,
+                           device=self.xyz.device)
+        abi = MkPixels.from_buffer_copy(self.abi)
+        abi.factor = ftab.data_ptr()
+        sp = table.abi()
+        check(L.mk_factor_table(ctypes.byref(abi), ctypes.byref(sp), ctypes.byref(phys), 1, None,
+                                _stream_handle(stream)))
+        self._ftab = (key, ftab)
+        return ftab
 
     def r0_min(self):
         """Smallest pixel distance (one read-back per Pixels object)."""
@@ -531,6 +560,23 @@ def default_launch(level=0, tile_atoms=None):
         level = 3
     ppt = 16 if level >= 4 else 8 if level >= 2 else 4
     return dict(DEFAULT_LAUNCH, pairs=level, pix_per_thread=ppt)
+FACTOR_TABLE_EXCURSION = 1e-6
+
+
+def factor_table_ok(tiles, pix, phys):
+    """Whether the split kernel may take each species' factor at the pixel's
+    own direction (``Pixels.factor_table``) instead of at the direction to
+    each tile: the two directions differ by at most 2 (|o| + r) / R0 (tile
+    origin o, radius r, pixel distance R0), which must stay below
+    FACTOR_TABLE_EXCURSION -- the bound the split form already keeps for the
+    factor's change across a tile, 2 r / R0, with the tile origins added.
+    Not with remove_forward, whose Q < Q_cut test stays per tile and pixel."""
+    if phys.remove_forward or not tiles.n_tiles:
+        return False
+    r0 = max(pix.r0_min(), 1e-300)
+    return 2.0 * (tiles.max_origin_norm() + tiles.max_radius()) / r0 < FACTOR_TABLE_EXCURSION
+
+
 PAIR_DELTA_MAX = 0.5     # rad: the long pair polynomials are then exact to ~2e-6 per term
 PAIR_SHORT_DELTA = 0.07  # rad: the short ones to 1e-6 (the kernel's MK_PAIR_SHORT_DELTA)
 
@@ -755,8 +801,12 @@ def grouping_launch(cfg, level, tiles, pix, k, info):
 
 
 def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None, fresnel=-1,
-              amp_real=None, out=None, accumulate=False, stream=None, fresnel_radius=0.0):
+              amp_real=None, out=None, accumulate=False, stream=None, fresnel_radius=0.0,
+              factor_table=None):
     """FP32 split-phase sum; returns float64 (P, 2) (a view of `out` if given).
+    ``factor_table`` None: the per-(species, pixel) factor table where
+    ``factor_table_ok`` admits it (else the factor per tile and pixel);
+    False: never; True: always.
     With ``fresnel`` set, only tiles wider than ``fresnel_radius`` [m] keep the
     |d|^2 term (0: all tiles). ``launch["pairs"]`` = 1 shares one sin/cos
     between pixels 2j and 2j+1; only legal where ``pairs_allowed`` holds;
@@ -784,10 +834,16 @@ def run_split(tiles: Tiles, pix: Pixels, phys, table: SpeciesTable, launch=None,
     if out is None:
         out = torch.zeros((pix.n, 2), dtype=torch.float64, device=pix.xyz.device)
     sp = table.abi()
+    use_tab = factor_table_ok(tiles, pix, phys) if factor_table is None else bool(factor_table)
+    pabi, ftab = pix.abi, None
+    if use_tab:
+        ftab = pix.factor_table(table, phys, stream)
+        pabi = MkPixels.from_buffer_copy(pix.abi)
+        pabi.factor = ftab.data_ptr()
     check(L.mk_kin_split_f32(ctypes.byref(tiles.abi), ctypes.byref(sp), ctypes.byref(phys),
-                             ctypes.byref(pix.abi), ctypes.byref(ln), _ptr(out), int(bool(accumulate)),
+                             ctypes.byref(pabi), ctypes.byref(ln), _ptr(out), int(bool(accumulate)),
                              _ptr(ws), ws_n, _stream_handle(stream)))
-    out._mk_keep = ws
+    out._mk_keep = (ws, ftab)
     return out
 
 

@@ -27,7 +27,7 @@ import numpy as np
 import torch
 
 from . import _lib, engine
-from ._lib import MkFrameDesc, MkLaunch, check
+from ._lib import MkFrameDesc, MkLaunch, MkPixels, check
 
 
 @dataclass
@@ -213,6 +213,25 @@ class BatchedScan:
         self.n_items, self.n_partial = int(n_items.value), int(n_part.value)
         raw = np.frombuffer(bytes(desc), dtype=np.uint8).copy()
         self.frames_dev = torch.as_tensor(raw).to(self._dev)
+        # per-(species, pixel) factors at every frame's pixel directions,
+        # where the tile origins allow it (engine.factor_table_ok)
+        self.pix_abi, self.ftab = self.pix.abi, None
+        if engine.factor_table_ok(tiles, self.pix, self.phys):
+            key = (self.table.key(), bytes(raw))
+            if getattr(self, "_ftab_key", None) == key and self._ftab is not None:
+                self.ftab = self._ftab
+            else:
+                self.ftab = torch.empty((len(self.table.labels), self.pix.n, 2),
+                                        dtype=torch.float32, device=self._dev)
+                abi = MkPixels.from_buffer_copy(self.pix.abi)
+                abi.factor = self.ftab.data_ptr()
+                sp = self.table.abi()
+                check(self.L.mk_factor_table(ctypes.byref(abi), ctypes.byref(sp),
+                                             ctypes.byref(self.phys), nf,
+                                             self.frames_dev.data_ptr(), engine._stream_handle()))
+                self._ftab_key, self._ftab = key, self.ftab
+            self.pix_abi = MkPixels.from_buffer_copy(self.pix.abi)
+            self.pix_abi.factor = self.ftab.data_ptr()
         need = int(self.L.mk_scan_workspace_size(self.n_partial))
         if self.ws is None or self.ws_bytes < need:
             self.ws = torch.empty(need, dtype=torch.uint8, device=self._dev)
@@ -241,7 +260,7 @@ class BatchedScan:
         """Launch the whole scan (asynchronous); returns (fields, sums) on device."""
         sp = self.table.abi()
         check(self.L.mk_kin_scan_f32(ctypes.byref(self.tiles_run.abi), ctypes.byref(sp),
-                                     ctypes.byref(self.phys), ctypes.byref(self.pix.abi),
+                                     ctypes.byref(self.phys), ctypes.byref(self.pix_abi),
                                      len(self.frames), self.frames_dev.data_ptr(), self.n_items,
                                      self.n_partial, ctypes.byref(self.launch), self.out.data_ptr(),
                                      self.sums.data_ptr(), self.ws.data_ptr(), self.ws_bytes,

@@ -45,6 +45,26 @@ def test_version_and_host_side_validation():
     assert L.mk_kin_plain_f64(0, None, None, None, None, None, None, 0, None, 0, None, 0,
                               None) == _lib.MK_EINVAL
     assert L.mk_sum_workspace_size(1000, 3) == 1000 * 3 * 16
+    # the factor table: no buffer, or remove_forward (whose Q < Q_cut test
+    # stays per tile and pixel), refused before any CUDA call
+    assert L.mk_factor_table(None, None, None, 1, None, None) == _lib.MK_EINVAL
+    buf = ctypes.c_void_p(256)
+    px = _lib.MkPixels(4, 4, buf, buf, buf, buf, buf)
+    sp = _lib.MkSpecies(1, buf, buf, buf, buf, None)
+    ph = _lib.MkPhysics()
+    ph.k = 5.0e10
+    assert L.mk_factor_table(ctypes.byref(px), ctypes.byref(sp), ctypes.byref(ph), 1, None,
+                             None) == _lib.MK_EINVAL
+    assert b"factor buffer" in L.mk_last_error()
+    px.factor = buf
+    ph.remove_forward = 1
+    assert L.mk_factor_table(ctypes.byref(px), ctypes.byref(sp), ctypes.byref(ph), 1, None,
+                             None) == _lib.MK_EINVAL
+    assert b"remove_forward" in L.mk_last_error()
+    ph.remove_forward = 0
+    assert L.mk_factor_table(ctypes.byref(px), ctypes.byref(sp), ctypes.byref(ph), 3, None,
+                             None) == _lib.MK_EINVAL
+    assert b"frame table" in L.mk_last_error()
     with pytest.raises(ValueError):
         _lib.check(_lib.MK_EINVAL)
     with pytest.raises(MemoryError):

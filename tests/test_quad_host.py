@@ -307,3 +307,16 @@ def test_square_launch_clamps():
     assert engine.default_launch(4) == engine.default_launch(3) == engine.default_launch(4, 1024)
     a = engine.analyser_launch(dict(pix_per_thread=16, threads=128, pairs=4))
     assert (a["pairs"], a["pix_per_thread"]) == (2, 8)
+
+
+def test_factor_table_admission():
+    """The per-(species, pixel) factor table needs 2 (|o| + r) / R0 below
+    1e-6 and no remove_forward."""
+    pix = _flat_pixels(16, 16, 55e-6, 1.0)
+    phys = types.SimpleNamespace(remove_forward=0)
+    assert engine.factor_table_ok(_tiles(2e-9, 6e-8), pix, phys)
+    assert not engine.factor_table_ok(_tiles(2e-9, 6e-7), pix, phys)
+    assert not engine.factor_table_ok(_tiles(4e-7, 2e-7), pix, phys)
+    assert not engine.factor_table_ok(_tiles(2e-9, 6e-8), _flat_pixels(16, 16, 55e-6, 0.05), phys)
+    assert not engine.factor_table_ok(_tiles(2e-9, 6e-8), pix, types.SimpleNamespace(remove_forward=1))
+    assert not engine.factor_table_ok(types.SimpleNamespace(n_tiles=0), pix, phys)
