@@ -44,7 +44,10 @@ def test_noalloc_entry_matches_workspace_entry(cuda):
     L = _lib.load()
     table, phys, tiles, pix = _inputs(cuda)
     cfg = dict(pix_per_thread=4, threads=128, slices=3)
-    ref = engine.run_split(tiles, pix, phys, table, launch=cfg, fresnel=1, amp_real=False)
+    # the factor per tile and pixel in both (the pixels passed below carry no
+    # factor table)
+    ref = engine.run_split(tiles, pix, phys, table, launch=cfg, fresnel=1, amp_real=False,
+                           factor_table=False)
     engine.sync()
     ln = MkLaunch(4, 128, 3, 1, 0)
     sp = table.abi()
@@ -81,8 +84,10 @@ def test_noalloc_entry_caps_slices_to_the_scratch(cuda):
     fit = (_lib.MK_NOALLOC_SCRATCH_BYTES - 256) // (16 * pix.n)
     assert fit == 7
     base = dict(pix_per_thread=4, threads=128, pairs=0)
-    ref7 = engine.run_split(tiles, pix, phys, atoms.table, launch=dict(base, slices=7), fresnel=0)
-    ref64 = engine.run_split(tiles, pix, phys, atoms.table, launch=dict(base, slices=64), fresnel=0)
+    ref7 = engine.run_split(tiles, pix, phys, atoms.table, launch=dict(base, slices=7), fresnel=0,
+                            factor_table=False)
+    ref64 = engine.run_split(tiles, pix, phys, atoms.table, launch=dict(base, slices=64), fresnel=0,
+                             factor_table=False)
     engine.sync()
     ln = MkLaunch(4, 128, 64, 0, int(tiles.amp_is_real()))
     sp = atoms.table.abi()
