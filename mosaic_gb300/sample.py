@@ -71,13 +71,17 @@ class ChunkedSample:
     def chunk_atom_count(self, chunk_number):
         return int(self._chunks[chunk_number - 1][0].shape[0])
 
-    def load_chunk_positions(self, chunk_number, use_gpu=False, raw=False):
+    def load_chunk_positions(self, chunk_number, use_gpu=False, raw=False, copy=True):
+        """The chunk's positions (A), thermally displaced when the sample has
+        a thermal model (unless ``raw``); ``copy=False`` returns the stored
+        array itself when no displacement applies (for readers that do not
+        modify it)."""
         pos = self._chunks[chunk_number - 1][0]
         if self.thermal and not raw:
             t = self.thermal
             return thermal_displacement(pos, t.get("sigma", 0.25), t.get("max_displacement", 1.0),
                                         t.get("seed", 40), chunk_number)
-        return pos.copy()
+        return pos.copy() if copy else pos
 
     def load_chunk_species(self, chunk_number, use_gpu=False, codes=False):
         _, c, labels = self._chunks[chunk_number - 1]
@@ -129,7 +133,8 @@ class DiskSample:
     def chunk_atom_count(self, chunk_number):
         return int(np.load(self._path("atomic_positions", chunk_number), mmap_mode="r").shape[0])
 
-    def load_chunk_positions(self, chunk_number, use_gpu=False, raw=False):
+    def load_chunk_positions(self, chunk_number, use_gpu=False, raw=False, copy=True):
+        # every read is a fresh array: ``copy`` has nothing to do here
         pos = np.load(self._path("atomic_positions", chunk_number))
         if self.thermal and not raw:
             t = self.thermal

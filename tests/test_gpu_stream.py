@@ -1,5 +1,5 @@
-"""Streamed staging (chunks straight into device arrays through pinned
-buffers) and the on-disk sample format, on the GPU."""
+"""Streamed staging (chunks straight into device arrays, copied from their
+own host arrays) and the on-disk sample format, on the GPU."""
 import numpy as np
 import pytest
 import torch
@@ -18,16 +18,26 @@ def _crystal():
     return w, [(pos[a:b], spc[a:b]) for a, b in zip(cut[:-1], cut[1:])]
 
 
-def test_streamed_staging_equals_host_collection(cuda):
+@pytest.mark.parametrize("thermal", [True, False])
+def test_streamed_staging_equals_host_collection(cuda, thermal):
+    """With a thermal model the chunks are fresh arrays; without one the
+    stream reads the sample's stored arrays in place (no copy), which it
+    leaves unchanged."""
     w, chunks = _crystal()
     B = workloads._beam(10000.0, 200.0)
-    s = ChunkedSample(chunks, thermal=dict(sigma=0.08, max_displacement=1.0, seed=40))
+    th = dict(sigma=0.08, max_displacement=1.0, seed=40) if thermal else None
+    s = ChunkedSample(chunks, thermal=th)
+    before = [s.load_chunk_positions(c) for c in range(1, s.chunk_total + 1)]
     pos_h, idx_h, labels_h = B.collect_atoms(s)
-    pos_d, idx_d, labels_d, counts = B.stream_atoms(s, cuda)
-    assert labels_d == labels_h
-    assert torch.equal(pos_d.cpu(), torch.as_tensor(pos_h))
-    assert torch.equal(idx_d.cpu(), torch.as_tensor(idx_h.astype(np.int32)))
-    assert np.array_equal(counts, np.bincount(idx_h, minlength=len(labels_h)))
+    for _ in range(2):      # a second call reuses the loader thread
+        pos_d, idx_d, labels_d, counts = B.stream_atoms(s, cuda)
+        assert labels_d == labels_h
+        assert torch.equal(pos_d.cpu(), torch.as_tensor(pos_h))
+        assert torch.equal(idx_d.cpu(), torch.as_tensor(idx_h.astype(np.int32)))
+        assert np.array_equal(counts, np.bincount(idx_h, minlength=len(labels_h)))
+        assert B.last_stream_bytes > 12 * pos_h.shape[0]
+    for c, p in enumerate(before, start=1):
+        assert np.array_equal(s.load_chunk_positions(c), p)
 
 
 def test_disk_sample_through_the_entry_point(cuda, tmp_path):
