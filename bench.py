@@ -697,6 +697,10 @@ def run_ours(args):
         return
 
     # End to end through the public entry point with host buffers.
+    # one untimed call first (the entry point's first use: its loader
+    # thread, the first touch of the sample's host pages by the copy
+    # engines), then the median of three calls
+    B.atomic_scattering_kinematic(w.sample, w.detector, w.stage, return_double=True, **kw)
     e2e_times = []
     for i in range(max(2, min(3, args.steps))):
         barrier()

@@ -40,7 +40,13 @@ class ChunkedSample:
         thermal: None or dict(sigma=, max_displacement=, seed=) for the
             Gaussian displacement applied on every load.
         dimensions: (Lx, Ly, Lz) in Angstrom (the sample box, informational).
+
+    With a seed the displacement of a chunk is the same on every load, so
+    the displaced positions are kept after the first (``keep_displaced``;
+    they cost one more copy of the positions in host memory).
     """
+
+    keep_displaced = True
 
     def __init__(self, chunks, thermal=None, dimensions=None, directory=""):
         self._chunks = []
@@ -54,6 +60,7 @@ class ChunkedSample:
             if codes.shape[0] != pos.shape[0]:
                 raise ValueError("positions/species size mismatch")
             self._chunks.append((pos, codes, labels))
+        self._displaced = {}
         self.thermal = thermal
         self.directory = directory
         if dimensions is None and self._chunks:
@@ -79,8 +86,14 @@ class ChunkedSample:
         pos = self._chunks[chunk_number - 1][0]
         if self.thermal and not raw:
             t = self.thermal
-            return thermal_displacement(pos, t.get("sigma", 0.25), t.get("max_displacement", 1.0),
-                                        t.get("seed", 40), chunk_number)
+            key = (t.get("sigma", 0.25), t.get("max_displacement", 1.0), t.get("seed", 40))
+            if key[2] is None or not self.keep_displaced:     # fresh entropy on every load
+                return thermal_displacement(pos, *key, chunk_number)
+            kept = self._displaced.get(chunk_number)
+            if kept is None or kept[0] != key:
+                kept = (key, thermal_displacement(pos, *key, chunk_number))
+                self._displaced[chunk_number] = kept
+            return kept[1].copy() if copy else kept[1]
         return pos.copy() if copy else pos
 
     def load_chunk_species(self, chunk_number, use_gpu=False, codes=False):

@@ -64,3 +64,26 @@ def test_label_files_and_bad_codes(tmp_path):
         assert "label table" in str(e)
     else:
         raise AssertionError("codes beyond the label table must raise")
+
+
+def test_seeded_displacements_are_kept_and_unseeded_are_fresh():
+    """A seeded thermal model displaces a chunk the same way on every load,
+    so the displaced positions are kept; they equal thermal_displacement,
+    a caller's copy cannot change them, and an unseeded model draws afresh."""
+    from mosaic_gb300.sample import ChunkedSample, thermal_displacement
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(-20, 20, (500, 3)).astype(np.float32)
+    spc = np.array(["Cu"] * 500)
+    th = dict(sigma=0.1, max_displacement=0.3, seed=7)
+    s = ChunkedSample([(pos, spc), (pos[:200], spc[:200])], thermal=th)
+    a = s.load_chunk_positions(2)
+    want = thermal_displacement(pos[:200], 0.1, 0.3, 7, 2)
+    assert np.array_equal(a, want)
+    a += 1.0                                    # the caller's copy
+    assert np.array_equal(s.load_chunk_positions(2), want)
+    assert np.array_equal(s.load_chunk_positions(2, copy=False), want)
+    assert np.array_equal(s.load_chunk_positions(1, raw=True), pos)
+    s.thermal = dict(th, seed=8)                # another model: drawn again
+    assert np.array_equal(s.load_chunk_positions(2), thermal_displacement(pos[:200], 0.1, 0.3, 8, 2))
+    u = ChunkedSample([(pos, spc)], thermal=dict(sigma=0.1, max_displacement=0.3, seed=None))
+    assert not np.array_equal(u.load_chunk_positions(1), u.load_chunk_positions(1))
