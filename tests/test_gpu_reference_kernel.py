@@ -172,9 +172,11 @@ def test_reference_kernel_speed_on_the_headline_chunk(cuda, ref_gpu):
     atoms = engine.atoms_lab(pos, idx, R, T, table, e0=B._beam_E0_map, grid=B._beam_grid(),
                              device=cuda)
     pix = engine.Pixels(coords / 1e10, ny, nz, phys, device=cuda)
-    su, _ = B.split_setup(engine.Tiles(atoms, B.k, 1024, device=cuda), pix, phys)
-    cfg = engine.grouping_launch(engine.default_launch(su.level), su.level, su.tiles, pix, B.k,
-                                 su.info)
+    # the headline's form: 512-atom tiles, whose default launch is the 4x4
+    # pixel square where the geometry admits it
+    su, _ = B.split_setup(engine.Tiles(atoms, B.k, 512, device=cuda), pix, phys)
+    cfg = engine.grouping_launch(engine.default_launch(su.level, 512), su.level, su.tiles, pix,
+                                 B.k, su.info)
     run = lambda: engine.run_split(su.tiles, pix, phys, table, launch=cfg, fresnel=su.fresnel,
                                    fresnel_radius=su.fresnel_radius)
     run()
