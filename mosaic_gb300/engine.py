@@ -514,16 +514,14 @@ class Tiles:
         self._ws = ws   # keep until the stream has consumed it
 
     def _extents(self):
-        """(largest tile radius, largest origin norm): one read-back per
-        object (its arrays do not change after the build)."""
+        """(largest tile radius, largest origin norm), from the origins read
+        back once per object (its arrays do not change after the build)."""
         if getattr(self, "_ext", None) is None:
             if not self.n_tiles:
                 self._ext = (0.0, 0.0)
             else:
-                o = self.origin[: self.n_tiles]
-                self._ext = tuple(torch.stack([o[:, 3].max(),
-                                               torch.linalg.vector_norm(o[:, :3], dim=1).max()]
-                                              ).tolist())
+                o = origins_host(self)
+                self._ext = (float(o[:, 3].max()), float(np.linalg.norm(o[:, :3], axis=1).max()))
         return self._ext
 
     def max_radius(self):
@@ -697,12 +695,23 @@ def square_bounds(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0):
     return dict(radius_m=radius, cross=rate * r_eff + fixed, **st)
 
 
+def origins_host(tiles):
+    """(n_tiles, 4) float64 tile origins and radii on the host: one
+    read-back per tiles object, which the extents and the fractions of tiles
+    within the pixel-sharing radii all use."""
+    h = getattr(tiles, "_origins_host", None)
+    if h is None:
+        h = (tiles.origin[: tiles.n_tiles].cpu().numpy() if tiles.n_tiles
+             else np.zeros((0, 4), dtype=np.float64))
+        tiles._origins_host = h
+    return h
+
+
 def tile_fraction_within(tiles, radius_m):
     """Fraction of the tiles whose radius is at most ``radius_m``."""
     if not tiles.n_tiles:
         return 1.0
-    r = tiles.origin[: tiles.n_tiles, 3]
-    return float((r <= float(radius_m)).double().mean())
+    return float((origins_host(tiles)[:, 3] <= float(radius_m)).mean())
 
 
 def pixel_grouping(tiles, pix: Pixels, k, budget_rad, fresnel_rad=0.0, analyser=False):
@@ -893,16 +902,14 @@ class TilesView:
         return self._real
 
     def _extents(self):
-        """(largest tile radius, largest origin norm): one read-back per
-        object (its arrays do not change after the build)."""
+        """(largest tile radius, largest origin norm), from the origins read
+        back once per object (its arrays do not change after the build)."""
         if getattr(self, "_ext", None) is None:
             if not self.n_tiles:
                 self._ext = (0.0, 0.0)
             else:
-                o = self.origin[: self.n_tiles]
-                self._ext = tuple(torch.stack([o[:, 3].max(),
-                                               torch.linalg.vector_norm(o[:, :3], dim=1).max()]
-                                              ).tolist())
+                o = origins_host(self)
+                self._ext = (float(o[:, 3].max()), float(np.linalg.norm(o[:, :3], axis=1).max()))
         return self._ext
 
     def max_radius(self):
