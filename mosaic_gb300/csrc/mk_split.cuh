@@ -610,11 +610,12 @@ __device__ __forceinline__ void mk_tile_terms_oct(
 // and inside quad j the quad form applies unchanged. Dropped beyond the
 // quad form: the departure of w over the 16 pixels from a plane, which the
 // host bounds from the FP64 pixel directions against its phase budget. Per
-// atom pair: three dot products (9), the four quad phases (6), four
-// sin/cos, u^2 and v^2 (2), the polynomials (6), the four products of the
-// shared factors (4) and 4 x 8 accumulators (32): ~61 FP32 lane operations
-// per 16 terms (3.8 a term, against 5.4 for octets), with the MUFU doing
-// one sin/cos per 4 terms as in every quad form.
+// atom: three dot products (9), the four quad phases (6), the four sin/cos
+// argument scalings (4), u^2 and v^2 (2), the polynomials (6), the four
+// products of the shared factors (4), 4 x 8 accumulators (32) and the
+// amplitude coefficients (2): 65 FP32 lane operations for 16 terms on tiles
+// that pass the phase straight to the sin/cos (4.1 a term, against 5.4 for
+// octets), with the MUFU doing one sin/cos per 4 terms as in every quad form.
 // acc[j][0..7] = K, R, S, Q (re, im) of quad j, f32x2 over atoms 2q, 2q+1.
 // Unrolled by 8 atom pairs, not 16 as the other forms: held to ~168
 // registers, the square loop ran the 8.19M-atom exposure 3.9 % faster so.
