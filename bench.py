@@ -627,7 +627,7 @@ def run_ours(args):
         raise RuntimeError(f"{args.config}: the split form declines this geometry")
     if args.launch:
         ppt, nt, mode = (int(v) for v in args.launch.split(","))
-        T = sizes[0] if len(sizes) == 1 else (1024 if 1024 in setups else min(setups))
+        T = sizes[0] if len(sizes) == 1 else (512 if 512 in setups else min(setups))
         launch, tune_tbl = dict(pix_per_thread=ppt, threads=nt, slices=0, pairs=mode), []
     elif args.profile:
         T = min(setups)
@@ -822,7 +822,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="nacl_screw_8m")
     ap.add_argument("--tile-atoms", type=int, default=0,
-                    help="atoms per tile (power of two, 128-4096; 0: the beam's default 1024)")
+                    help="atoms per tile (power of two, 128-4096; 0: the beam's default 512)")
     ap.add_argument("--fp64-grid", type=int, default=32,
                     help="side of the edge-to-edge pixel grid the FP64 reference is computed on")
     ap.add_argument("--no-cpu", action="store_true")

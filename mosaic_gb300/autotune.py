@@ -36,7 +36,7 @@ QUAD_CANDIDATES = [(4, 128), (4, 256), (8, 128), (8, 64), (4, 64)]
 OCTET_CANDIDATES = [(8, 128), (8, 256), (8, 64)]
 SQUARE_CANDIDATES = [(16, 128), (16, 192)]
 TILE_SIZES = (512, 1024, 2048)
-DEFAULT_TILE_ATOMS = 1024
+DEFAULT_TILE_ATOMS = engine.DEFAULT_TILE_ATOMS
 DEFAULT = dict(pix_per_thread=4, threads=128, slices=0, pairs=0)
 PROBE_ATOMS = 96 * 1024
 FINALISTS, ROUNDS, FINAL_SCALE = 3, 3, 4

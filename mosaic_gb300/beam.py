@@ -52,7 +52,7 @@ class beam:
         # (the reference's _kernel_phase_tol_rad, Beam.py:1404-1406).
         self._use_fast_kernel = True
         self._kernel_phase_tol_rad = 1e-6
-        self._kernel_tile_atoms = None      # None: autotuned (1024 untuned)
+        self._kernel_tile_atoms = None      # None: autotuned (512 untuned)
         self._kernel_launch = None          # None: autotuned
         # tune tile size and launch shape on the first use of a detector size
         # (as the reference tunes its fast kernel on first use, Beam.py:8871-8940);
@@ -440,7 +440,7 @@ class beam:
 
     def tile_atoms_for(self, n_pix, kind="exposure"):
         """Atoms per tile: ``_kernel_tile_atoms`` when set, else the
-        autotuner's cached choice for this detector size (1024 untuned)."""
+        autotuner's cached choice for this detector size (512 untuned)."""
         if self._kernel_tile_atoms:
             return int(self._kernel_tile_atoms)
         from . import autotune
