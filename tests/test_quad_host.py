@@ -321,3 +321,51 @@ def test_factor_table_admission():
     assert not engine.factor_table_ok(_tiles(2e-9, 6e-8), _flat_pixels(16, 16, 55e-6, 0.05), phys)
     assert not engine.factor_table_ok(_tiles(2e-9, 6e-8), pix, types.SimpleNamespace(remove_forward=1))
     assert not engine.factor_table_ok(types.SimpleNamespace(n_tiles=0), pix, phys)
+
+
+@pytest.mark.parametrize("form", ["octet", "square"])
+@pytest.mark.parametrize("dist,o_max", [(1.0, 6e-8), (0.5, 3e-8), (0.2, 1e-8)])
+def test_group_bound_covers_the_dropped_phase(form, dist, o_max):
+    """The phase the octet (2x4) and square (4x4) forms drop, measured in
+    FP64 on a flat detector for atoms anywhere in tiles of the form's radius
+    at tile origins up to o_max from the sample origin: the kernel's phase
+    model -- the group's mean direction plus the pixel offsets times the
+    means of its quads' within-quad steps, the directions taken to each tile
+    origin -- against the exact 2 pi D.(b - u'(P)) of every pixel, u'(P) the
+    unit vector from the tile origin to the pixel. It stays within the
+    bound's cross term for that radius (``octet_bounds``, ``square_bounds``)."""
+    k = 2 * np.pi / 1.2398e-10
+    kappa = k / (2 * np.pi)
+    p = 55e-6
+    gr, gc = (2, 4) if form == "octet" else (4, 4)
+    bounds = engine.octet_bounds if form == "octet" else engine.square_bounds
+    rng = np.random.default_rng(9)
+    pix = _flat_pixels(16, 16, p, dist, y0=0.4 * dist, z0=0.2 * dist)
+    r = bounds(_tiles(1e-9, o_max), pix, k, 1e-6)["radius_m"]
+    bound = bounds(_tiles(r, o_max), pix, k, 1e-6)["cross"]
+    assert bound <= 1e-6 * (1 + 1e-9)
+    P = pix.xyz.numpy().reshape(16, 16, 3)          # rows x columns x 3
+    b = np.array([1.0, 0.0, 0.0])
+    worst = 0.0
+    for _ in range(6):
+        o = rng.standard_normal(3)
+        o *= o_max * rng.uniform(0.5, 1.0) / np.linalg.norm(o)
+        d = rng.standard_normal((64, 3))
+        d *= (r * rng.uniform(0.0, 1.0, (64, 1)) ** (1 / 3)) / np.linalg.norm(d, axis=1, keepdims=True)
+        U = P - o
+        U /= np.linalg.norm(U, axis=-1, keepdims=True)
+        W = b - U                                   # w of every pixel for this tile
+        for r0 in range(0, 16, gr):
+            for c0 in range(0, 16, gc):
+                S = W[r0:r0 + gr, c0:c0 + gc]       # one octet or square
+                quads = [S[i:i + 2, j:j + 2] for i in range(0, gr, 2) for j in range(0, gc, 2)]
+                nq = len(quads)
+                g = sum((q[0, 1] - q[0, 0]) + (q[1, 1] - q[1, 0]) for q in quads) / (2 * nq)
+                h = sum((q[1, 0] - q[0, 0]) + (q[1, 1] - q[0, 1]) for q in quads) / (2 * nq)
+                mean = S.reshape(-1, 3).mean(0)
+                co = np.arange(gc) - (gc - 1) / 2
+                ro = np.arange(gr) - (gr - 1) / 2
+                model = mean + co[None, :, None] * g + ro[:, None, None] * h
+                diff = (S - model).reshape(-1, 3)
+                worst = max(worst, float(np.abs(2 * np.pi * kappa * d @ diff.T).max()))
+    assert 0.0 < worst <= bound, (worst, bound)
