@@ -33,6 +33,8 @@
 // Atom tiles reach shared memory by 1-D TMA bulk copies (cp.async.bulk),
 // double-buffered on two mbarriers; every wait is bounded (mk_common.cuh).
 #pragma once
+#include <cuda_bf16.h>
+
 #include "mk_common.cuh"
 
 struct MkSplitArgs {
@@ -1070,8 +1072,16 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
     // with it and w rebuilt in the fold they fit three 128-thread blocks per
     // SM (152 registers) instead of two (234); measured +2 % on the 8.19M-atom
     // step, while the 4-pixel kernels (126 registers already) lost 1.4 %.
+    // The square kernels keep a compact state, 12 bytes a pixel: the two
+    // sums as float2 and their Kahan compensations rounded to bfloat16
+    // (8 significant bits of a term already below the sum's last bit, which
+    // keeps the folds' sum good to ~2^-32 relative), so that three blocks fit
+    // an SM with 1024-atom tiles (3 x (48 + 24) KB).
     constexpr bool KS = ((PM == 2 || PM == 3) && PIX == 8) || (PM == 4 && PIX == 16);
-    float4 *s_kahan = reinterpret_cast<float4 *>(s_amp + 2 * T);
+    constexpr bool KC = PM == 4;
+    float4 *s_kahan = reinterpret_cast<float4 *>(s_amp + 2 * T);            // [PIX][NT]
+    float2 *s_kacc = reinterpret_cast<float2 *>(s_amp + 2 * T);             // KC: [PIX][NT]
+    __nv_bfloat162 *s_kcmp = reinterpret_cast<__nv_bfloat162 *>(s_kacc + PIX * NT);
     const int tid = threadIdx.x;
     const uint32_t tile_bytes = (uint32_t)T * (uint32_t)(sizeof(float4) + sizeof(float2));
 
@@ -1131,7 +1141,12 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
             pix[p] = PM == 1 ? pb * (NT * PIX) + 2 * ((p >> 1) * NT + tid) + (p & 1)
                              : pb * (NT * PIX) + p * NT + tid;
             accr[p] = acci[p] = cmpr[p] = cmpi[p] = 0.f;
-            if constexpr (KS) s_kahan[p * NT + tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if constexpr (KC) {
+                s_kacc[p * NT + tid] = make_float2(0.f, 0.f);
+                s_kcmp[p * NT + tid] = __floats2bfloat162_rn(0.f, 0.f);
+            } else if constexpr (KS) {
+                s_kahan[p * NT + tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         }
         // pixels this thread writes (a quad's repeated edge pixel is not)
         unsigned keep = (1u << PIX) - 1u;
@@ -1441,7 +1456,11 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                 const float tr = csr[p] * gr - csi[p] * gi;
                 const float ti = csr[p] * gi + csi[p] * gr;
                 float ar = accr[p], ai = acci[p], kr = cmpr[p], ki = cmpi[p];
-                if constexpr (KS) {
+                if constexpr (KC) {
+                    const float2 a2 = s_kacc[p * NT + tid];
+                    const __nv_bfloat162 c2 = s_kcmp[p * NT + tid];
+                    ar = a2.x; ai = a2.y; kr = __low2float(c2); ki = __high2float(c2);
+                } else if constexpr (KS) {
                     const float4 k4 = s_kahan[p * NT + tid];
                     ar = k4.x; ai = k4.y; kr = k4.z; ki = k4.w;
                 }
@@ -1453,7 +1472,10 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
                 z = ai + y;
                 ki = (z - ai) - y;
                 ai = z;
-                if constexpr (KS) {
+                if constexpr (KC) {
+                    s_kacc[p * NT + tid] = make_float2(ar, ai);
+                    s_kcmp[p * NT + tid] = __floats2bfloat162_rn(kr, ki);
+                } else if constexpr (KS) {
                     s_kahan[p * NT + tid] = make_float4(ar, ai, kr, ki);
                 } else {
                     accr[p] = ar; acci[p] = ai; cmpr[p] = kr; cmpi[p] = ki;
@@ -1462,7 +1484,11 @@ __global__ void __launch_bounds__(NT, (mk_min_blocks<NT, PIX, PM, ANA>()))
         }
 #pragma unroll
         for (int p = 0; p < PIX; ++p) {
-            if constexpr (KS) {
+            if constexpr (KC) {
+                const float2 a2 = s_kacc[p * NT + tid];
+                const __nv_bfloat162 c2 = s_kcmp[p * NT + tid];
+                accr[p] = a2.x; acci[p] = a2.y; cmpr[p] = __low2float(c2); cmpi[p] = __high2float(c2);
+            } else if constexpr (KS) {
                 const float4 k4 = s_kahan[p * NT + tid];
                 accr[p] = k4.x; acci[p] = k4.y; cmpr[p] = k4.z; cmpi[p] = k4.w;
             }

@@ -2,8 +2,8 @@
 // sharing their half differences; 16 pixels a thread, Fresnel/complex
 // variants; no analyser). The square loop is held to 12 warps per SM (~168
 // registers a thread): three 128-thread blocks where their shared memory
-// fits (tiles of up to 512 atoms), else two; 192-thread blocks (two per SM
-// with 1024-atom tiles) are in mk_split_sq192.cu.
+// fits (tiles of up to 1024 atoms with the compact Kahan state), else two;
+// 192-thread blocks (two per SM) are in mk_split_sq192.cu.
 #include "mk_split.cuh"
 
 mk_split_fn mk_pick_sq192(bool fresnel, bool cplx);

@@ -177,14 +177,15 @@ static mk_split_fn mk_pick(int nt, int pix, bool fresnel, bool cplx, int pair, b
     }
 }
 
-// Two tile buffers; 8-pixel quad, octet and square kernels add their
-// per-pixel Kahan state.
+// Two tile buffers; 8-pixel quad and octet kernels add their per-pixel
+// Kahan state (16 bytes a pixel), square kernels their compact one (12).
 static size_t mk_split_smem(int T, const mk_launch *launch)
 {
     size_t b = 128 + (size_t)2 * T * (sizeof(float4) + sizeof(float2));
-    if (((launch->pairs == 2 || launch->pairs == 3) && launch->pix_per_thread == 8) ||
-        (launch->pairs == 4 && launch->pix_per_thread == 16))
+    if ((launch->pairs == 2 || launch->pairs == 3) && launch->pix_per_thread == 8)
         b += sizeof(float4) * (size_t)launch->pix_per_thread * launch->threads;
+    if (launch->pairs == 4 && launch->pix_per_thread == 16)
+        b += (sizeof(float2) + 4) * (size_t)launch->pix_per_thread * launch->threads;
     return b;
 }
 

@@ -305,7 +305,8 @@ def test_square_launch_clamps():
     assert (c["pairs"], c["pix_per_thread"]) == (1, 4)
     assert engine.default_launch(4, 512) == dict(pix_per_thread=16, threads=128, slices=0, pairs=4)
     assert engine.default_launch(4) == engine.default_launch(4, engine.DEFAULT_TILE_ATOMS)
-    assert engine.default_launch(4, 1024) == engine.default_launch(3)
+    assert engine.default_launch(4, 1024)["pairs"] == 4
+    assert engine.default_launch(4, 2048) == engine.default_launch(3)
     a = engine.analyser_launch(dict(pix_per_thread=16, threads=128, pairs=4))
     assert (a["pairs"], a["pix_per_thread"]) == (2, 8)
 
